@@ -1,0 +1,170 @@
+/*
+ * gudni_cuda.h -- C ABI of the GB300 (sm_103a) rasterizer that replaces gudni's
+ * OpenCL raster kernels (generateThresholds, sortThresholds, renderThresholds in
+ * src/Graphics/Gudni/OpenCL/Kernels.cl).
+ *
+ * The host keeps the reference's serialized buffer layout.  Every record below is
+ * byte-compatible with the pile the Haskell host builds, so a host that today hands
+ * those piles to OpenCL hands the same bytes to these entry points.
+ *
+ * Plain C types only: no CUDA or torch types appear in any signature.  A `stream`
+ * argument is a cudaStream_t passed as void* (NULL = the context's own stream).
+ */
+#ifndef GUDNI_CUDA_H
+#define GUDNI_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- records */
+
+/* Slice {start, length}.  Util/Pile.hs:124-143, Kernels.cl:312-315. */
+typedef struct gudni_slice {
+    uint32_t start;
+    uint32_t length;
+} gudni_slice;
+
+/* Shape record, 16 bytes.  tag = substance type (bits 63-62), compound type
+ * (bits 61-60), substance id (bits 59-0); geo_start is in 16-byte units of the
+ * geometry pile; num_strands strands follow back to back.
+ * Raster/Types.hs:159-168, Raster/ShapeInfo.hs:89-99, Kernels.cl:318-324. */
+typedef struct gudni_shape {
+    uint64_t tag;
+    uint32_t geo_start;
+    uint32_t num_strands;
+} gudni_shape;
+
+/* Tile record, 32 bytes.  Raster/Types.hs:176-198, Kernels.cl:335-341. */
+typedef struct gudni_tile_info {
+    int32_t left, top, right, bottom;   /* tile box in pixels */
+    int16_t hdepth, vdepth;             /* log2 width, log2 height */
+    int32_t column_allocation;          /* first column slot of the tile in its job */
+    gudni_slice shapes;                 /* the tile's shapes in the job's shape pile */
+} gudni_tile_info;
+
+/* Picture usage record, 24 bytes.  Figure/Picture.hs:169-205, Kernels.cl:349-354. */
+typedef struct gudni_picture_use {
+    float translate_x, translate_y;
+    int32_t size_x, size_y;
+    int32_t mem_offset;                 /* byte offset into the picture pile */
+    float scale;
+} gudni_picture_use;
+
+/* Radial-gradient record, 48 bytes.  New substance with no counterpart in the
+ * reference (which only has solid colours and pictures): colour = inner + (outer -
+ * inner) * min(1, |p - centre| / radius), p = the integer pixel position, constant
+ * over the pixel like a picture texel.  A substance of this type stores its record
+ * index as a uint32 in the .x lane of its substance colour. */
+typedef struct gudni_radial {
+    float center_x, center_y, radius, pad;
+    float inner[4];
+    float outer[4];
+} gudni_radial;
+
+/* Shape tag bits.  Raster/Constants.hs:74-89. */
+#define GUDNI_TAG_SUBSTANCE_MASK  0xC000000000000000ULL
+#define GUDNI_TAG_SOLID           0x8000000000000000ULL
+#define GUDNI_TAG_PICTURE         0x4000000000000000ULL
+#define GUDNI_TAG_RADIAL          0xC000000000000000ULL /* new substance type */
+#define GUDNI_TAG_COMPOUND_MASK   0x3000000000000000ULL
+#define GUDNI_TAG_CONTINUE        0x1000000000000000ULL
+#define GUDNI_TAG_ADD             0x2000000000000000ULL
+#define GUDNI_TAG_SUBTRACT        0x3000000000000000ULL
+#define GUDNI_TAG_ID_MASK         0x0FFFFFFFFFFFFFFFULL
+
+#define GUDNI_RANDOM_FIELD_SIZE 4096  /* Raster/Constants.hs:68 */
+
+/* Raster specification: the reference's RasterSpec (OpenCL/Rasterizer.hs:37-50) plus
+ * the compile-time knobs it injects as #defines (OpenCL/Setup.hs:45-64). */
+typedef struct gudni_spec {
+    int32_t max_tile_size;          /* specMaxTileSize (power of two) */
+    int32_t threads_per_tile;       /* specThreadsPerTile (power of two, >= max_tile_size) */
+    int32_t max_strands_per_tile;   /* specMaxStrandsPerTile */
+    int32_t max_tiles_per_call;     /* specMaxTilesPerCall */
+    int32_t max_thresholds;         /* MAXTHRESHOLDS: threshold queue capacity per column */
+    int32_t max_shape;              /* MAXSHAPE: shapes per column (<= 64*stack_sections-1) */
+    int32_t stack_sections;         /* SHAPESTACKSECTIONS: 64-bit words of the shape stack */
+    float   stochastic_factor;      /* STOCHASTIC_FACTOR (the reference ships 0.0) */
+} gudni_spec;
+
+/* ----------------------------------------------------------------- status */
+
+#define GUDNI_OK                      0
+#define GUDNI_ERR_BAD_INPUT          -1  /* argument or record out of range */
+#define GUDNI_ERR_THRESHOLD_OVERFLOW -2  /* a column needed more than max_thresholds */
+#define GUDNI_ERR_ITER_LIMIT         -3  /* a device loop hit its iteration cap */
+#define GUDNI_ERR_CUDA               -4  /* a CUDA call failed; see gudni_last_error */
+#define GUDNI_ERR_NO_DEVICE          -5
+#define GUDNI_ERR_NOT_READY          -6  /* common buffers not uploaded */
+#define GUDNI_ERR_OUT_OF_MEMORY      -7
+
+/* ---------------------------------------------------------------- context */
+
+typedef struct gudni_ctx gudni_ctx;
+
+/* Create a rasterizer on CUDA device `device`.  Replaces setupOpenCL
+ * (OpenCL/Setup.hs:102-147): there is no JIT step, the spec's knobs are kernel
+ * arguments / template parameters.  Returns NULL on failure (gudni_last_error(NULL)
+ * then describes why). */
+gudni_ctx* gudni_create(const gudni_spec* spec, int device);
+void gudni_destroy(gudni_ctx* ctx);
+
+/* Last error message for this context (or the last failed gudni_create when ctx is
+ * NULL).  Never NULL. */
+const char* gudni_last_error(const gudni_ctx* ctx);
+
+/* Upload the per-frame buffers shared by all jobs: geometry pile, substance pile
+ * (4 floats each), picture pile, picture usages, radial gradients and the random
+ * field (GUDNI_RANDOM_FIELD_SIZE floats; may be NULL when stochastic_factor is 0).
+ * Replaces the BuffersInCommon set-up of queueRasterJobs (OpenCL/CallKernels.hs:
+ * 208-240).  Host pointers; copies are made before the call returns. */
+int gudni_upload_common(gudni_ctx* ctx,
+                        const void* geometry, size_t geometry_bytes,
+                        const float* substances, size_t n_substances,
+                        const uint8_t* pictures, size_t picture_bytes,
+                        const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                        const gudni_radial* radials, size_t n_radials,
+                        const float* random_field);
+
+/* Rasterize one job: the generateThresholds -> sortThresholds -> renderThresholds
+ * sequence of generateCall (OpenCL/CallKernels.hs:88-179), fused into one launch.
+ * shapes/tiles/out are HOST pointers; `out` receives bitmap_w*bitmap_h BGRA words
+ * (only the job's tiles are written).  Blocks until the pixels are in `out`.
+ * Arguments follow the kernels' argument lists (Kernels.cl:2030-2040, 2117-2132). */
+int gudni_raster_job(gudni_ctx* ctx,
+                     const gudni_shape* shapes, size_t n_shapes,
+                     const gudni_tile_info* tiles, size_t n_tiles,
+                     int32_t columns_to_alloc,
+                     int32_t bitmap_w, int32_t bitmap_h,
+                     int32_t compute_depth, int32_t frame_number, int32_t job_index,
+                     const float background[4],
+                     uint32_t* out);
+
+/* Same as gudni_raster_job with DEVICE pointers for shapes, tiles and out, enqueued
+ * on `stream` without synchronising.  Errors found on the device are reported by the
+ * next gudni_sync_status on this context. */
+int gudni_raster_job_device(gudni_ctx* ctx,
+                            const gudni_shape* shapes, size_t n_shapes,
+                            const gudni_tile_info* tiles, size_t n_tiles,
+                            int32_t columns_to_alloc,
+                            int32_t bitmap_w, int32_t bitmap_h,
+                            int32_t compute_depth, int32_t frame_number, int32_t job_index,
+                            const float background[4],
+                            uint32_t* out, void* stream);
+
+/* Wait for the context's stream and return the accumulated device status
+ * (GUDNI_OK or the first error raised by a kernel since the last call). */
+int gudni_sync_status(gudni_ctx* ctx);
+
+/* Device bytes of threshold scratch the context holds right now. */
+size_t gudni_scratch_bytes(const gudni_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GUDNI_CUDA_H */

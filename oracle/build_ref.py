@@ -1,0 +1,109 @@
+"""ORACLE -- test infrastructure only.
+
+Build recipe for oracle/_ref/: the reference's own OpenCL kernels
+(src/Graphics/Gudni/OpenCL/Kernels.cl, read where it lies under the reference
+checkout) compiled for the CPU as C++, to pin the restatement in
+oracle/raster_oracle.cpp.
+
+Steps, all mechanical:
+  1. Replace the file's first 40 lines with the #define block the reference host
+     injects at JIT time (OpenCL/Setup.hs:45-64, CppDefines.hs:66-70), preceded by
+     the OpenCL-C shim (oracle/ref_shim.h).  MAXSHAPE and SHAPESTACKSECTIONS are
+     compile-time constants as in the reference; MAXTHRESHOLDS becomes a runtime
+     capacity (it only sizes the per-column slabs).
+  2. Rewrite OpenCL vector literals `(float4)(a, b, ...)` into calls of the shim's
+     constructor `ocl_make<float4>(a, b, ...)` (C++ would read them as casts of a
+     comma expression).
+  3. Append the host driver oracle/ref_driver.inc and compile with g++.
+
+Outputs go to oracle/_ref/ only (git-ignored).  Nothing in the package imports this.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_ref")
+DEFAULT_REFERENCE = "/root/reference"
+KERNELS_REL = os.path.join("src", "Graphics", "Gudni", "OpenCL", "Kernels.cl")
+SOURCE_PADDING = 40  # sOURCEfILEpADDING, Raster/Constants.hs:70
+
+VECTOR_LITERAL = re.compile(
+    r"\(\s*(float2|float4|float8|int2|int4|uchar4|COLOR|SPACE2|SPACE4|THRESHOLD)\s*\)\s*\(")
+
+
+def defines(max_shape: int, sections: int, stochastic: float) -> list[str]:
+    """The #define list of cppDefines (OpenCL/Setup.hs:45-64)."""
+    return [
+        f"#define STOCHASTIC_FACTOR {stochastic!r}",
+        "#define RANDOMFIELDSIZE 4096",
+        "#define MAXTHRESHOLDS (gudni_ref_max_thresholds)",
+        f"#define MAXSHAPE {max_shape}",
+        f"#define SHAPESTACKSECTIONS {sections}",
+        "#define SHAPETAG_SUBSTANCETYPE_BITMASK 0xC000000000000000",
+        "#define SHAPETAG_SUBSTANCETYPE_SOLIDCOLOR 0x8000000000000000",
+        "#define SHAPETAG_SUBSTANCETYPE_PICTURE 0x4000000000000000",
+        "#define SHAPETAG_SUBSTANCETYPE_SHIFT 30",
+        "#define SHAPETAG_COMPOUNDTYPE_BITMASK 0x3000000000000000",
+        "#define SHAPETAG_COMPOUNDTYPE_CONTINUE 0x1000000000000000",
+        "#define SHAPETAG_COMPOUNDTYPE_ADD 0x2000000000000000",
+        "#define SHAPETAG_COMPOUNDTYPE_SUBTRACT 0x3000000000000000",
+        "#define SHAPETAG_COMPOUNDTYPE_SHIFT 28",
+        "#define SHAPETAG_SUBSTANCEID_BITMASK 0x0FFFFFFFFFFFFFFF",
+    ]
+
+
+def library_name(max_shape: int, sections: int) -> str:
+    return os.path.join(OUT_DIR, f"libgudni_ref_m{max_shape}_s{sections}.so")
+
+
+def generate(reference: str, max_shape: int, sections: int, stochastic: float = 0.0) -> str:
+    src_path = os.path.join(reference, KERNELS_REL)
+    with open(src_path, "r") as f:
+        lines = f.read().split("\n")
+    head = ['#include "ref_shim.h"'] + defines(max_shape, sections, stochastic)
+    head += ["// padding"] * max(0, SOURCE_PADDING - len(head))
+    body = "\n".join(lines[SOURCE_PADDING:])
+    body = VECTOR_LITERAL.sub(lambda m: f"ocl_make<{m.group(1)}>(", body)
+    text = "\n".join(head) + "\n" + body + '\n#include "ref_driver.inc"\n'
+    os.makedirs(OUT_DIR, exist_ok=True)
+    out = os.path.join(OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp")
+    with open(out, "w") as f:
+        f.write(text)
+    return out
+
+
+def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: int = 8,
+          force: bool = False) -> str | None:
+    """Build the reference kernels for one (MAXSHAPE, SHAPESTACKSECTIONS) pair.
+    Returns the library path, or None when the reference checkout is absent."""
+    lib = library_name(max_shape, sections)
+    if not os.path.isfile(os.path.join(reference, KERNELS_REL)):
+        return lib if os.path.isfile(lib) else None
+    if os.path.isfile(lib) and not force:
+        return lib
+    cpp = generate(reference, max_shape, sections)
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
+           "-fPIC", "-shared", "-w", "-I", HERE, cpp, "-o", lib]
+    subprocess.run(cmd, check=True)
+    return lib
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--reference", default=DEFAULT_REFERENCE)
+    ap.add_argument("--max-shape", type=int, default=127)
+    ap.add_argument("--sections", type=int, default=8)
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args(argv)
+    lib = build(a.reference, a.max_shape, a.sections, a.force)
+    print(lib if lib else "reference checkout not found; nothing built")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,127 @@
+"""ORACLE -- test infrastructure only.
+
+Python driver of the CPU restatement of gudni's raster kernels
+(oracle/raster_oracle.cpp) and of the reference's own Kernels.cl compiled for the CPU
+(oracle/_ref/, made by oracle/build_ref.py when the reference checkout is present).
+
+Only tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module,
+and only as the checker / baseline: the product path never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libgudni_oracle.so")
+SRC = os.path.join(HERE, "raster_oracle.cpp")
+HDR = os.path.join(ROOT, "include", "gudni_cuda.h")
+
+
+def build(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.isfile(LIB) or max(os.path.getmtime(SRC), os.path.getmtime(HDR)) > os.path.getmtime(LIB):
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
+               "-fPIC", "-shared", SRC, "-o", LIB]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+class OracleStats(C.Structure):
+    _fields_ = [("max_queue", C.c_int64), ("thresholds", C.c_int64), ("sections", C.c_int64),
+                ("max_shape_bits", C.c_int64), ("overflow", C.c_int64)]
+
+
+_lib = None
+_ref_libs: dict = {}
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(build())
+        vp = C.c_void_p
+        lib.oracle_raster_job.restype = C.c_int
+        lib.oracle_raster_job.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_float,
+                                          vp, C.c_int, C.POINTER(OracleStats)]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if (a is not None and a.size) else None
+
+
+def render_frame(frame, n_threads: int = 0, max_thresholds: Optional[int] = None,
+                 stats: Optional[dict] = None) -> np.ndarray:
+    """Rasterize a serialized frame on the CPU; returns (H, W) uint32 BGRA words.
+    Pixels no job writes stay 0."""
+    lib = _load()
+    spec = frame.spec
+    out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
+    maxt = max_thresholds or spec.max_thresholds
+    agg = {"max_queue": 0, "thresholds": 0, "sections": 0, "max_shape_bits": 0, "overflow": 0}
+    bg = np.ascontiguousarray(frame.background, dtype=np.float32)
+    for ji, job in enumerate(frame.jobs):
+        st = OracleStats()
+        lib.oracle_raster_job(_p(frame.geometry), _p(frame.substances), _p(frame.pictures), _p(frame.picture_uses),
+                              _p(frame.radials), _p(frame.random_field), _p(job.shapes), _p(job.tiles),
+                              len(job.tiles), spec.threads_per_tile, frame.compute_depth, frame.canvas_w,
+                              frame.canvas_h, 0, ji, _p(bg), maxt, spec.max_shape, spec.stack_sections,
+                              spec.stochastic_factor, _p(out), n_threads, C.byref(st))
+        agg["max_queue"] = max(agg["max_queue"], st.max_queue)
+        agg["thresholds"] += st.thresholds
+        agg["sections"] += st.sections
+        agg["max_shape_bits"] = max(agg["max_shape_bits"], st.max_shape_bits)
+        agg["overflow"] |= st.overflow
+    if stats is not None:
+        stats.update(agg)
+    return out
+
+
+def ref_available(max_shape: int = 127, sections: int = 8) -> bool:
+    from . import build_ref
+    return os.path.isfile(build_ref.library_name(max_shape, sections)) or os.path.isfile(
+        os.path.join(build_ref.DEFAULT_REFERENCE, build_ref.KERNELS_REL))
+
+
+def _load_ref(max_shape: int, sections: int):
+    key = (max_shape, sections)
+    if key not in _ref_libs:
+        from . import build_ref
+        path = build_ref.build(max_shape=max_shape, sections=sections)
+        if path is None or not os.path.isfile(path):
+            raise FileNotFoundError("reference kernels not built (no reference checkout)")
+        lib = C.CDLL(path)
+        vp, sz = C.c_void_p, C.c_size_t
+        lib.gudni_ref_raster_job.restype = C.c_int
+        lib.gudni_ref_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, vp, sz, vp, C.c_int, C.c_int,
+                                             C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, vp,
+                                             C.c_int]
+        _ref_libs[key] = lib
+    return _ref_libs[key]
+
+
+def ref_render_frame(frame, max_thresholds: int, n_threads: int = 0) -> np.ndarray:
+    """Rasterize with the reference's own Kernels.cl (compiled for the CPU)."""
+    spec = frame.spec
+    lib = _load_ref(spec.max_shape, spec.stack_sections)
+    out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
+    bg = np.ascontiguousarray(frame.background, dtype=np.float32)
+    for ji, job in enumerate(frame.jobs):
+        rc = lib.gudni_ref_raster_job(_p(frame.geometry), frame.geometry.size, _p(frame.substances),
+                                      len(frame.substances), _p(frame.pictures), frame.pictures.size,
+                                      _p(frame.picture_uses), len(frame.picture_uses), _p(frame.random_field),
+                                      _p(job.shapes), len(job.shapes), _p(job.tiles), len(job.tiles),
+                                      spec.threads_per_tile, frame.compute_depth, frame.canvas_w,
+                                      frame.canvas_h, 0, ji, _p(bg), max_thresholds, _p(out), n_threads)
+        if rc != 0:
+            raise RuntimeError(f"reference kernels failed: {rc}")
+    return out
