@@ -1,0 +1,442 @@
+// C ABI of the raster path (include/gudni_cuda.h).
+//
+// A context owns its device, stream, the uploaded common buffers, per-job staging
+// buffers and the threshold scratch.  Scratch is sized for the resident grid
+// (SMs x resident blocks x block), not for the job: each resident thread reuses one
+// slot for every column it runs.  This replaces the reference's per-job allocation of
+// columns x MAXTHRESHOLDS thresholds (OpenCL/CallKernels.hs:124-127).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "gudni_cuda.h"
+#include "raster_kernels.h"
+
+using gudni::ColumnLaunch;
+
+namespace {
+
+std::mutex g_create_mutex;
+std::string g_create_error;
+
+template <class T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t reserve(size_t n) {
+    if (n <= cap && ptr) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct gudni_ctx {
+  gudni_spec spec;
+  int device = 0;
+  int sm_count = 0;
+  int sections = 1;
+  int blocks_per_sm = 1;
+  int grid = 1;
+  int working_capacity = 256;
+  cudaStream_t stream = nullptr;
+  std::string error;
+
+  // common buffers (BuffersInCommon)
+  bool common_ready = false;
+  DevBuf<uint8_t> geometry;
+  size_t geometry_bytes = 0;
+  DevBuf<float4> substances;
+  size_t n_substances = 0;
+  DevBuf<uint8_t> pictures;
+  size_t picture_bytes = 0;
+  DevBuf<gudni_picture_use> uses;
+  size_t n_uses = 0;
+  DevBuf<gudni_radial> radials;
+  size_t n_radials = 0;
+  DevBuf<float> random_field;
+  bool has_random = false;
+
+  // per-job staging
+  DevBuf<gudni_shape> shapes;
+  DevBuf<gudni_tile_info> tiles;
+  DevBuf<uint32_t> out;
+
+  // scratch: fast pass (grid slots x working capacity), fallback (list x max_thresholds)
+  DevBuf<float4> thr;
+  DevBuf<uint32_t> hdr;
+  DevBuf<uint32_t> idx;
+  DevBuf<float4> big_thr;
+  DevBuf<uint32_t> big_hdr;
+  DevBuf<uint32_t> big_idx;
+  DevBuf<uint32_t> overflow_items;
+  DevBuf<uint32_t> overflow_count;
+  DevBuf<int> status;
+  DevBuf<int64_t> counters;
+  int pending_status = 0;
+  cudaStream_t last_stream = nullptr;  // stream of the last enqueued job
+};
+
+namespace {
+
+int fail(gudni_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->error = msg;
+  return code;
+}
+
+int cuda_fail(gudni_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, GUDNI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int status_to_code(int bits) {
+  if (bits & gudni::kStatusBadInput) return GUDNI_ERR_BAD_INPUT;
+  if (bits & gudni::kStatusOverflow) return GUDNI_ERR_THRESHOLD_OVERFLOW;
+  if (bits & gudni::kStatusIterLimit) return GUDNI_ERR_ITER_LIMIT;
+  return GUDNI_OK;
+}
+
+const char* status_message(int bits) {
+  if (bits & gudni::kStatusBadInput) return "a shape, strand, substance or picture record points outside its buffer";
+  if (bits & gudni::kStatusOverflow) return "a column needed more thresholds than max_thresholds";
+  if (bits & gudni::kStatusIterLimit) return "a device loop hit its iteration cap";
+  return "";
+}
+
+bool valid_spec(const gudni_spec* s, std::string& why) {
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (!s) { why = "null spec"; return false; }
+  if (!pow2(s->threads_per_tile) || s->threads_per_tile > (1 << 20)) { why = "threads_per_tile must be a power of two"; return false; }
+  if (s->max_thresholds < 4) { why = "max_thresholds must be >= 4"; return false; }
+  if (s->max_shape < 1 || s->max_shape > 64 * 32 - 1) { why = "max_shape must be in [1, 2047]"; return false; }
+  if (s->stack_sections < 1 || s->max_shape > 64 * s->stack_sections - 1) {
+    why = "max_shape must be <= 64*stack_sections-1";
+    return false;
+  }
+  if (!(s->stochastic_factor == s->stochastic_factor)) { why = "stochastic_factor is NaN"; return false; }
+  return true;
+}
+
+int ensure_scratch(gudni_ctx* ctx) {
+  const size_t slots = (size_t)ctx->grid * gudni::kRasterBlock;
+  const size_t cap = (size_t)ctx->working_capacity;
+  cudaError_t e;
+  if ((e = ctx->thr.reserve(slots * cap)) != cudaSuccess) return cuda_fail(ctx, e, "scratch thresholds");
+  if ((e = ctx->hdr.reserve(slots * cap)) != cudaSuccess) return cuda_fail(ctx, e, "scratch headers");
+  if ((e = ctx->idx.reserve(slots * (size_t)ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "scratch shape indices");
+  if ((e = ctx->status.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "status word");
+  if ((e = ctx->overflow_count.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
+  if ((e = ctx->counters.reserve(4)) != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  return GUDNI_OK;
+}
+
+int validate_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes, const gudni_tile_info* tiles,
+                 size_t n_tiles, int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth, bool host) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!ctx->common_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "gudni_upload_common has not been called");
+  if (bitmap_w <= 0 || bitmap_h <= 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "bitmap size must be positive");
+  if ((int64_t)bitmap_w * bitmap_h > (int64_t)1 << 31) return fail(ctx, GUDNI_ERR_BAD_INPUT, "bitmap too large");
+  if (compute_depth < 0 || compute_depth > 20 || (1 << compute_depth) != ctx->spec.threads_per_tile)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "compute_depth must be log2(threads_per_tile)");
+  if (n_tiles > 0 && !tiles) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null tiles");
+  if (n_shapes > 0 && !shapes) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null shapes");
+  if ((uint64_t)n_tiles * (uint64_t)ctx->spec.threads_per_tile >= (1ull << 32))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many work items in one job");
+  if (host) {
+    for (size_t i = 0; i < n_tiles; ++i) {
+      const gudni_tile_info& t = tiles[i];
+      if ((uint64_t)t.shapes.start + t.shapes.length > n_shapes || t.hdepth < 0 || t.hdepth > 24 ||
+          t.vdepth < 0 || t.vdepth > 24 || t.left < 0 || t.top < 0)
+        return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(i) + " is malformed");
+    }
+  }
+  return GUDNI_OK;
+}
+
+gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n_shapes,
+                           const gudni_tile_info* d_tiles, size_t n_tiles, int32_t bitmap_w, int32_t bitmap_h,
+                           int32_t compute_depth, int32_t job_index, const float background[4], uint32_t* d_out) {
+  gudni::RasterInputs in;
+  in.geometry = ctx->geometry.ptr;
+  in.geometry_bytes = ctx->geometry_bytes;
+  in.substances = ctx->substances.ptr;
+  in.n_substances = (uint32_t)ctx->n_substances;
+  in.pictures = ctx->pictures.ptr;
+  in.picture_bytes = ctx->picture_bytes;
+  in.uses = ctx->uses.ptr;
+  in.n_uses = (uint32_t)ctx->n_uses;
+  in.radials = ctx->radials.ptr;
+  in.n_radials = (uint32_t)ctx->n_radials;
+  in.random_field = ctx->has_random ? ctx->random_field.ptr : nullptr;
+  in.stochastic = ctx->spec.stochastic_factor;
+  in.shapes = d_shapes;
+  in.n_shapes = (uint32_t)n_shapes;
+  in.tiles = d_tiles;
+  in.n_tiles = (int)n_tiles;
+  in.log2_tpt = compute_depth;
+  in.bitmap_w = bitmap_w;
+  in.bitmap_h = bitmap_h;
+  in.job_index = job_index;
+  in.background = make_float4(background[0], background[1], background[2], background[3]);
+  in.max_shape = ctx->spec.max_shape;
+  in.out = d_out;
+  return in;
+}
+
+// Enqueue the fast pass; `sync_fallback` then reads the overflow count and runs the
+// full-capacity pass over the recorded columns.
+int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, cudaStream_t stream) {
+  int rc = ensure_scratch(ctx);
+  if (rc) return rc;
+  const uint32_t n_items = (uint32_t)(n_tiles * (size_t)ctx->spec.threads_per_tile);
+  cudaError_t e;
+  if ((e = ctx->overflow_items.reserve(std::max<uint32_t>(n_items, 1))) != cudaSuccess)
+    return cuda_fail(ctx, e, "overflow list");
+  if ((e = cudaMemsetAsync(ctx->overflow_count.ptr, 0, sizeof(uint32_t), stream)) != cudaSuccess)
+    return cuda_fail(ctx, e, "memset");
+  if (n_items == 0) return GUDNI_OK;
+  ColumnLaunch a;
+  a.in = in;
+  a.scratch = gudni::ColumnScratch{ctx->thr.ptr, ctx->hdr.ptr, ctx->idx.ptr, ctx->working_capacity,
+                                   ctx->spec.max_shape};
+  a.items = nullptr;
+  a.n_items = n_items;
+  const bool fast_is_full = ctx->working_capacity >= ctx->spec.max_thresholds;
+  a.overflow_items = fast_is_full ? nullptr : ctx->overflow_items.ptr;
+  a.overflow_cap = n_items;
+  a.overflow_count = ctx->overflow_count.ptr;
+  a.status = ctx->status.ptr;
+  a.section_counter = nullptr;
+  const uint32_t blocks_needed = (n_items + gudni::kRasterBlock - 1) / gudni::kRasterBlock;
+  const int grid = (int)std::min<uint32_t>(blocks_needed, (uint32_t)ctx->grid);
+  if ((e = gudni::launch_columns(a, ctx->sections, grid, stream)) != cudaSuccess)
+    return cuda_fail(ctx, e, "raster launch");
+  return GUDNI_OK;
+}
+
+int run_fallback(gudni_ctx* ctx, const gudni::RasterInputs& in, cudaStream_t stream) {
+  uint32_t count = 0;
+  cudaError_t e = cudaMemcpyAsync(&count, ctx->overflow_count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
+  if (count == 0) return GUDNI_OK;
+  // slots for the full-capacity pass: bounded so the pass holds at most ~2 GB
+  const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
+  size_t slots = std::max<size_t>(gudni::kRasterBlock, ((size_t)2 << 30) / per_slot);
+  slots = std::min<size_t>(slots, ((size_t)count + gudni::kRasterBlock - 1) / gudni::kRasterBlock * gudni::kRasterBlock);
+  slots = (slots / gudni::kRasterBlock) * gudni::kRasterBlock;
+  if ((e = ctx->big_thr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_hdr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_idx.reserve(slots * ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  ColumnLaunch a;
+  a.in = in;
+  a.scratch = gudni::ColumnScratch{ctx->big_thr.ptr, ctx->big_hdr.ptr, ctx->big_idx.ptr, ctx->spec.max_thresholds,
+                                   ctx->spec.max_shape};
+  a.items = ctx->overflow_items.ptr;
+  a.n_items = count;
+  a.overflow_items = nullptr;
+  a.overflow_cap = 0;
+  a.overflow_count = nullptr;
+  a.status = ctx->status.ptr;
+  a.section_counter = nullptr;
+  if ((e = gudni::launch_columns(a, ctx->sections, (int)(slots / gudni::kRasterBlock), stream)) != cudaSuccess)
+    return cuda_fail(ctx, e, "fallback launch");
+  return GUDNI_OK;
+}
+
+int read_status(gudni_ctx* ctx, cudaStream_t stream) {
+  int bits = 0;
+  cudaError_t e = cudaMemcpyAsync(&bits, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "status read");
+  bits |= ctx->pending_status;
+  ctx->pending_status = 0;
+  if (bits) return fail(ctx, status_to_code(bits), status_message(bits));
+  return GUDNI_OK;
+}
+
+template <class T>
+int upload(gudni_ctx* ctx, DevBuf<T>& buf, const void* src, size_t count, const char* what) {
+  cudaError_t e = buf.reserve(count);
+  if (e == cudaSuccess && count) e = cudaMemcpyAsync(buf.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, what);
+  return GUDNI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gudni_ctx* gudni_create(const gudni_spec* spec, int device) {
+  std::lock_guard<std::mutex> lock(g_create_mutex);
+  std::string why;
+  if (!valid_spec(spec, why)) {
+    g_create_error = "invalid spec: " + why;
+    return nullptr;
+  }
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  if (device < 0 || device >= n) {
+    g_create_error = "device index out of range";
+    return nullptr;
+  }
+  gudni_ctx* ctx = new gudni_ctx();
+  ctx->spec = *spec;
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    g_create_error = std::string("CUDA setup failed: ") + cudaGetErrorString(e);
+    delete ctx;
+    return nullptr;
+  }
+  ctx->sections = gudni::sections_for(spec->max_shape);
+  if ((e = gudni::columns_occupancy(ctx->sections, &ctx->blocks_per_sm)) != cudaSuccess || ctx->blocks_per_sm < 1)
+    ctx->blocks_per_sm = 1;
+  ctx->grid = ctx->sm_count * ctx->blocks_per_sm;
+  ctx->working_capacity = std::min(spec->max_thresholds, 256);
+  if (const char* env = std::getenv("GUDNI_WORKING_CAPACITY")) {
+    int v = std::atoi(env);
+    if (v >= 4) ctx->working_capacity = std::min(spec->max_thresholds, v);
+  }
+  return ctx;
+}
+
+void gudni_destroy(gudni_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->geometry.release(); ctx->substances.release(); ctx->pictures.release(); ctx->uses.release();
+  ctx->radials.release(); ctx->random_field.release(); ctx->shapes.release(); ctx->tiles.release();
+  ctx->out.release(); ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release();
+  ctx->big_hdr.release(); ctx->big_idx.release(); ctx->overflow_items.release();
+  ctx->overflow_count.release(); ctx->status.release(); ctx->counters.release();
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* gudni_last_error(const gudni_ctx* ctx) {
+  if (!ctx) return g_create_error.c_str();
+  return ctx->error.c_str();
+}
+
+int gudni_upload_common(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
+                        size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                        const gudni_picture_use* picture_uses, size_t n_picture_uses, const gudni_radial* radials,
+                        size_t n_radials, const float* random_field) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  if ((geometry_bytes && !geometry) || (n_substances && !substances) || (picture_bytes && !pictures) ||
+      (n_picture_uses && !picture_uses) || (n_radials && !radials))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null buffer with non-zero size");
+  if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
+  for (size_t i = 0; i < n_picture_uses; ++i) {
+    const gudni_picture_use& u = picture_uses[i];
+    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 ||
+        (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
+  }
+  ctx->common_ready = false;
+  int rc;
+  if ((rc = upload(ctx, ctx->geometry, geometry, geometry_bytes, "geometry upload"))) return rc;
+  if ((rc = upload(ctx, ctx->substances, substances, n_substances, "substance upload"))) return rc;
+  if ((rc = upload(ctx, ctx->pictures, pictures, picture_bytes, "picture upload"))) return rc;
+  if ((rc = upload(ctx, ctx->uses, picture_uses, n_picture_uses, "picture use upload"))) return rc;
+  if ((rc = upload(ctx, ctx->radials, radials, n_radials, "radial upload"))) return rc;
+  ctx->has_random = random_field != nullptr;
+  if (random_field && (rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload"))) return rc;
+  ctx->geometry_bytes = geometry_bytes;
+  ctx->n_substances = n_substances;
+  ctx->picture_bytes = picture_bytes;
+  ctx->n_uses = n_picture_uses;
+  ctx->n_radials = n_radials;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "upload");
+  ctx->common_ready = true;
+  return GUDNI_OK;
+}
+
+int gudni_raster_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes, const gudni_tile_info* tiles,
+                     size_t n_tiles, int32_t columns_to_alloc, int32_t bitmap_w, int32_t bitmap_h,
+                     int32_t compute_depth, int32_t frame_number, int32_t job_index, const float background[4],
+                     uint32_t* out) {
+  (void)columns_to_alloc;
+  (void)frame_number;
+  int rc = validate_job(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, true);
+  if (rc) return rc;
+  if (!out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null out or background");
+  cudaSetDevice(ctx->device);
+  const size_t pixels = (size_t)bitmap_w * (size_t)bitmap_h;
+  if ((rc = upload(ctx, ctx->shapes, shapes, n_shapes, "shape upload"))) return rc;
+  if ((rc = upload(ctx, ctx->tiles, tiles, n_tiles, "tile upload"))) return rc;
+  // pixels outside this job's tiles keep the caller's values (the reference reads
+  // the whole target back through a host-pointer buffer, Instances.hs:60-75)
+  if ((rc = upload(ctx, ctx->out, out, pixels, "bitmap upload"))) return rc;
+  gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, n_shapes, ctx->tiles.ptr, n_tiles, bitmap_w, bitmap_h,
+                                  compute_depth, job_index, background, ctx->out.ptr);
+  if ((rc = enqueue_job(ctx, in, n_tiles, ctx->stream))) return rc;
+  if ((rc = run_fallback(ctx, in, ctx->stream))) return rc;
+  cudaError_t e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
+  return read_status(ctx, ctx->stream);
+}
+
+int gudni_raster_job_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes, const gudni_tile_info* tiles,
+                            size_t n_tiles, int32_t columns_to_alloc, int32_t bitmap_w, int32_t bitmap_h,
+                            int32_t compute_depth, int32_t frame_number, int32_t job_index,
+                            const float background[4], uint32_t* out, void* stream) {
+  (void)columns_to_alloc;
+  (void)frame_number;
+  int rc = validate_job(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, false);
+  if (rc) return rc;
+  if (!out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null out or background");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth,
+                                  job_index, background, out);
+  if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
+  if (ctx->working_capacity < ctx->spec.max_thresholds) {
+    if ((rc = run_fallback(ctx, in, s))) return rc;
+  }
+  return GUDNI_OK;
+}
+
+int gudni_sync_status(gudni_ctx* ctx) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  if (ctx->last_stream && ctx->last_stream != ctx->stream) {
+    cudaError_t e = cudaStreamSynchronize(ctx->last_stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream sync");
+  }
+  return read_status(ctx, ctx->stream);
+}
+
+size_t gudni_scratch_bytes(const gudni_ctx* ctx) {
+  if (!ctx) return 0;
+  return ctx->thr.cap * sizeof(float4) + ctx->hdr.cap * 4 + ctx->idx.cap * 4 + ctx->big_thr.cap * sizeof(float4) +
+         ctx->big_hdr.cap * 4 + ctx->big_idx.cap * 4;
+}
+
+}  // extern "C"

@@ -1,0 +1,656 @@
+// Device-side column machine of the raster path (sm_103a).
+//
+// One "column" is the reference's work item: the 1-pixel-wide slab of one tile that
+// one OpenCL work-item renders (initTileState, Kernels.cl:1692-1718).  Per column the
+// machine generates thresholds (generateThresholds, K:2030-2082), orders them
+// (sortThresholds, K:2084-2115) and scans them into pixels (renderThresholds,
+// K:2117-2167).  The arithmetic is the reference's, operation for operation, in IEEE
+// single precision (the library is built with --fmad=false and IEEE division and
+// square root), so results are bit-identical to the reference kernels evaluated with
+// IEEE semantics.
+//
+// Ordering: instead of a bubble sort after generation, each threshold is inserted
+// into its sorted place as it is generated (the reference's own insertThreshold,
+// K:1105-1124).  Both produce the unique stable order of the comparator K:1940-1951
+// over the reversed push order, so the queue the render scan sees is identical.
+//
+// Safety: every loop is bounded; strand, shape, substance and picture reads are
+// bounds-checked against the uploaded buffers; violations set a status bit and skip
+// the read instead of faulting.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "gudni_cuda.h"
+
+namespace gudni {
+
+// status bits raised by kernels (mapped to GUDNI_ERR_* by the host)
+constexpr int kStatusOverflow = 1;   // a column needed more than max_thresholds
+constexpr int kStatusIterLimit = 2;  // a bounded loop hit its cap
+constexpr int kStatusBadInput = 4;   // a record pointed outside its buffer
+
+constexpr float kMinCrop = 0.2f;            // MINCROP K:47
+constexpr float kLeft = 0.0f;               // LEFTBORDER K:90
+constexpr float kRight = 1.0f;              // RIGHTBORDER K:91
+constexpr float kFlatness = 0.25f;          // TAXICAB_FLATNESS K:250
+constexpr float kHalf = 0.5f;               // T K:249
+constexpr int kLargePrime = 7919;           // K:83
+constexpr int kBifurcateCap = 96;           // halvings of a quadratic before giving up
+constexpr int kSectionCap = 1 << 22;        // sections per pixel before giving up
+
+constexpr uint32_t kPositive = 0x80000000u;
+constexpr uint32_t kPersistSlopeMask = 0xC0000000u;
+constexpr uint32_t kPersistTop = 0xC0000000u;
+constexpr uint32_t kPersistBottom = 0x40000000u;
+constexpr uint32_t kPersist = 0x40000000u;
+constexpr uint32_t kUnpersist = 0xBFFFFFFFu;
+constexpr uint32_t kShapeBitMask = 0x0FFFFFFFu;
+
+// Everything a column reads.  Device pointers.
+struct RasterInputs {
+  const uint8_t* geometry;       // strand heap
+  size_t geometry_bytes;
+  const float4* substances;
+  uint32_t n_substances;
+  const uint8_t* pictures;
+  size_t picture_bytes;
+  const gudni_picture_use* uses;
+  uint32_t n_uses;
+  const gudni_radial* radials;
+  uint32_t n_radials;
+  const float* random_field;     // may be null when stochastic == 0
+  float stochastic;
+  const gudni_shape* shapes;     // job shape pile
+  uint32_t n_shapes;
+  const gudni_tile_info* tiles;  // job tile pile
+  int n_tiles;
+  int log2_tpt;                  // computeDepth
+  int bitmap_w, bitmap_h;
+  int job_index;
+  float4 background;
+  int max_shape;
+  uint32_t* out;                 // bitmap_w * bitmap_h BGRA words
+};
+
+__device__ __forceinline__ float cl_min(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float cl_max(float x, float y) { return x < y ? y : x; }
+__device__ __forceinline__ float cl_fmin(float x, float y) {
+  return isnan(y) ? x : (isnan(x) ? y : cl_min(x, y));
+}
+__device__ __forceinline__ float cl_fmax(float x, float y) {
+  return isnan(y) ? x : (isnan(x) ? y : cl_max(x, y));
+}
+
+__device__ __forceinline__ bool hPositive(uint32_t h) { return (h & kPositive) != 0; }
+__device__ __forceinline__ bool hPersistTop(uint32_t h) { return (h & kPersistSlopeMask) == kPersistTop; }
+__device__ __forceinline__ bool hPersistBottom(uint32_t h) { return (h & kPersistSlopeMask) == kPersistBottom; }
+__device__ __forceinline__ bool tKeep(uint32_t h, float4 t) {
+  return ((h & kPersist) != 0) || (t.y - t.x >= kMinCrop);
+}
+__device__ __forceinline__ float tTopX(uint32_t h, float4 t) { return hPositive(h) ? t.z : t.w; }
+
+// thresholdInvertedSlope K:240-246
+__device__ __forceinline__ float invSlope(uint32_t h, float4 t) {
+  float sign = hPositive(h) ? 1.0f : -1.0f;
+  return (t.x == t.y) ? FLT_MAX : (t.w - t.z) / (t.y - t.x) * sign;
+}
+// thresholdIntersectX K:900-913
+__device__ __forceinline__ float intersectX(uint32_t h, float4 t, float y) {
+  if (t.z == t.w) return t.z;
+  float sy = hPositive(h) ? t.x : t.y;
+  return ((y - sy) * invSlope(h, t)) + t.z;
+}
+// thresholdIsBelow K:1079-1094
+__device__ __forceinline__ bool isBelow(uint32_t ah, float4 a, uint32_t bh, float4 b) {
+  if (a.x > b.x) return true;
+  if (a.x != b.x) return false;
+  float ax = tTopX(ah, a), bx = tTopX(bh, b);
+  if (ax > bx) return true;
+  if (ax != bx) return false;
+  return invSlope(ah, a) > invSlope(bh, b);
+}
+
+// Threshold queue of one column: entries live in [start, cap) of the column's slab
+// and grow toward index 0 (initQueueSlice / pushTopSlot, K:402-405, K:1615-1620).
+struct Queue {
+  float4* thr;
+  uint32_t* hdr;
+  int start;
+  int cap;
+  bool overflow;
+  __device__ __forceinline__ int length() const { return cap - start; }
+  __device__ __forceinline__ float4 get(int i) const { return thr[start + i]; }
+  __device__ __forceinline__ uint32_t getH(int i) const { return hdr[start + i]; }
+  __device__ __forceinline__ void set(int i, float4 t) { thr[start + i] = t; }
+  __device__ __forceinline__ void setH(int i, uint32_t h) { hdr[start + i] = h; }
+  __device__ __forceinline__ void pop() { start += 1; }
+  // insertThreshold K:1105-1124: the new entry goes in front of the first entry it is
+  // not strictly below.
+  __device__ __forceinline__ void insert(uint32_t h, float4 t) {
+    if (start == 0) {
+      overflow = true;
+      return;
+    }
+    start -= 1;
+    const int len = cap - start;
+    int cursor = 0;
+    while (cursor < len - 1) {
+      uint32_t oh = hdr[start + cursor + 1];
+      float4 o = thr[start + cursor + 1];
+      if (!isBelow(h, t, oh, o)) break;
+      hdr[start + cursor] = oh;
+      thr[start + cursor] = o;
+      cursor += 1;
+    }
+    hdr[start + cursor] = h;
+    thr[start + cursor] = t;
+  }
+};
+
+template <int SECTIONS>
+struct ShapeStack {
+  uint64_t w[SECTIONS];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int i = 0; i < SECTIONS; ++i) w[i] = 0ull;
+  }
+  __device__ __forceinline__ void flip(uint32_t bit) { w[bit >> 6] ^= (1ull << (bit & 63)); }
+  __device__ __forceinline__ void pass(uint32_t h) { flip(h & kShapeBitMask); }
+  __device__ __forceinline__ void passTop(uint32_t h) { if (hPersistTop(h)) pass(h); }
+  __device__ __forceinline__ void passBottom(uint32_t h) { if (hPersistBottom(h)) pass(h); }
+  // findTop K:281-292
+  __device__ __forceinline__ int findTop(int ignoreAbove) const {
+    int sec = ignoreAbove >> 6;
+    int bits = ignoreAbove & 63;
+    uint64_t s = (~(~0ull << bits)) & w[sec];
+    while (s == 0ull && sec > 0) {
+      sec -= 1;
+      s = w[sec];
+    }
+    return (sec << 6) + (64 - __clzll((long long)s)) - 1;
+  }
+};
+
+// Column geometry (TileState, K:438-451 / initTileState K:1692-1718).
+struct ColumnState {
+  uint32_t shapeStart;
+  int numShapes;
+  int deltaX, deltaY;
+  int internalY;
+  int tileH;
+  int intHeight;
+  float floatHeight;
+  int threadUnique;
+  bool active;
+};
+
+__device__ __forceinline__ ColumnState initColumn(const RasterInputs& in, const gudni_tile_info& ti, int column) {
+  ColumnState c;
+  const int computeDepth = in.log2_tpt;
+  c.shapeStart = ti.shapes.start;
+  c.numShapes = (int)ti.shapes.length;
+  int hDepth = ti.hdepth, vDepth = ti.vdepth;
+  int diffDepth = max(0, vDepth - (computeDepth - hDepth));
+  int desiredHeight = 1 << diffDepth;
+  int internalX = ((1 << hDepth) - 1) & column;
+  c.internalY = (column >> hDepth) << diffDepth;
+  c.deltaX = internalX + ti.left;
+  c.deltaY = c.internalY + ti.top;
+  c.threadUnique = (ti.column_allocation + (1 << computeDepth) +
+                    in.job_index * (1 << (computeDepth + computeDepth))) * kLargePrime;
+  c.intHeight = min(desiredHeight, in.bitmap_h - c.deltaY);
+  c.floatHeight = (float)c.intHeight;
+  c.tileH = ti.bottom - ti.top;
+  c.active = c.internalY < c.tileH && c.deltaX < in.bitmap_w && c.deltaY < in.bitmap_h;
+  return c;
+}
+
+// ------------------------------------------------------------------ generate
+struct Trav {
+  float2 left, control, right;
+  float xPos;
+  int index;
+};
+
+// bifurcateCurve K:1233-1258 (bounded)
+__device__ __forceinline__ void bifurcate(Trav& t, int& status) {
+  if (t.left.x == t.control.x && t.left.y == t.control.y) return;
+  for (int it = 0;; ++it) {
+    if (it >= kBifurcateCap) {
+      status |= kStatusIterLimit;
+      return;
+    }
+    float2 lm = make_float2((1.0f - kHalf) * t.left.x + kHalf * t.control.x,
+                            (1.0f - kHalf) * t.left.y + kHalf * t.control.y);
+    float2 rm = make_float2((1.0f - kHalf) * t.control.x + kHalf * t.right.x,
+                            (1.0f - kHalf) * t.control.y + kHalf * t.right.y);
+    float2 on = make_float2((1.0f - kHalf) * lm.x + kHalf * rm.x, (1.0f - kHalf) * lm.y + kHalf * rm.y);
+    float flat = fabsf(on.x - t.control.x) + fabsf(on.y - t.control.y);
+    if (!(flat > kFlatness)) return;
+    if (t.xPos < on.x) {
+      t.control = lm;
+      t.right = on;
+    } else {
+      t.left = on;
+      t.control = rm;
+    }
+  }
+}
+
+// intersectCurve K:1226-1230
+__device__ __forceinline__ float intersectCurve(Trav t, int& status) {
+  bifurcate(t, status);
+  if (t.left.x == t.right.x) return cl_min(t.left.y, t.right.y);
+  return (((t.right.y - t.left.y) / (t.right.x - t.left.x)) * (t.xPos - t.left.x)) + t.left.y;
+}
+
+struct GenState {
+  Queue* q;
+  const ColumnState* c;
+};
+
+// addLineSegment / addThreshold K:1155-1220 (lineToThreshold/lineToHeader K:1131-1150,
+// trimThresholdTop K:982-1005), inserting into sorted position.
+__device__ __forceinline__ void addLineSegment(GenState& g, float2 left, float2 right, uint32_t shapeBit,
+                                               bool& added, bool& enclosed) {
+  float4 t = make_float4(cl_fmin(left.y, right.y), cl_fmax(left.y, right.y), left.x, right.x);
+  bool positive = left.y <= right.y;
+  bool persist = (left.x != right.x) && (left.x == kLeft);
+  uint32_t h = (positive ? kPositive : 0u) | (persist ? kPersist : 0u) | shapeBit;
+  if (!tKeep(h, t)) return;
+  enclosed = enclosed || ((t.x <= 0.0f) && hPersistTop(h)) || ((t.y <= 0.0f) && hPersistBottom(h));
+  if ((t.x < g.c->floatHeight) && (t.y > 0.0f) && (t.z < kRight)) {
+    if (t.x <= 0.0f) {
+      float splitX = intersectX(h, t, 0.0f);
+      if (hPositive(h)) {
+        t = make_float4(0.0f, t.y, splitX, t.w);
+        h = h & kUnpersist;
+      } else {
+        t = make_float4(0.0f, t.y, t.z, splitX);
+      }
+    }
+    if (t.w <= kLeft) {
+      enclosed = true;
+    } else {
+      added = true;
+      g.q->insert(h, t);
+    }
+  }
+}
+
+// spawnThresholds K:1264-1333
+__device__ __forceinline__ void spawnThresholds(GenState& g, uint32_t shapeBit, Trav& l, Trav& r, bool& added,
+                                                bool& enclosed, int& status) {
+  float yL = (l.left.x >= kLeft) ? l.left.y : intersectCurve(l, status);
+  bool leftWing = false;
+  if ((l.right.x < kRight) && (l.right.x > kLeft)) {
+    addLineSegment(g, make_float2(l.xPos, yL), l.right, shapeBit, added, enclosed);
+    leftWing = true;
+  }
+  float yR = (r.right.x <= kRight) ? r.right.y : intersectCurve(r, status);
+  bool rightWing = false;
+  if ((r.left.x > kLeft) && (r.left.x < kRight) && (l.index != r.index)) {
+    addLineSegment(g, r.left, make_float2(r.xPos, yR), shapeBit, added, enclosed);
+    rightWing = true;
+  }
+  if (l.right.x < r.left.x || (!leftWing && !rightWing)) {
+    float2 bl = (leftWing || (l.left.x == l.right.x)) ? l.right : make_float2(l.xPos, yL);
+    float2 br = (rightWing || (r.left.x == r.right.x)) ? r.left : make_float2(r.xPos, yR);
+    addLineSegment(g, bl, br, shapeBit, added, enclosed);
+  }
+}
+
+// searchTree K:1337-1357 over the strand's complete binary tree of (point, control)
+__device__ __forceinline__ void searchTree(Trav& t, const float4* tree, int treeSize, float2 d, bool isLeft) {
+  t.index = 0;
+  while (t.index < treeSize) {
+    float4 n = tree[t.index];
+    float cx = n.x - d.x, cy = n.y - d.y;
+    if ((t.xPos < cx) || (isLeft && t.xPos == cx)) {
+      t.right = make_float2(cx, cy);
+      t.index = (t.index << 1) + 1;
+    } else {
+      t.left = make_float2(cx, cy);
+      t.control = make_float2(n.z - d.x, n.w - d.y);
+      t.index = (t.index << 1) + 2;
+    }
+  }
+}
+
+// buildThresholdArray K:1540-1595 with traverseTree K:1378-1408.
+// Returns the number of shape bits assigned; shape indices go to `shapeIdx`.
+template <int SECTIONS>
+__device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, const ColumnState& c, Queue& q,
+                                                    ShapeStack<SECTIONS>& stack, uint32_t* shapeIdx,
+                                                    int& status) {
+  GenState g{&q, &c};
+  const float2 d = make_float2((float)c.deltaX, (float)c.deltaY);
+  uint32_t shapeBits = 0;
+  for (int n = 0; n < c.numShapes && (int)shapeBits < in.max_shape; ++n) {
+    const uint32_t shapeIndex = c.shapeStart + (uint32_t)n;
+    const gudni_shape shape = in.shapes[shapeIndex];
+    bool added = false;
+    bool enclosedByShape = false;
+    size_t off = (size_t)shape.geo_start * 16;
+    for (uint32_t k = 0; k < shape.num_strands; ++k) {
+      if (off + 32 > in.geometry_bytes) {
+        status |= kStatusBadInput;
+        break;
+      }
+      const uint8_t* strand = in.geometry + off;
+      const uint32_t size = (uint32_t)(*reinterpret_cast<const uint16_t*>(strand));
+      // a serialized strand is 2k+2 eight-byte units (k >= 1 curves); an odd size
+      // would misalign the float4 reads of every strand after it
+      if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > in.geometry_bytes) {
+        status |= kStatusBadInput;
+        break;
+      }
+      bool enclosedByStrand = false;
+      const int treeSize = ((int)size - 4) / 2;
+      const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
+      const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
+      Trav l;
+      l.right = make_float2(rp.x - d.x, rp.y - d.y);
+      l.left = make_float2(lc.x - d.x, lc.y - d.y);
+      l.control = make_float2(lc.z - d.x, lc.w - d.y);
+      l.xPos = 0.0f;
+      l.index = 0;
+      if (l.left.x <= kRight && l.right.x > kLeft) {  // checkInRange K:1360-1363
+        Trav r = l;
+        l.xPos = cl_max(kLeft, l.left.x);
+        r.xPos = cl_min(kRight, l.right.x);
+        const float4* tree = reinterpret_cast<const float4*>(strand + 32);
+        searchTree(l, tree, treeSize, d, true);
+        searchTree(r, tree, treeSize, d, false);
+        spawnThresholds(g, shapeBits, l, r, added, enclosedByStrand, status);
+        if (q.overflow) return shapeBits;
+      }
+      off += (size_t)size * 8;
+      enclosedByShape = enclosedByShape != enclosedByStrand;
+    }
+    if (enclosedByShape) stack.flip(shapeBits);
+    if (added || enclosedByShape) {
+      shapeIdx[shapeBits] = shapeIndex;
+      shapeBits += 1;
+    }
+  }
+  return shapeBits;
+}
+
+// ------------------------------------------------------------------ render
+__device__ __forceinline__ float4 composite(float4 fg, float4 bg) {  // K:878-887
+  float alphaOut = fg.w + bg.w * (1.0f - fg.w);
+  if (alphaOut > 0.0f) {
+    // (background * ALPHA(background)) * (1 - ALPHA(foreground)), left to right
+    float k = 1.0f - fg.w;
+    return make_float4(((fg.x * fg.w) + ((bg.x * bg.w) * k)) / alphaOut,
+                       ((fg.y * fg.w) + ((bg.y * bg.w) * k)) / alphaOut,
+                       ((fg.z * fg.w) + ((bg.z * bg.w) * k)) / alphaOut, alphaOut);
+  }
+  return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// readColor K:1411-1442 plus the radial-gradient substance (evaluated at the
+// integer pixel position like a picture texel).
+__device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int py, uint64_t sid, uint64_t type,
+                                            int& status) {
+  if (sid >= in.n_substances) {
+    status |= kStatusBadInput;
+    return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  const float4 sub = in.substances[sid];
+  if (type == GUDNI_TAG_SOLID) return sub;
+  const uint32_t id = __float_as_uint(sub.x);
+  if (type == GUDNI_TAG_RADIAL) {
+    if (id >= in.n_radials) {
+      status |= kStatusBadInput;
+      return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    const gudni_radial& g = in.radials[id];
+    float dx = (float)px - g.center_x, dy = (float)py - g.center_y;
+    float dist = sqrtf(dx * dx + dy * dy);
+    float t = dist / g.radius;
+    t = t < 1.0f ? t : 1.0f;
+    return make_float4(g.inner[0] + (g.outer[0] - g.inner[0]) * t, g.inner[1] + (g.outer[1] - g.inner[1]) * t,
+                       g.inner[2] + (g.outer[2] - g.inner[2]) * t, g.inner[3] + (g.outer[3] - g.inner[3]) * t);
+  }
+  if (id >= in.n_uses) {
+    status |= kStatusBadInput;
+    return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  const gudni_picture_use u = in.uses[id];
+  float scale = u.scale < 1e-7f ? 1e-7f : u.scale;
+  int rx = (int)(((float)px / scale) - u.translate_x);  // cvt.rzi: saturating, NaN -> 0
+  int ry = (int)(((float)py / scale) - u.translate_y);
+  if (rx >= 0 && ry >= 0 && rx < u.size_x && ry < u.size_y) {
+    size_t o = (size_t)u.mem_offset + 4 * ((size_t)ry * (size_t)u.size_x + (size_t)rx);
+    if (o + 4 > in.picture_bytes) {
+      status |= kStatusBadInput;
+      return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    uchar4 p = *reinterpret_cast<const uchar4*>(in.pictures + o);
+    return make_float4((float)p.x / 255.0f, (float)p.y / 255.0f, (float)p.z / 255.0f, (float)p.w / 255.0f);
+  }
+  return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// determineColor K:1447-1513
+template <int SECTIONS>
+__device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
+                                                 const uint32_t* shapeIdx, int px, int py, int& status) {
+  int topBit = in.max_shape;
+  float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float4 next = base;
+  bool done = false;
+  uint64_t lastId = ~0ull;
+  bool lastIsContinue = true;
+  bool lastIsSet = false;
+  while (!done) {
+    bool shouldComposite = true;
+    topBit = stack.findTop(topBit);
+    if (topBit < 0) {
+      next = in.background;
+      done = true;
+      lastIsSet = true;
+    } else {
+      const uint32_t ref = shapeIdx[topBit];
+      const uint64_t tag = in.shapes[ref].tag;
+      const uint64_t sid = tag & GUDNI_TAG_ID_MASK;
+      const uint64_t comp = tag & GUDNI_TAG_COMPOUND_MASK;
+      if (sid == lastId) {
+        if (lastIsContinue) {
+          if (comp != GUDNI_TAG_CONTINUE) {
+            lastIsSet = comp == GUDNI_TAG_ADD;
+            lastIsContinue = false;
+          } else {
+            lastIsSet = !lastIsSet;
+          }
+        }
+        shouldComposite = false;
+      } else {
+        next = readColor(in, px, py, sid, tag & GUDNI_TAG_SUBSTANCE_MASK, status);
+        lastIsSet = comp == GUDNI_TAG_ADD || comp == GUDNI_TAG_CONTINUE;
+      }
+      lastId = sid;
+    }
+    if (shouldComposite && lastIsSet) {
+      base = composite(base, next);
+      if (base.w == 1.0f) done = true;
+    }
+  }
+  return base;
+}
+
+struct Parse {
+  int current, numActive;
+  float sStartX, sStartY, sEndX, sEndY;
+  float pixelY;
+};
+
+// splitNext K:1069-1077 (countActive K:1007, nextSlicePoint K:1026, sliceActive K:1040)
+__device__ __forceinline__ float splitNext(Queue& q, Parse& p) {
+  const int len = q.length();
+  float slicePoint = FLT_MAX;
+  const float top = q.get(0).x;
+  int n = 1;
+  while (n < len) {
+    float t = q.get(n).x;
+    if (t > top) {
+      slicePoint = t;
+      break;
+    }
+    n += 1;
+  }
+  p.numActive = n;
+  float sp = slicePoint;
+  for (int i = 0; i < n; ++i) {
+    float bottom = q.get(i).y;
+    if (top < bottom) sp = cl_min(sp, bottom);
+  }
+  slicePoint = cl_min(slicePoint, sp);
+  for (int cursor = 0; cursor < n; ++cursor) {
+    uint32_t ch = q.getH(cursor);
+    float4 cur = q.get(cursor);
+    if (cur.x < slicePoint && slicePoint < cur.y) {
+      float splitX = intersectX(ch, cur, slicePoint);
+      uint32_t sh;
+      float4 split;
+      if (hPositive(ch)) {
+        split = make_float4(slicePoint, cur.y, splitX, cur.w);
+        cur = make_float4(cur.x, slicePoint, cur.z, splitX);
+        sh = ch & kUnpersist;
+      } else {
+        split = make_float4(slicePoint, cur.y, cur.z, splitX);
+        cur = make_float4(cur.x, slicePoint, splitX, cur.w);
+        sh = ch;
+        ch = ch & kUnpersist;
+      }
+      q.setH(cursor, ch);
+      q.set(cursor, cur);
+      if (tKeep(sh, split)) {
+        q.insert(sh, split);
+        if (q.overflow) return slicePoint;
+      }
+    }
+  }
+  return slicePoint;
+}
+
+// verticalAdvance K:1744-1824
+template <int SECTIONS>
+__device__ __forceinline__ void verticalAdvance(Queue& q, const ColumnState& c, Parse& p,
+                                                ShapeStack<SECTIONS>& stack) {
+  if (p.sEndX != kRight) return;
+  for (int i = 0; i < p.numActive; ++i) stack.pass(q.getH(i));
+  const float nextBreak = cl_min(c.floatHeight, p.pixelY);
+  const float activeBottom = q.length() > 0 ? q.get(0).y : FLT_MAX;
+  if (activeBottom == p.sEndY) {
+    while (p.numActive > 0) {
+      stack.passBottom(q.getH(0));
+      q.pop();
+      p.numActive -= 1;
+    }
+  }
+  float nextBottom;
+  if (p.numActive > 0) {
+    nextBottom = cl_min(activeBottom, nextBreak);
+  } else {
+    const float nextTop = p.numActive < q.length() ? q.get(p.numActive).x : FLT_MAX;
+    if (nextTop > p.sEndY) {
+      nextBottom = cl_min(nextBreak, nextTop);
+    } else {
+      nextBottom = cl_min(nextBreak, splitNext(q, p));
+      while (p.numActive > 0 && q.get(0).x == q.get(0).y) {
+        stack.passTop(q.getH(0));
+        q.pop();
+        p.numActive -= 1;
+      }
+      for (int i = 0; i < p.numActive; ++i) {
+        if (q.get(i).x > 0.0f) stack.passTop(q.getH(i));
+      }
+    }
+  }
+  p.sStartY = p.sEndY;
+  p.sEndY = nextBottom;
+  p.sStartX = p.sEndX = kLeft;
+  p.current = 0;
+}
+
+// convert_uchar of colour * 255: round toward zero, clamp to [0,255], NaN -> 0
+__device__ __forceinline__ uint32_t toByte(float v) {
+  if (!(v > 0.0f)) return 0u;
+  if (v >= 255.0f) return 255u;
+  return (uint32_t)(int)v;
+}
+
+// renderThresholdArray K:1978-2028 (calculatePixel K:1881-1916, horizontalAdvance
+// K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
+template <int SECTIONS>
+__device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
+                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
+                                             int64_t* sectionCounter) {
+  Parse p;
+  p.current = 0;
+  p.numActive = 0;
+  p.sStartX = kLeft;
+  p.sStartY = 0.0f;
+  p.sEndX = kRight;
+  p.sEndY = 0.0f;
+  int cursor = 0;
+  if (in.stochastic != 0.0f && in.random_field) {  // initRandomField K:1597-1606
+    cursor = (int)(__float_as_uint(in.random_field[c.threadUnique & (GUDNI_RANDOM_FIELD_SIZE - 1)]) &
+                   (GUDNI_RANDOM_FIELD_SIZE - 1));
+  }
+  const int px = c.deltaX;
+  int py = c.deltaY;
+  uint32_t* outp = in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
+  int64_t sections = 0;
+  for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
+    int guard = 0;
+    while ((p.sEndX < kRight) || (p.sEndY < p.pixelY)) {
+      if (++guard > kSectionCap) {
+        status |= kStatusIterLimit;
+        return;
+      }
+      verticalAdvance(q, c, p, stack);
+      if (q.overflow) return;
+      // horizontalAdvance
+      float nextX = kRight;
+      if (p.current < p.numActive) {
+        const float4 t = q.get(p.current);
+        const uint32_t h = q.getH(p.current);
+        const float yMid = p.sStartY + ((p.sEndY - p.sStartY) * 0.5f);
+        const float x = intersectX(h, t, yMid);
+        nextX = x >= kRight ? kLeft : cl_max(kLeft, x);  // thresholdMidXLow K:916-926
+      }
+      p.sStartX = p.sEndX;
+      p.sEndX = nextX;
+      const float4 color = determineColor(in, stack, shapeIdx, px, py, status);
+      float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
+      if (in.stochastic != 0.0f) {  // getRandom K:1608-1613
+        cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);
+        const float random = in.random_field ? in.random_field[cursor] : 0.0f;
+        area = area + (area * random * in.stochastic);
+      }
+      acc0 += color.x * area;
+      acc1 += color.y * area;
+      acc2 += color.z * area;
+      acc4 += area;
+      if (p.current < p.numActive) stack.pass(q.getH(p.current));
+      p.current += 1;
+      ++sections;
+    }
+    const float r = acc0 / acc4, g = acc1 / acc4, b = acc2 / acc4;
+    *outp = toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
+    outp += in.bitmap_w;
+    p.sStartX = kLeft;
+    p.sStartY = p.pixelY;
+    py += 1;
+  }
+  if (sectionCounter) atomicAdd(reinterpret_cast<unsigned long long*>(sectionCounter), (unsigned long long)sections);
+}
+
+}  // namespace gudni

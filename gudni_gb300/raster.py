@@ -1,0 +1,106 @@
+"""Host-side mirror of the reference's OpenCL dispatch, over the CUDA C ABI.
+
+  Rasterizer(spec)           setupOpenCL        (OpenCL/Setup.hs:102-147)
+  Rasterizer.upload_common   BuffersInCommon    (OpenCL/CallKernels.hs:208-240)
+  Rasterizer.raster_job      raster/generateCall (OpenCL/CallKernels.hs:88-206)
+  Rasterizer.queue_jobs      queueRasterJobs    (OpenCL/CallKernels.hs:218-242)
+
+Every call goes through libgudni_cuda.so; there is no CPU path.  If the library is
+missing or no CUDA device is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import lib as L
+
+
+class RasterError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{L.STATUS.get(code, code)}: {message}")
+        self.code = code
+
+
+class Rasterizer:
+    def __init__(self, spec: L.Spec, device: int = 0):
+        self.lib = L.load_cuda()
+        self.spec = spec
+        self._spec_ref = L.Spec(*[getattr(spec, f) for f, _ in L.Spec._fields_])
+        h = self.lib.gudni_create(C.byref(self._spec_ref), device)
+        if not h:
+            raise RuntimeError("gudni_create failed: " + self.lib.gudni_last_error(None).decode())
+        self.ctx = h
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.gudni_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise RasterError(rc, self.lib.gudni_last_error(self.ctx).decode())
+
+    def upload_common(self, frame) -> None:
+        rf = frame.random_field if frame.random_field is not None else None
+        self._check(self.lib.gudni_upload_common(
+            self.ctx, L.ptr(frame.geometry), frame.geometry.size, L.ptr(frame.substances),
+            len(frame.substances), L.ptr(frame.pictures), frame.pictures.size, L.ptr(frame.picture_uses),
+            len(frame.picture_uses), L.ptr(frame.radials), len(frame.radials), L.ptr(rf)))
+
+    def raster_job(self, frame, job_index: int, out: np.ndarray, frame_number: int = 0) -> None:
+        """Rasterize one job into the host bitmap `out` ((H, W) uint32)."""
+        job = frame.jobs[job_index]
+        assert out.dtype == np.uint32 and out.flags.c_contiguous and out.size == frame.canvas_w * frame.canvas_h
+        bg = np.ascontiguousarray(frame.background, np.float32)
+        self._check(self.lib.gudni_raster_job(
+            self.ctx, L.ptr(job.shapes), len(job.shapes), L.ptr(job.tiles), len(job.tiles), job.columns,
+            frame.canvas_w, frame.canvas_h, frame.compute_depth, frame_number, job_index, bg.ctypes.data,
+            out.ctypes.data))
+
+    def queue_jobs(self, frame, out: Optional[np.ndarray] = None, frame_number: int = 0) -> np.ndarray:
+        """Upload the common buffers and rasterize every job (host buffers)."""
+        if out is None:
+            out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
+        self.upload_common(frame)
+        for j in range(len(frame.jobs)):
+            self.raster_job(frame, j, out, frame_number)
+        return out
+
+    def raster_job_device(self, frame, job_index: int, shapes_ptr: int, tiles_ptr: int, out_ptr: int,
+                          stream: int = 0, frame_number: int = 0) -> None:
+        """Enqueue one job with device-resident shapes/tiles/out (torch data_ptr()s)."""
+        job = frame.jobs[job_index]
+        bg = np.ascontiguousarray(frame.background, np.float32)
+        self._check(self.lib.gudni_raster_job_device(
+            self.ctx, shapes_ptr, len(job.shapes), tiles_ptr, len(job.tiles), job.columns, frame.canvas_w,
+            frame.canvas_h, frame.compute_depth, frame_number, job_index, bg.ctypes.data, out_ptr,
+            stream or None))
+
+    def sync_status(self) -> None:
+        self._check(self.lib.gudni_sync_status(self.ctx))
+
+    def scratch_bytes(self) -> int:
+        return int(self.lib.gudni_scratch_bytes(self.ctx))
+
+
+def bgra_to_rgb(words: np.ndarray) -> np.ndarray:
+    """(H, W) BGRA words -> (H, W, 3) uint8 RGB."""
+    b = (words & 0xFF).astype(np.uint8)
+    g = ((words >> 8) & 0xFF).astype(np.uint8)
+    r = ((words >> 16) & 0xFF).astype(np.uint8)
+    return np.stack([r, g, b], axis=-1)

@@ -82,11 +82,14 @@ def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: in
     """Build the reference kernels for one (MAXSHAPE, SHAPESTACKSECTIONS) pair.
     Returns the library path, or None when the reference checkout is absent."""
     lib = library_name(max_shape, sections)
-    if not os.path.isfile(os.path.join(reference, KERNELS_REL)):
-        return lib if os.path.isfile(lib) else None
+    cpp = os.path.join(OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp")
     if os.path.isfile(lib) and not force:
         return lib
-    cpp = generate(reference, max_shape, sections)
+    if os.path.isfile(os.path.join(reference, KERNELS_REL)):
+        cpp = generate(reference, max_shape, sections)
+    elif not os.path.isfile(cpp):
+        # neither the reference checkout nor a translation unit generated from it
+        return None
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
            "-fPIC", "-shared", "-w", "-I", HERE, cpp, "-o", lib]
     subprocess.run(cmd, check=True)

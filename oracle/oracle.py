@@ -88,8 +88,9 @@ def render_frame(frame, n_threads: int = 0, max_thresholds: Optional[int] = None
 
 def ref_available(max_shape: int = 127, sections: int = 8) -> bool:
     from . import build_ref
-    return os.path.isfile(build_ref.library_name(max_shape, sections)) or os.path.isfile(
-        os.path.join(build_ref.DEFAULT_REFERENCE, build_ref.KERNELS_REL))
+    return (os.path.isfile(build_ref.library_name(max_shape, sections))
+            or os.path.isfile(os.path.join(build_ref.OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp"))
+            or os.path.isfile(os.path.join(build_ref.DEFAULT_REFERENCE, build_ref.KERNELS_REL)))
 
 
 def _load_ref(max_shape: int, sections: int):

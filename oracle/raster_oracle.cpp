@@ -417,9 +417,10 @@ struct Common {
 inline f4 composite(f4 fg, f4 bg) {  // K:878-887
   float alphaOut = fg.w + bg.w * (1.0f - fg.w);
   if (alphaOut > 0) {
-    float k = bg.w * (1.0f - fg.w);
-    return f4{((fg.x * fg.w) + (bg.x * k)) / alphaOut, ((fg.y * fg.w) + (bg.y * k)) / alphaOut,
-              ((fg.z * fg.w) + (bg.z * k)) / alphaOut, alphaOut};
+    // (background * ALPHA(background)) * (1 - ALPHA(foreground)), left to right
+    float k = 1.0f - fg.w;
+    return f4{((fg.x * fg.w) + ((bg.x * bg.w) * k)) / alphaOut, ((fg.y * fg.w) + ((bg.y * bg.w) * k)) / alphaOut,
+              ((fg.z * fg.w) + ((bg.z * bg.w) * k)) / alphaOut, alphaOut};
   }
   return f4{0, 0, 0, 0};
 }

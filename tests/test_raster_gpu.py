@@ -1,0 +1,144 @@
+"""CUDA raster path against the golden fixtures (reference kernels) and the oracle,
+through the C ABI.  Parity bar: <=1 LSB per channel and >=99.9% of pixels exact; the
+kernels are expected to be bit-exact and the tests report the exact fraction."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+sys.path.insert(0, GOLDEN)
+
+import fixture_scenes as F  # noqa: E402
+from conftest import assert_parity  # noqa: E402
+from gudni_gb300 import lib as L  # noqa: E402
+from gudni_gb300 import scene as S  # noqa: E402
+from gudni_gb300 import scenes as G  # noqa: E402
+from gudni_gb300.raster import RasterError, Rasterizer  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+with open(os.path.join(GOLDEN, "golden.json")) as f:
+    INDEX = json.load(f)
+
+
+def render(frame, **kw):
+    with Rasterizer(frame.spec) as r:
+        return r.queue_jobs(frame, **kw)
+
+
+@pytest.mark.parametrize("name", F.ALL)
+def test_golden_fixtures(name):
+    frame = F.build(name)
+    got = render(frame)
+    entry = INDEX[name]
+    if "image_file" in entry:
+        want = np.load(os.path.join(GOLDEN, entry["image_file"]))
+    else:
+        want = O.render_frame(frame)
+    assert_parity(got, want)
+    assert np.array_equal(got, want), f"{(got != want).sum()} pixels differ (within tolerance)"
+
+
+@pytest.mark.parametrize("tpt,tile", [(32, 32), (64, 32), (128, 32), (16, 16), (256, 16)])
+def test_random_scene_threads_per_tile(tpt, tile):
+    flat = G.random_shapes(seed=40 + tpt, width=160, height=120, n_shapes=30)
+    frame = S.serialize_flat(flat, L.make_spec(tile, tpt, 4096, 127, 8))
+    assert_parity(render(frame), O.render_frame(frame))
+
+
+def test_glyph_page_small_all_substances():
+    flat = G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25)
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 511, 8))
+    assert len(frame.radials) > 0 and len(frame.picture_uses) > 0
+    assert_parity(render(frame), O.render_frame(frame))
+
+
+def test_many_shapes_wide_stack():
+    """More shapes per column than one 64-bit stack word (max_shape 1023)."""
+    flat = G.random_shapes(seed=77, width=96, height=80, n_shapes=300, seg_lo=4, seg_hi=10)
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 8192, 1023, 16))
+    assert_parity(render(frame), O.render_frame(frame))
+
+
+def test_fallback_pass_matches(monkeypatch):
+    """Columns overflowing the small working capacity are re-run at full capacity."""
+    monkeypatch.setenv("GUDNI_WORKING_CAPACITY", "8")
+    frame = F.build("random_128x96")
+    got = render(frame)
+    want = np.load(os.path.join(GOLDEN, INDEX["random_128x96"]["image_file"]))
+    assert np.array_equal(got, want)
+
+
+def test_threshold_overflow_is_an_error():
+    frame = F.build("random_128x96")
+    frame.spec = L.make_spec(32, 32, 16, 127, 8)  # capacity far below the ~230 needed
+    with Rasterizer(frame.spec) as r:
+        with pytest.raises(RasterError) as e:
+            r.queue_jobs(frame)
+        assert e.value.code == -2
+        # the context stays usable
+        frame2 = F.build("tiny_square")
+        frame2.spec = frame.spec
+        r.queue_jobs(frame2)
+
+
+def test_corrupt_strand_is_bad_input_not_a_fault():
+    frame = F.build("knob")
+    frame.geometry = frame.geometry.copy()
+    frame.geometry[0:2] = np.frombuffer(np.uint16(7).tobytes(), np.uint8)  # odd strand size
+    with Rasterizer(frame.spec) as r:
+        with pytest.raises(RasterError) as e:
+            r.queue_jobs(frame)
+        assert e.value.code == -1
+        good = F.build("knob")
+        assert np.array_equal(r.queue_jobs(good), np.load(os.path.join(GOLDEN, "knob.npy")))
+
+
+def test_shape_pointing_past_geometry_is_bad_input():
+    frame = F.build("hourglass")
+    frame.jobs[0].shapes = frame.jobs[0].shapes.copy()
+    frame.jobs[0].shapes["geo_start"] = 1 << 20
+    with Rasterizer(frame.spec) as r:
+        with pytest.raises(RasterError) as e:
+            r.queue_jobs(frame)
+        assert e.value.code == -1
+
+
+def test_empty_scene_is_background():
+    frame = S.serialize(S.Scene((0.2, 0.4, 0.6, 1.0), S.EMPTY), 37, 23, L.make_spec(16, 16, 64))
+    got = render(frame)
+    assert np.array_equal(got, O.render_frame(frame))
+    b, g, r = got[0, 0] & 0xFF, (got[0, 0] >> 8) & 0xFF, (got[0, 0] >> 16) & 0xFF
+    assert (r, g, b) == (51, 102, 153)
+
+
+def test_one_pixel_canvas():
+    frame = F.build("tiny_square")
+    tiny = S.serialize(F.tiny_square(), 1, 1, frame.spec)
+    assert np.array_equal(render(tiny), O.render_frame(tiny))
+
+
+def test_device_pointer_path():
+    import torch
+    frame = F.build("random_odd_tiles")
+    want = np.load(os.path.join(GOLDEN, "random_odd_tiles.npy"))
+    dev = torch.device("cuda:0")
+    out = torch.zeros(frame.canvas_h * frame.canvas_w, dtype=torch.int32, device=dev)
+    with Rasterizer(frame.spec) as r:
+        r.upload_common(frame)
+        keep = []
+        for j, job in enumerate(frame.jobs):
+            sh = torch.from_numpy(job.shapes.view(np.uint8).copy()).to(dev)
+            ti = torch.from_numpy(job.tiles.view(np.uint8).copy()).to(dev)
+            keep += [sh, ti]
+            r.raster_job_device(frame, j, sh.data_ptr(), ti.data_ptr(), out.data_ptr(),
+                                stream=torch.cuda.current_stream().cuda_stream)
+        r.sync_status()
+        torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
+    assert np.array_equal(got, want)
