@@ -230,11 +230,14 @@ int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, c
   return GUDNI_OK;
 }
 
-int run_fallback(gudni_ctx* ctx, const gudni::RasterInputs& in, cudaStream_t stream) {
+int run_fallback(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, cudaStream_t stream) {
   uint32_t count = 0;
   cudaError_t e = cudaMemcpyAsync(&count, ctx->overflow_count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
+  // the list holds at most one entry per work item (a larger count already raised
+  // the overflow status in the kernel)
+  count = std::min<uint32_t>(count, (uint32_t)(n_tiles * (size_t)ctx->spec.threads_per_tile));
   if (count == 0) return GUDNI_OK;
   // slots for the full-capacity pass: bounded so the pass holds at most ~2 GB
   const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
@@ -353,7 +356,7 @@ int gudni_upload_common(gudni_ctx* ctx, const void* geometry, size_t geometry_by
   if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
   for (size_t i = 0; i < n_picture_uses; ++i) {
     const gudni_picture_use& u = picture_uses[i];
-    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 ||
+    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 ||
         (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
       return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
   }
@@ -396,7 +399,7 @@ int gudni_raster_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, n_shapes, ctx->tiles.ptr, n_tiles, bitmap_w, bitmap_h,
                                   compute_depth, job_index, background, ctx->out.ptr);
   if ((rc = enqueue_job(ctx, in, n_tiles, ctx->stream))) return rc;
-  if ((rc = run_fallback(ctx, in, ctx->stream))) return rc;
+  if ((rc = run_fallback(ctx, in, n_tiles, ctx->stream))) return rc;
   cudaError_t e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
   return read_status(ctx, ctx->stream);
@@ -412,13 +415,15 @@ int gudni_raster_job_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_
   if (rc) return rc;
   if (!out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null out or background");
   cudaSetDevice(ctx->device);
+  if (((uintptr_t)shapes & 7) != 0 || ((uintptr_t)tiles & 3) != 0 || ((uintptr_t)out & 3) != 0)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "misaligned device pointer");
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   ctx->last_stream = s;
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth,
                                   job_index, background, out);
   if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
   if (ctx->working_capacity < ctx->spec.max_thresholds) {
-    if ((rc = run_fallback(ctx, in, s))) return rc;
+    if ((rc = run_fallback(ctx, in, n_tiles, s))) return rc;
   }
   return GUDNI_OK;
 }
