@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "gudni_cuda.h"
 #include "raster_kernels.h"
@@ -92,6 +93,12 @@ struct gudni_ctx {
   DevBuf<int64_t> counters;
   int pending_status = 0;
   cudaStream_t last_stream = nullptr;  // stream of the last enqueued job
+  bool counters_on = false;
+  uint64_t launches = 0;
+  DevBuf<int32_t> tile_jobs;           // frame launches: job index per tile
+  std::vector<gudni_shape> h_shapes;   // frame launches: concatenated host piles
+  std::vector<gudni_tile_info> h_tiles;
+  std::vector<int32_t> h_tile_jobs;
 };
 
 namespace {
@@ -140,9 +147,15 @@ int ensure_scratch(gudni_ctx* ctx) {
   if ((e = ctx->thr.reserve(slots * cap)) != cudaSuccess) return cuda_fail(ctx, e, "scratch thresholds");
   if ((e = ctx->hdr.reserve(slots * cap)) != cudaSuccess) return cuda_fail(ctx, e, "scratch headers");
   if ((e = ctx->idx.reserve(slots * (size_t)ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "scratch shape indices");
-  if ((e = ctx->status.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "status word");
+  if (!ctx->status.ptr) {  // device memory starts undefined: clear the words once
+    if ((e = ctx->status.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "status word");
+    if ((e = cudaMemset(ctx->status.ptr, 0, sizeof(int))) != cudaSuccess) return cuda_fail(ctx, e, "status word");
+  }
   if ((e = ctx->overflow_count.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
-  if ((e = ctx->counters.reserve(4)) != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  if (!ctx->counters.ptr) {
+    if ((e = ctx->counters.reserve(4)) != cudaSuccess) return cuda_fail(ctx, e, "counters");
+    if ((e = cudaMemset(ctx->counters.ptr, 0, 4 * sizeof(int64_t))) != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  }
   return GUDNI_OK;
 }
 
@@ -196,6 +209,8 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   in.background = make_float4(background[0], background[1], background[2], background[3]);
   in.max_shape = ctx->spec.max_shape;
   in.out = d_out;
+  in.tile_jobs = nullptr;
+  in.counters = ctx->counters_on ? ctx->counters.ptr : nullptr;
   return in;
 }
 
@@ -222,11 +237,11 @@ int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, c
   a.overflow_cap = n_items;
   a.overflow_count = ctx->overflow_count.ptr;
   a.status = ctx->status.ptr;
-  a.section_counter = nullptr;
   const uint32_t blocks_needed = (n_items + gudni::kRasterBlock - 1) / gudni::kRasterBlock;
   const int grid = (int)std::min<uint32_t>(blocks_needed, (uint32_t)ctx->grid);
   if ((e = gudni::launch_columns(a, ctx->sections, grid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "raster launch");
+  ctx->launches += 1;
   return GUDNI_OK;
 }
 
@@ -257,14 +272,19 @@ int run_fallback(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, 
   a.overflow_cap = 0;
   a.overflow_count = nullptr;
   a.status = ctx->status.ptr;
-  a.section_counter = nullptr;
   if ((e = gudni::launch_columns(a, ctx->sections, (int)(slots / gudni::kRasterBlock), stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "fallback launch");
+  ctx->launches += 1;
   return GUDNI_OK;
 }
 
 int read_status(gudni_ctx* ctx, cudaStream_t stream) {
   int bits = 0;
+  if (!ctx->status.ptr) {
+    bits = ctx->pending_status;
+    ctx->pending_status = 0;
+    return bits ? fail(ctx, status_to_code(bits), status_message(bits)) : GUDNI_OK;
+  }
   cudaError_t e = cudaMemcpyAsync(&bits, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -334,7 +354,7 @@ void gudni_destroy(gudni_ctx* ctx) {
   ctx->radials.release(); ctx->random_field.release(); ctx->shapes.release(); ctx->tiles.release();
   ctx->out.release(); ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release();
   ctx->big_hdr.release(); ctx->big_idx.release(); ctx->overflow_items.release();
-  ctx->overflow_count.release(); ctx->status.release(); ctx->counters.release();
+  ctx->overflow_count.release(); ctx->status.release(); ctx->counters.release(); ctx->tile_jobs.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -443,5 +463,96 @@ size_t gudni_scratch_bytes(const gudni_ctx* ctx) {
   return ctx->thr.cap * sizeof(float4) + ctx->hdr.cap * 4 + ctx->idx.cap * 4 + ctx->big_thr.cap * sizeof(float4) +
          ctx->big_hdr.cap * 4 + ctx->big_idx.cap * 4;
 }
+
+int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs, int32_t bitmap_w,
+                       int32_t bitmap_h, int32_t compute_depth, int32_t frame_number, const float background[4],
+                       uint32_t* out) {
+  (void)frame_number;
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if ((n_jobs && !jobs) || !out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null argument");
+  // concatenate the jobs' piles; each tile's shape slice is offset into the whole
+  ctx->h_shapes.clear();
+  ctx->h_tiles.clear();
+  ctx->h_tile_jobs.clear();
+  for (size_t j = 0; j < n_jobs; ++j) {
+    const gudni_job_desc& d = jobs[j];
+    int rc = validate_job(ctx, d.shapes, d.n_shapes, d.tiles, d.n_tiles, bitmap_w, bitmap_h, compute_depth, true);
+    if (rc) return rc;
+    const uint32_t base = (uint32_t)ctx->h_shapes.size();
+    ctx->h_shapes.insert(ctx->h_shapes.end(), d.shapes, d.shapes + d.n_shapes);
+    for (size_t t = 0; t < d.n_tiles; ++t) {
+      gudni_tile_info ti = d.tiles[t];
+      ti.shapes.start += base;
+      ctx->h_tiles.push_back(ti);
+      ctx->h_tile_jobs.push_back((int32_t)j);
+    }
+  }
+  if ((uint64_t)ctx->h_tiles.size() * (uint64_t)ctx->spec.threads_per_tile >= (1ull << 32))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many work items in one frame");
+  cudaSetDevice(ctx->device);
+  int rc;
+  const size_t pixels = (size_t)bitmap_w * (size_t)bitmap_h;
+  if ((rc = upload(ctx, ctx->shapes, ctx->h_shapes.data(), ctx->h_shapes.size(), "shape upload"))) return rc;
+  if ((rc = upload(ctx, ctx->tiles, ctx->h_tiles.data(), ctx->h_tiles.size(), "tile upload"))) return rc;
+  if ((rc = upload(ctx, ctx->tile_jobs, ctx->h_tile_jobs.data(), ctx->h_tile_jobs.size(), "tile job upload"))) return rc;
+  cudaError_t e = ctx->out.reserve(pixels);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap");
+  gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, ctx->h_shapes.size(), ctx->tiles.ptr, ctx->h_tiles.size(),
+                                  bitmap_w, bitmap_h, compute_depth, 0, background, ctx->out.ptr);
+  in.tile_jobs = ctx->tile_jobs.ptr;
+  if ((rc = enqueue_job(ctx, in, ctx->h_tiles.size(), ctx->stream))) return rc;
+  if ((rc = run_fallback(ctx, in, ctx->h_tiles.size(), ctx->stream))) return rc;
+  e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
+  return read_status(ctx, ctx->stream);
+}
+
+int gudni_raster_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
+                              const gudni_tile_info* tiles, const int32_t* tile_jobs, size_t n_tiles,
+                              int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth, int32_t frame_number,
+                              const float background[4], uint32_t* out, void* stream) {
+  (void)frame_number;
+  int rc = validate_job(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, false);
+  if (rc) return rc;
+  if (!out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null out or background");
+  if (((uintptr_t)shapes & 7) != 0 || ((uintptr_t)tiles & 3) != 0 || ((uintptr_t)out & 3) != 0 ||
+      ((uintptr_t)tile_jobs & 3) != 0)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "misaligned device pointer");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, 0,
+                                  background, out);
+  in.tile_jobs = tile_jobs;
+  if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
+  if (ctx->working_capacity < ctx->spec.max_thresholds) {
+    if ((rc = run_fallback(ctx, in, n_tiles, s))) return rc;
+  }
+  return GUDNI_OK;
+}
+
+int gudni_enable_counters(gudni_ctx* ctx, int enable) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = ctx->counters.reserve(4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->counters.ptr, 0, 4 * sizeof(int64_t), ctx->stream);  // reset
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  ctx->counters_on = enable != 0;
+  return GUDNI_OK;
+}
+
+int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]) {
+  if (!ctx || !out) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = ctx->counters.reserve(4);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(out, ctx->counters.ptr, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(ctx->counters.ptr, 0, 4 * sizeof(int64_t));
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  return GUDNI_OK;
+}
+
+uint64_t gudni_launch_count(const gudni_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 }  // extern "C"

@@ -50,13 +50,17 @@ __global__ void __launch_bounds__(kRasterBlock) raster_columns_kernel(ColumnLaun
       status |= kStatusBadInput;
       continue;
     }
-    const ColumnState c = initColumn(a.in, ti, column);
+    const ColumnState c = initColumn(a.in, ti, column, a.in.tile_jobs ? a.in.tile_jobs[tile] : a.in.job_index);
     if (!c.active) continue;
     Queue q{thr, hdr, a.scratch.capacity, a.scratch.capacity, false};
     ShapeStack<SECTIONS> stack;
     stack.clear();
-    buildThresholds<SECTIONS>(a.in, c, q, stack, idx, status);
-    if (!q.overflow) renderColumn<SECTIONS>(a.in, c, q, stack, idx, status, a.section_counter);
+    const uint32_t bits = buildThresholds<SECTIONS>(a.in, c, q, stack, idx, status);
+    if (a.in.counters && !q.overflow) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&a.in.counters[2]), (unsigned long long)q.length());
+      atomicMax(reinterpret_cast<unsigned long long*>(&a.in.counters[3]), (unsigned long long)bits);
+    }
+    if (!q.overflow) renderColumn<SECTIONS>(a.in, c, q, stack, idx, status);
     if (q.overflow) {
       if (a.overflow_items) {
         const uint32_t k = atomicAdd(a.overflow_count, 1u);

@@ -72,6 +72,8 @@ struct RasterInputs {
   float4 background;
   int max_shape;
   uint32_t* out;                 // bitmap_w * bitmap_h BGRA words
+  const int32_t* tile_jobs;      // optional per-tile job index (frame launches)
+  int64_t* counters;             // optional work counters (see gudni_enable_counters)
 };
 
 __device__ __forceinline__ float cl_min(float x, float y) { return y < x ? y : x; }
@@ -186,7 +188,8 @@ struct ColumnState {
   bool active;
 };
 
-__device__ __forceinline__ ColumnState initColumn(const RasterInputs& in, const gudni_tile_info& ti, int column) {
+__device__ __forceinline__ ColumnState initColumn(const RasterInputs& in, const gudni_tile_info& ti, int column,
+                                                  int job_index) {
   ColumnState c;
   const int computeDepth = in.log2_tpt;
   c.shapeStart = ti.shapes.start;
@@ -199,7 +202,7 @@ __device__ __forceinline__ ColumnState initColumn(const RasterInputs& in, const 
   c.deltaX = internalX + ti.left;
   c.deltaY = c.internalY + ti.top;
   c.threadUnique = (ti.column_allocation + (1 << computeDepth) +
-                    in.job_index * (1 << (computeDepth + computeDepth))) * kLargePrime;
+                    job_index * (1 << (computeDepth + computeDepth))) * kLargePrime;
   c.intHeight = min(desiredHeight, in.bitmap_h - c.deltaY);
   c.floatHeight = (float)c.intHeight;
   c.tileH = ti.bottom - ti.top;
@@ -395,7 +398,7 @@ __device__ __forceinline__ float4 composite(float4 fg, float4 bg) {  // K:878-88
 // readColor K:1411-1442 plus the radial-gradient substance (evaluated at the
 // integer pixel position like a picture texel).
 __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int py, uint64_t sid, uint64_t type,
-                                            int& status) {
+                                            int& status, int64_t& texels) {
   if (sid >= in.n_substances) {
     status |= kStatusBadInput;
     return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -431,6 +434,7 @@ __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int 
       return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
     uchar4 p = *reinterpret_cast<const uchar4*>(in.pictures + o);
+    ++texels;
     return make_float4((float)p.x / 255.0f, (float)p.y / 255.0f, (float)p.z / 255.0f, (float)p.w / 255.0f);
   }
   return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -439,7 +443,8 @@ __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int 
 // determineColor K:1447-1513
 template <int SECTIONS>
 __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
-                                                 const uint32_t* shapeIdx, int px, int py, int& status) {
+                                                 const uint32_t* shapeIdx, int px, int py, int& status,
+                                                 int64_t& texels) {
   int topBit = in.max_shape;
   float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float4 next = base;
@@ -470,7 +475,7 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
         }
         shouldComposite = false;
       } else {
-        next = readColor(in, px, py, sid, tag & GUDNI_TAG_SUBSTANCE_MASK, status);
+        next = readColor(in, px, py, sid, tag & GUDNI_TAG_SUBSTANCE_MASK, status, texels);
         lastIsSet = comp == GUDNI_TAG_ADD || comp == GUDNI_TAG_CONTINUE;
       }
       lastId = sid;
@@ -589,8 +594,7 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 // K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
 template <int SECTIONS>
 __device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
-                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
-                                             int64_t* sectionCounter) {
+                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status) {
   Parse p;
   p.current = 0;
   p.numActive = 0;
@@ -607,6 +611,7 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   int py = c.deltaY;
   uint32_t* outp = in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
   int64_t sections = 0;
+  int64_t texels = 0;
   for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
     int guard = 0;
@@ -628,7 +633,7 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       }
       p.sStartX = p.sEndX;
       p.sEndX = nextX;
-      const float4 color = determineColor(in, stack, shapeIdx, px, py, status);
+      const float4 color = determineColor(in, stack, shapeIdx, px, py, status, texels);
       float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
       if (in.stochastic != 0.0f) {  // getRandom K:1608-1613
         cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);
@@ -650,7 +655,10 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
     p.sStartY = p.pixelY;
     py += 1;
   }
-  if (sectionCounter) atomicAdd(reinterpret_cast<unsigned long long*>(sectionCounter), (unsigned long long)sections);
+  if (in.counters) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[0]), (unsigned long long)sections);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[1]), (unsigned long long)texels);
+  }
 }
 
 }  // namespace gudni

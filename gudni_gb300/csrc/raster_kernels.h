@@ -26,7 +26,6 @@ struct ColumnLaunch {
   uint32_t overflow_cap;
   uint32_t* overflow_count;
   int* status;                // kStatus* bits
-  int64_t* section_counter;   // optional: sections scanned
 };
 
 int sections_for(int max_shape);

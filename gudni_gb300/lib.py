@@ -131,6 +131,12 @@ def _copy(ptr, count, dtype) -> np.ndarray:
 
 
 # ------------------------------------------------------------------ CUDA library
+class JobDesc(C.Structure):
+    """gudni_job_desc."""
+    _fields_ = [("shapes", C.c_void_p), ("n_shapes", C.c_size_t), ("tiles", C.c_void_p),
+                ("n_tiles", C.c_size_t), ("columns_to_alloc", C.c_int32)]
+
+
 def cuda_library_path() -> str:
     return _build.CUDA_LIB
 
@@ -164,6 +170,16 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_sync_status.argtypes = [vp]
     lib.gudni_scratch_bytes.restype = sz
     lib.gudni_scratch_bytes.argtypes = [vp]
+    lib.gudni_raster_frame.restype = C.c_int
+    lib.gudni_raster_frame.argtypes = [vp, C.POINTER(JobDesc), sz, i32, i32, i32, i32, vp, vp]
+    lib.gudni_raster_tiles_device.restype = C.c_int
+    lib.gudni_raster_tiles_device.argtypes = [vp, vp, sz, vp, vp, sz, i32, i32, i32, i32, vp, vp, vp]
+    lib.gudni_enable_counters.restype = C.c_int
+    lib.gudni_enable_counters.argtypes = [vp, C.c_int]
+    lib.gudni_read_counters.restype = C.c_int
+    lib.gudni_read_counters.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.gudni_launch_count.restype = C.c_uint64
+    lib.gudni_launch_count.argtypes = [vp]
     _cuda = lib
     return lib
 

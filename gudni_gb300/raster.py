@@ -81,6 +81,41 @@ class Rasterizer:
             self.raster_job(frame, j, out, frame_number)
         return out
 
+    def raster_frame(self, frame, out: Optional[np.ndarray] = None, frame_number: int = 0,
+                     upload_common: bool = True) -> np.ndarray:
+        """All jobs of a frame in one launch (host buffers)."""
+        if out is None:
+            out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
+        assert out.dtype == np.uint32 and out.flags.c_contiguous and out.size == frame.canvas_w * frame.canvas_h
+        if upload_common:
+            self.upload_common(frame)
+        descs = (L.JobDesc * max(1, len(frame.jobs)))()
+        for i, j in enumerate(frame.jobs):
+            descs[i] = L.JobDesc(L.ptr(j.shapes), len(j.shapes), L.ptr(j.tiles), len(j.tiles), j.columns)
+        bg = np.ascontiguousarray(frame.background, np.float32)
+        self._check(self.lib.gudni_raster_frame(self.ctx, descs, len(frame.jobs), frame.canvas_w, frame.canvas_h,
+                                                frame.compute_depth, frame_number, bg.ctypes.data, out.ctypes.data))
+        return out
+
+    def raster_tiles_device(self, frame, shapes_ptr: int, n_shapes: int, tiles_ptr: int, tile_jobs_ptr: int,
+                            n_tiles: int, out_ptr: int, stream: int = 0, frame_number: int = 0) -> None:
+        """Enqueue a whole frame whose concatenated piles are device-resident."""
+        bg = np.ascontiguousarray(frame.background, np.float32)
+        self._check(self.lib.gudni_raster_tiles_device(
+            self.ctx, shapes_ptr, n_shapes, tiles_ptr, tile_jobs_ptr or None, n_tiles, frame.canvas_w,
+            frame.canvas_h, frame.compute_depth, frame_number, bg.ctypes.data, out_ptr, stream or None))
+
+    def enable_counters(self, on: bool = True) -> None:
+        self._check(self.lib.gudni_enable_counters(self.ctx, 1 if on else 0))
+
+    def read_counters(self) -> dict:
+        c = (C.c_int64 * 4)()
+        self._check(self.lib.gudni_read_counters(self.ctx, c))
+        return {"sections": c[0], "texels": c[1], "thresholds": c[2], "max_shape_bits": c[3]}
+
+    def launch_count(self) -> int:
+        return int(self.lib.gudni_launch_count(self.ctx))
+
     def raster_job_device(self, frame, job_index: int, shapes_ptr: int, tiles_ptr: int, out_ptr: int,
                           stream: int = 0, frame_number: int = 0) -> None:
         """Enqueue one job with device-resident shapes/tiles/out (torch data_ptr()s)."""

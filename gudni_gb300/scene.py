@@ -488,3 +488,21 @@ def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndar
     return Frame(flat.canvas_w, flat.canvas_h, spec, flat.background.copy(), geo,
                  subs.reshape(-1, 4), flat.pictures.copy(), uses, rads,
                  np.ascontiguousarray(random_field, dtype=np.float32), jobs, stats)
+
+
+def concatenated_piles(frame: Frame):
+    """The frame's shape piles concatenated, tiles with their shape slices offset into
+    the concatenation, and the job index of every tile (the layout of
+    gudni_raster_tiles_device)."""
+    shapes, tiles, jobs = [], [], []
+    base = 0
+    for j, job in enumerate(frame.jobs):
+        shapes.append(job.shapes)
+        t = job.tiles.copy()
+        t["shape_start"] += np.uint32(base)
+        tiles.append(t)
+        jobs.append(np.full(len(t), j, np.int32))
+        base += len(job.shapes)
+    return (np.concatenate(shapes) if shapes else np.zeros(0, L.SHAPE_DTYPE),
+            np.concatenate(tiles) if tiles else np.zeros(0, L.TILE_DTYPE),
+            np.concatenate(jobs) if jobs else np.zeros(0, np.int32))

@@ -156,6 +156,44 @@ int gudni_raster_job_device(gudni_ctx* ctx,
                             const float background[4],
                             uint32_t* out, void* stream);
 
+/* One job of a frame, for gudni_raster_frame (a RasterJob, Raster/Job.hs:72-76). */
+typedef struct gudni_job_desc {
+    const gudni_shape* shapes;
+    size_t n_shapes;
+    const gudni_tile_info* tiles;
+    size_t n_tiles;
+    int32_t columns_to_alloc;
+} gudni_job_desc;
+
+/* Rasterize every job of a frame in one launch: the loop of queueRasterJobs
+ * (OpenCL/CallKernels.hs:218-242, zipWithM_ raster jobs [0..]) with the job index of
+ * jobs[i] equal to i.  Host pointers; the frame's tiles cover the canvas, so every
+ * pixel of `out` (bitmap_w*bitmap_h BGRA words) is written.  Blocks until done. */
+int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs,
+                       int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth,
+                       int32_t frame_number, const float background[4], uint32_t* out);
+
+/* Device-resident form of gudni_raster_frame: the jobs' shape piles concatenated in
+ * `shapes`, their tile piles concatenated in `tiles` with each tile's shape slice
+ * already offset into the concatenated shapes, and tile_jobs[t] the job index of tile
+ * t (may be NULL: all tiles belong to job 0).  Enqueued on `stream`. */
+int gudni_raster_tiles_device(gudni_ctx* ctx,
+                              const gudni_shape* shapes, size_t n_shapes,
+                              const gudni_tile_info* tiles, const int32_t* tile_jobs, size_t n_tiles,
+                              int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth,
+                              int32_t frame_number, const float background[4],
+                              uint32_t* out, void* stream);
+
+/* Work counters of the next launches, for measurement: when enabled, kernels add
+ * [0] sections scanned, [1] picture texels read, [2] thresholds generated,
+ * [3] largest shape-bit count of a column.  gudni_read_counters returns and clears
+ * them.  Counting costs a few atomics per column; it is off by default. */
+int gudni_enable_counters(gudni_ctx* ctx, int enable);
+int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
+
+/* Number of kernel launches this context has issued. */
+uint64_t gudni_launch_count(const gudni_ctx* ctx);
+
 /* Wait for the context's stream and return the accumulated device status
  * (GUDNI_OK or the first error raised by a kernel since the last call). */
 int gudni_sync_status(gudni_ctx* ctx);
