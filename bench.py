@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 raster path (gudni's generate -> sort -> render kernels).
+
+Workload (default): the 3840x2160 page -- 5000 glyph-like outlines plus 2000 random
+shapes, 30% with subtract combinators, 20% radial gradients, 10% textured from a
+seeded 1024x1024 RGBA8 noise picture (seeded synthetic data; the reference ships no
+scene data).  Raster spec: 32x32 tiles, 32 threads per tile, MAXTHRESHOLDS 4096,
+MAXSHAPE 127, 8 stack words.
+
+A step renders the whole frame (all of its jobs).
+  value  Mpixels/s with the frame's piles resident in HBM, one fused launch per frame
+         (gudni_raster_tiles_device), timed with CUDA events on the launching stream
+  e2e    the same metric through the frame-level C ABI call with HOST buffers
+         (gudni_upload_common + gudni_raster_frame from pinned memory, output read
+         back), timed on the host clock
+The L2 (126 MB) is flushed between timed steps by writing a 256 MB buffer.
+
+`--impl reference` times the reference's own kernels (Kernels.cl compiled for the
+CPU, oracle/_ref) -- or, where that translation unit is not present, the oracle's
+restatement -- on all host cores, one frame per step.
+
+Multi-GPU: frames are independent, so N ranks render N replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+UNIT = "Mpixels/s"
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "raster_columns_{}.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample-frames", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="page4k", choices=sorted(WORKLOADS))
+    return ap.parse_args()
+
+
+WORKLOADS = {
+    # the headline plain workload
+    "page4k": ("page_3840x2160_glyphs5000_shapes2000",
+               "Mpixels/s (plain single-frame raster, 3840x2160 page, <=1 LSB RGBA8)"),
+    # the small CPU-runnable plain workload: 512x512, 64 random shapes of 8-32 segments
+    "random512": ("random_512x512_shapes64",
+                  "Mpixels/s (plain single-frame raster, 512x512 64 shapes, <=1 LSB RGBA8)"),
+}
+
+
+def make_frame(workload: str = "page4k"):
+    from gudni_gb300 import lib as L
+    from gudni_gb300 import scene as S
+    from gudni_gb300 import scenes as G
+
+    spec = L.make_spec(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+                       stack_sections=8)
+    flat = G.glyph_page(seed=1) if workload == "page4k" else G.random_shapes(seed=0)
+    return S.serialize_flat(flat, spec)
+
+
+def config_dict(frame, workload="page4k"):
+    sp = frame.spec
+    return {"workload": WORKLOADS[workload][0], "canvas": [frame.canvas_w, frame.canvas_h],
+            "shapes": int(frame.stats["shapes"]), "strands": int(frame.stats["strands"]),
+            "tiles": int(frame.n_tiles), "jobs": len(frame.jobs),
+            "tile_size": sp.max_tile_size, "threads_per_tile": sp.threads_per_tile,
+            "max_thresholds": sp.max_thresholds, "max_shape": sp.max_shape,
+            "stack_sections": sp.stack_sections, "l2": "flushed between steps (256 MB write)",
+            "data": "synthetic, seeded"}
+
+
+def algorithmic_bytes(frame, texels: int) -> int:
+    """B_alg per frame: every tile reads its shape records and strand trees once, the
+    tile records, substance and picture-use records, the texels it samples, and
+    writes every pixel once."""
+    geo = frame.geometry
+    # bytes of each shape's strands, by walking the strand headers
+    shape_bytes = {}
+    total = 0
+    for job in frame.jobs:
+        for s in job.shapes:
+            key = (int(s["geo_start"]), int(s["num_strands"]))
+            if key not in shape_bytes:
+                off = key[0] * 16
+                nb = 0
+                for _ in range(key[1]):
+                    size = int(geo[off]) | (int(geo[off + 1]) << 8)
+                    nb += 8 * size
+                    off += 8 * size
+                shape_bytes[key] = nb
+            total += 16 + shape_bytes[key]
+        total += 32 * len(job.tiles)
+    total += 16 * len(frame.substances) + 24 * len(frame.picture_uses) + 48 * len(frame.radials)
+    total += 4 * texels + 4 * frame.canvas_w * frame.canvas_h
+    return int(total)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    path = PROFILE_SUMMARY.format(WORKLOADS[workload][0])
+    if os.path.isfile(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch"), d
+    return None, None
+
+
+def cpu_baseline(frame, frames: int):
+    """The reference kernels (or the oracle restatement) on all host cores, one frame
+    per sample; returns (Mpixels/s, kind, cores, image)."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    st = {}
+    img = O.render_frame(frame, stats=st)  # oracle pass: sizes the reference's slabs, parity image
+    kind = "port"
+    fn = lambda: O.render_frame(frame)  # noqa: E731
+    try:
+        if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
+            cap = int(st["max_queue"]) + 16
+            O.ref_render_frame(frame, max_thresholds=cap)  # build + warm
+            fn = lambda: O.ref_render_frame(frame, max_thresholds=cap)  # noqa: E731
+            kind = "reference"
+    except Exception:
+        kind = "port"
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        fn()
+    dt = (time.perf_counter() - t0) / frames
+    return frame.canvas_w * frame.canvas_h / dt / 1e6, kind, cores, img, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    frame = make_frame(args.workload)
+    from oracle import oracle as O
+    st = {}
+    O.render_frame(frame, stats=st)
+    cap = int(st["max_queue"]) + 16
+    kind = "port"
+    fn = lambda: O.render_frame(frame)  # noqa: E731
+    if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
+        try:
+            O.ref_render_frame(frame, max_thresholds=cap)
+            fn = lambda: O.ref_render_frame(frame, max_thresholds=cap)  # noqa: E731
+            kind = "reference"
+        except Exception:
+            kind = "port"
+    for _ in range(args.warmup):
+        fn()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fn()
+        times.append(time.perf_counter() - t0)
+    ms = 1000 * sum(times) / len(times)
+    v = frame.canvas_w * frame.canvas_h / (ms / 1000) / 1e6
+    cores = os.cpu_count() or 1
+    sample = "one full frame per step (all jobs), OpenMP over all host cores"
+    line = {"impl": "reference", "metric": WORKLOADS[args.workload][1], "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(frame, args.workload),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from gudni_gb300 import lib as L
+    from gudni_gb300 import scene as S
+    from gudni_gb300.raster import Rasterizer
+
+    frame = make_frame(args.workload)
+    shapes, tiles, tile_jobs = S.concatenated_piles(frame)
+    r = Rasterizer(frame.spec, device=local)
+    r.upload_common(frame)
+    d_shapes = torch.from_numpy(shapes.view(np.uint8).copy()).to(dev)
+    d_tiles = torch.from_numpy(tiles.view(np.uint8).copy()).to(dev)
+    d_jobs = torch.from_numpy(tile_jobs.copy()).to(dev)
+    d_out = torch.zeros(frame.canvas_w * frame.canvas_h, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        r.raster_tiles_device(frame, d_shapes.data_ptr(), len(shapes), d_tiles.data_ptr(), d_jobs.data_ptr(),
+                              len(tiles), d_out.data_ptr(), stream=stream.cuda_stream)
+
+    # one counted launch (untimed) for the work figures
+    r.enable_counters(True)
+    step()
+    torch.cuda.synchronize()
+    counters = r.read_counters()
+    r.enable_counters(False)
+    r.sync_status()
+
+    for _ in range(args.warmup):
+        step()
+        flush.zero_()
+    torch.cuda.synchronize()
+    r.sync_status()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = r.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+            flush.zero_()  # L2 flush between timed steps (outside the events)
+        torch.cuda.synchronize()
+    barrier()
+    launches = r.launch_count() - launches0
+    r.sync_status()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    pixels = frame.canvas_w * frame.canvas_h
+    value = world * pixels / (ms / 1000) / 1e6
+
+    # end to end through the frame-level C ABI with pinned host buffers
+    def pinned(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        t.numpy()[:] = a.view(np.uint8).reshape(-1)
+        return t
+
+    import copy
+    hframe = copy.copy(frame)
+    keep = []
+    for name in ("geometry", "substances", "pictures", "picture_uses", "radials", "random_field"):
+        a = getattr(frame, name)
+        t = pinned(np.ascontiguousarray(a))
+        keep.append(t)
+        setattr(hframe, name, t.numpy().view(a.dtype).reshape(a.shape))
+    hjobs = []
+    for j in frame.jobs:
+        ts, tt = pinned(j.shapes), pinned(j.tiles)
+        keep += [ts, tt]
+        hjobs.append(S.Job(ts.numpy().view(L.SHAPE_DTYPE), tt.numpy().view(L.TILE_DTYPE), j.columns))
+    hframe.jobs = hjobs
+    out_pin = torch.empty(pixels * 4, dtype=torch.uint8, pin_memory=True)
+    out_np = out_pin.numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
+    for _ in range(args.warmup):
+        r.raster_frame(hframe, out=out_np)
+    barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.raster_frame(hframe, out=out_np)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = (frame.geometry.nbytes + frame.substances.nbytes + frame.pictures.nbytes + frame.picture_uses.nbytes +
+           frame.radials.nbytes + frame.random_field.nbytes + shapes.nbytes + tiles.nbytes + tile_jobs.nbytes)
+    e2e = {"value": world * pixels / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(pixels * 4), "ms_per_step": 1000 * e2e_s,
+           "call": "gudni_upload_common + gudni_raster_frame (host buffers)"}
+
+    if rank != 0:
+        r.close()
+        return 0
+
+    gpu_img = d_out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
+    b_alg = algorithmic_bytes(frame, counters["texels"])
+    peak, peak_src = measured_peaks()
+    achieved = b_alg / (ms / 1000) / 1e9
+    traffic, prof = profile_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "algorithmic_bytes_per_launch": b_alg,
+                "peak_source": f"{peak_src} (hbm_gbs burst)",
+                "kernel": "raster_columns_kernel (one fused launch per frame)",
+                "note": "the scan is divergent scalar FP32/INT work; SM issue utilisation, not HBM, bounds it"}
+    if prof:
+        roofline["profile"] = {k: prof[k] for k in prof if k != "dram_bytes_per_launch"}
+
+    line = {"metric": WORKLOADS[args.workload][1], "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(frame, args.workload),
+            "frames_per_s": 1000.0 / ms * world, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks.summary(), "roofline": roofline,
+            "work": {"thresholds": counters["thresholds"], "sections": counters["sections"],
+                     "texels": counters["texels"], "max_shape_bits": counters["max_shape_bits"],
+                     "sections_per_s": counters["sections"] / (ms / 1000)},
+            "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
+    if world == 1 and not args.no_cpu_baseline:
+        v, kind, cores, img, dt = cpu_baseline(frame, args.cpu_sample_frames)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+                                "sample": f"{args.cpu_sample_frames} full frame(s), {dt:.2f} s each"}
+        d = np.abs(gpu_img.view(np.uint8).astype(np.int16) - img.view(np.uint8).astype(np.int16))
+        line["parity_vs_oracle"] = {"max_lsb": int(d.max()),
+                                    "exact_pixel_frac": float(np.mean(np.all(d.reshape(-1, 4) == 0, axis=1)))}
+    print(json.dumps(line))
+    r.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -94,6 +94,7 @@ struct gudni_ctx {
   int pending_status = 0;
   cudaStream_t last_stream = nullptr;  // stream of the last enqueued job
   bool counters_on = false;
+  size_t fallback_slots = 0;
   uint64_t launches = 0;
   DevBuf<int32_t> tile_jobs;           // frame launches: job index per tile
   std::vector<gudni_shape> h_shapes;   // frame launches: concatenated host piles
@@ -214,26 +215,45 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   return in;
 }
 
-// Enqueue the fast pass; `sync_fallback` then reads the overflow count and runs the
-// full-capacity pass over the recorded columns.
+// Scratch for the full-capacity pass: a fixed pool of slots (at most ~512 MB).
+int ensure_fallback_pool(gudni_ctx* ctx) {
+  if (ctx->fallback_slots) return GUDNI_OK;
+  const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
+  size_t slots = ((size_t)512 << 20) / per_slot;
+  slots = std::min<size_t>(slots, (size_t)ctx->grid * gudni::kRasterBlock);
+  slots = std::max<size_t>(gudni::kRasterBlock, (slots / gudni::kRasterBlock) * gudni::kRasterBlock);
+  cudaError_t e;
+  if ((e = ctx->big_thr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_hdr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_idx.reserve(slots * ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  ctx->fallback_slots = slots;
+  return GUDNI_OK;
+}
+
+// Enqueue the fast pass and the full-capacity pass over the columns the fast pass
+// could not hold.  No host synchronisation: the second launch reads the overflow
+// count on the device.
 int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, cudaStream_t stream) {
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
   const uint32_t n_items = (uint32_t)(n_tiles * (size_t)ctx->spec.threads_per_tile);
-  cudaError_t e;
-  if ((e = ctx->overflow_items.reserve(std::max<uint32_t>(n_items, 1))) != cudaSuccess)
-    return cuda_fail(ctx, e, "overflow list");
-  if ((e = cudaMemsetAsync(ctx->overflow_count.ptr, 0, sizeof(uint32_t), stream)) != cudaSuccess)
-    return cuda_fail(ctx, e, "memset");
   if (n_items == 0) return GUDNI_OK;
+  cudaError_t e;
+  const bool need_fallback = ctx->working_capacity < ctx->spec.max_thresholds;
+  if (need_fallback) {
+    if ((e = ctx->overflow_items.reserve(n_items)) != cudaSuccess) return cuda_fail(ctx, e, "overflow list");
+    if ((e = cudaMemsetAsync(ctx->overflow_count.ptr, 0, sizeof(uint32_t), stream)) != cudaSuccess)
+      return cuda_fail(ctx, e, "memset");
+    if ((rc = ensure_fallback_pool(ctx))) return rc;
+  }
   ColumnLaunch a;
   a.in = in;
   a.scratch = gudni::ColumnScratch{ctx->thr.ptr, ctx->hdr.ptr, ctx->idx.ptr, ctx->working_capacity,
                                    ctx->spec.max_shape};
   a.items = nullptr;
   a.n_items = n_items;
-  const bool fast_is_full = ctx->working_capacity >= ctx->spec.max_thresholds;
-  a.overflow_items = fast_is_full ? nullptr : ctx->overflow_items.ptr;
+  a.n_items_dev = nullptr;
+  a.overflow_items = need_fallback ? ctx->overflow_items.ptr : nullptr;
   a.overflow_cap = n_items;
   a.overflow_count = ctx->overflow_count.ptr;
   a.status = ctx->status.ptr;
@@ -242,37 +262,18 @@ int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, c
   if ((e = gudni::launch_columns(a, ctx->sections, grid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "raster launch");
   ctx->launches += 1;
-  return GUDNI_OK;
-}
-
-int run_fallback(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, cudaStream_t stream) {
-  uint32_t count = 0;
-  cudaError_t e = cudaMemcpyAsync(&count, ctx->overflow_count.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
-  // the list holds at most one entry per work item (a larger count already raised
-  // the overflow status in the kernel)
-  count = std::min<uint32_t>(count, (uint32_t)(n_tiles * (size_t)ctx->spec.threads_per_tile));
-  if (count == 0) return GUDNI_OK;
-  // slots for the full-capacity pass: bounded so the pass holds at most ~2 GB
-  const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
-  size_t slots = std::max<size_t>(gudni::kRasterBlock, ((size_t)2 << 30) / per_slot);
-  slots = std::min<size_t>(slots, ((size_t)count + gudni::kRasterBlock - 1) / gudni::kRasterBlock * gudni::kRasterBlock);
-  slots = (slots / gudni::kRasterBlock) * gudni::kRasterBlock;
-  if ((e = ctx->big_thr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  if ((e = ctx->big_hdr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  if ((e = ctx->big_idx.reserve(slots * ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  ColumnLaunch a;
-  a.in = in;
-  a.scratch = gudni::ColumnScratch{ctx->big_thr.ptr, ctx->big_hdr.ptr, ctx->big_idx.ptr, ctx->spec.max_thresholds,
+  if (!need_fallback) return GUDNI_OK;
+  ColumnLaunch f = a;
+  f.scratch = gudni::ColumnScratch{ctx->big_thr.ptr, ctx->big_hdr.ptr, ctx->big_idx.ptr, ctx->spec.max_thresholds,
                                    ctx->spec.max_shape};
-  a.items = ctx->overflow_items.ptr;
-  a.n_items = count;
-  a.overflow_items = nullptr;
-  a.overflow_cap = 0;
-  a.overflow_count = nullptr;
-  a.status = ctx->status.ptr;
-  if ((e = gudni::launch_columns(a, ctx->sections, (int)(slots / gudni::kRasterBlock), stream)) != cudaSuccess)
+  f.items = ctx->overflow_items.ptr;
+  f.n_items = n_items;
+  f.n_items_dev = ctx->overflow_count.ptr;
+  f.overflow_items = nullptr;
+  f.overflow_cap = 0;
+  f.overflow_count = nullptr;
+  const int fgrid = (int)std::min<size_t>(ctx->fallback_slots / gudni::kRasterBlock, blocks_needed);
+  if ((e = gudni::launch_columns(f, ctx->sections, std::max(fgrid, 1), stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "fallback launch");
   ctx->launches += 1;
   return GUDNI_OK;
@@ -419,7 +420,6 @@ int gudni_raster_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, n_shapes, ctx->tiles.ptr, n_tiles, bitmap_w, bitmap_h,
                                   compute_depth, job_index, background, ctx->out.ptr);
   if ((rc = enqueue_job(ctx, in, n_tiles, ctx->stream))) return rc;
-  if ((rc = run_fallback(ctx, in, n_tiles, ctx->stream))) return rc;
   cudaError_t e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
   return read_status(ctx, ctx->stream);
@@ -442,9 +442,6 @@ int gudni_raster_job_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth,
                                   job_index, background, out);
   if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
-  if (ctx->working_capacity < ctx->spec.max_thresholds) {
-    if ((rc = run_fallback(ctx, in, n_tiles, s))) return rc;
-  }
   return GUDNI_OK;
 }
 
@@ -501,7 +498,6 @@ int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs
                                   bitmap_w, bitmap_h, compute_depth, 0, background, ctx->out.ptr);
   in.tile_jobs = ctx->tile_jobs.ptr;
   if ((rc = enqueue_job(ctx, in, ctx->h_tiles.size(), ctx->stream))) return rc;
-  if ((rc = run_fallback(ctx, in, ctx->h_tiles.size(), ctx->stream))) return rc;
   e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
   return read_status(ctx, ctx->stream);
@@ -525,9 +521,6 @@ int gudni_raster_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t 
                                   background, out);
   in.tile_jobs = tile_jobs;
   if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
-  if (ctx->working_capacity < ctx->spec.max_thresholds) {
-    if ((rc = run_fallback(ctx, in, n_tiles, s))) return rc;
-  }
   return GUDNI_OK;
 }
 

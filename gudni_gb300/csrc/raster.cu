@@ -14,8 +14,10 @@
 //
 // Capacity: the fast pass uses a small working capacity.  A column that needs more
 // is recorded in an overflow list and re-run by a second launch of the same kernel
-// with the spec's full max_thresholds; the result does not depend on the capacity,
-// only on whether it suffices.  A column that exceeds max_thresholds raises
+// with the spec's full max_thresholds; the second launch reads the list's length on
+// the device, so the pair is enqueued without a host round trip (and can be captured
+// in a CUDA graph).  The result does not depend on the capacity, only on whether it
+// suffices.  A column that exceeds max_thresholds raises
 // kStatusOverflow (the reference silently writes past its slab there,
 // Kernels.cl:375-380, 1096-1103).
 
@@ -41,7 +43,9 @@ __global__ void __launch_bounds__(kRasterBlock) raster_columns_kernel(ColumnLaun
   uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
   const uint32_t tmask = (1u << a.in.log2_tpt) - 1u;
   int status = 0;
-  for (uint32_t w = slot; w < a.n_items; w += nslots) {
+  uint32_t n_items = a.n_items;
+  if (a.n_items_dev) n_items = min(n_items, *a.n_items_dev);
+  for (uint32_t w = slot; w < n_items; w += nslots) {
     const uint32_t item = a.items ? a.items[w] : w;
     const int tile = (int)(item >> a.in.log2_tpt);
     const int column = (int)(item & tmask);

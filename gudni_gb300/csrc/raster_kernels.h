@@ -21,7 +21,8 @@ struct ColumnLaunch {
   RasterInputs in;
   ColumnScratch scratch;
   const uint32_t* items;      // optional explicit work-item list
-  uint32_t n_items;           // tiles * threads_per_tile, or the list's length
+  uint32_t n_items;           // tiles * threads_per_tile, or the list's capacity
+  const uint32_t* n_items_dev;  // optional: the list's length, read on the device
   uint32_t* overflow_items;   // where columns that overflow `capacity` are recorded
   uint32_t overflow_cap;
   uint32_t* overflow_count;

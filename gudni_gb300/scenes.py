@@ -108,6 +108,27 @@ def random_shape_specs(rng, width, height, n_shapes, seg_lo=8, seg_hi=32,
     return specs
 
 
+def local_shape_specs(rng, width, height, n_shapes, seg_lo=8, seg_hi=32, size_lo=16.0,
+                      size_hi=1024.0) -> List[ShapeSpec]:
+    """Random closed shapes like random_shape_specs, but each confined to a box of
+    side log-uniform in [size_lo, size_hi] placed uniformly on the canvas, so the
+    shapes per tile vary strongly across the canvas."""
+    specs = []
+    for _ in range(n_shapes):
+        n = int(rng.integers(seg_lo, seg_hi + 1))
+        side = np.float32(np.exp(rng.uniform(np.log(size_lo), np.log(size_hi))))
+        ox = np.float32(rng.random() * width) - side / 2
+        oy = np.float32(rng.random() * height) - side / 2
+        pts = rng.random((n, 4), dtype=np.float32) * side
+        pts[:, 0::2] += ox
+        pts[:, 1::2] += oy
+        rgb = rng.random(3, dtype=np.float32)
+        a = np.float32(0.3 + 0.7 * rng.random(dtype=np.float32))
+        specs.append(ShapeSpec([[pts.astype(np.float32)]], [S.ADD], 0,
+                               (float(rgb[0]), float(rgb[1]), float(rgb[2]), float(a))))
+    return specs
+
+
 WHITE = (1.0, 1.0, 1.0, 1.0)
 
 
@@ -156,8 +177,10 @@ def glyph_page(seed=1, width=3840, height=2160, n_glyphs=5000, n_shapes=2000,
                subtract_frac=0.3, radial_frac=0.2, texture_frac=0.1) -> S.FlatScene:
     """The 4K page: n_glyphs glyph-like outlines (2 contours of 10-40 quadratic
     segments, em size log-uniform 12-48 px) laid out in lines, plus n_shapes random
-    shapes; subtract_frac of the substances subtract a smaller second shape,
-    radial_frac use a radial gradient, texture_frac a seeded 1024^2 noise texture."""
+    shapes of 8-32 segments each confined to a box of side log-uniform 16-1024 px;
+    subtract_frac of the substances subtract a smaller second shape, radial_frac use
+    a radial gradient, texture_frac a seeded 1024^2 noise texture.  Substances are
+    shuffled into one z-order."""
     rng = _rng(seed)
     specs: List[ShapeSpec] = []
     x, y, line_h = 8.0, 8.0, 0.0
@@ -176,7 +199,7 @@ def glyph_page(seed=1, width=3840, height=2160, n_glyphs=5000, n_shapes=2000,
                                subtract_frac, radial_frac, texture_frac, em))
         x += em * 0.8
         line_h = max(line_h, em)
-    for sp in random_shape_specs(rng, width, height, n_shapes, 8, 32):
+    for sp in local_shape_specs(rng, width, height, n_shapes, 8, 32):
         specs.append(_decorate(rng, sp, width, height, subtract_frac, radial_frac, texture_frac,
                                float(min(width, height)) / 8))
     order = rng.permutation(len(specs))
