@@ -276,7 +276,11 @@ def main():
     d_jobs = torch.from_numpy(tile_jobs.copy()).to(dev)
     d_out = torch.zeros(frame.canvas_w * frame.canvas_h, dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # one dedicated stream for the kernels, the events and the L2 flushes
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize()  # inputs were copied on the default stream
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
 
     def step():
         r.raster_tiles_device(frame, d_shapes.data_ptr(), len(shapes), d_tiles.data_ptr(), d_jobs.data_ptr(),

@@ -2,9 +2,14 @@
 //
 // A context owns its device, stream, the uploaded common buffers, per-job staging
 // buffers and the threshold scratch.  Scratch is sized for the resident grid
-// (SMs x resident blocks x block), not for the job: each resident thread reuses one
-// slot for every column it runs.  This replaces the reference's per-job allocation of
-// columns x MAXTHRESHOLDS thresholds (OpenCL/CallKernels.hs:124-127).
+// (SMs x resident blocks x 128 threads), not for the job: each resident thread reuses
+// one slot for every column it runs.  This replaces the reference's per-job
+// allocation of columns x MAXTHRESHOLDS thresholds (OpenCL/CallKernels.hs:124-127).
+//
+// Every launch is a pair on one stream: the fast pass over the tiles and the
+// full-capacity pass over the columns that overflowed it (raster.cu).  Nothing
+// between them, or after them, waits on the host until the caller asks for the
+// output or the status.
 
 #include <cuda_runtime.h>
 
@@ -13,13 +18,14 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <vector>
 
 #include "gudni_cuda.h"
 #include "raster_kernels.h"
 
-using gudni::ColumnLaunch;
+using gudni::TileLaunch;
 
 namespace {
 
@@ -75,31 +81,45 @@ struct gudni_ctx {
   DevBuf<float> random_field;
   bool has_random = false;
 
-  // per-job staging
+  // per-job / per-frame staging
   DevBuf<gudni_shape> shapes;
   DevBuf<gudni_tile_info> tiles;
+  DevBuf<int32_t> tile_jobs;
   DevBuf<uint32_t> out;
+  std::vector<gudni_shape> h_shapes;
+  std::vector<gudni_tile_info> h_tiles;
+  std::vector<int32_t> h_tile_jobs;
 
-  // scratch: fast pass (grid slots x working capacity), fallback (list x max_thresholds)
+  // batch
+  bool batch_ready = false;
+  size_t batch_tiles = 0;
+  size_t batch_shapes = 0;
+  size_t batch_scenes = 0;
+  size_t batch_pixels = 0;
+  DevBuf<gudni_shape> b_shapes;
+  DevBuf<gudni_tile_info> b_tiles;
+  DevBuf<int32_t> b_tile_scene;
+  DevBuf<uint32_t> b_order;
+  DevBuf<gudni::SceneInfo> b_scenes;
+  DevBuf<uint32_t> b_out;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+
+  // scratch: fast pass (grid slots x working capacity), full-capacity pool
   DevBuf<float4> thr;
   DevBuf<uint32_t> hdr;
   DevBuf<uint32_t> idx;
   DevBuf<float4> big_thr;
   DevBuf<uint32_t> big_hdr;
   DevBuf<uint32_t> big_idx;
+  size_t fallback_slots = 0;
   DevBuf<uint32_t> overflow_items;
-  DevBuf<uint32_t> overflow_count;
+  DevBuf<uint32_t> words;   // [0] overflow count, [1] next tile
   DevBuf<int> status;
   DevBuf<int64_t> counters;
-  int pending_status = 0;
-  cudaStream_t last_stream = nullptr;  // stream of the last enqueued job
   bool counters_on = false;
-  size_t fallback_slots = 0;
   uint64_t launches = 0;
-  DevBuf<int32_t> tile_jobs;           // frame launches: job index per tile
-  std::vector<gudni_shape> h_shapes;   // frame launches: concatenated host piles
-  std::vector<gudni_tile_info> h_tiles;
-  std::vector<int32_t> h_tile_jobs;
+  cudaStream_t last_stream = nullptr;
 };
 
 namespace {
@@ -110,7 +130,8 @@ int fail(gudni_ctx* ctx, int code, const std::string& msg) {
 }
 
 int cuda_fail(gudni_ctx* ctx, cudaError_t e, const char* what) {
-  return fail(ctx, GUDNI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  return fail(ctx, e == cudaErrorMemoryAllocation ? GUDNI_ERR_OUT_OF_MEMORY : GUDNI_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
 }
 
 int status_to_code(int bits) {
@@ -121,7 +142,7 @@ int status_to_code(int bits) {
 }
 
 const char* status_message(int bits) {
-  if (bits & gudni::kStatusBadInput) return "a shape, strand, substance or picture record points outside its buffer";
+  if (bits & gudni::kStatusBadInput) return "a shape, strand, substance, picture or tile record points outside its buffer";
   if (bits & gudni::kStatusOverflow) return "a column needed more thresholds than max_thresholds";
   if (bits & gudni::kStatusIterLimit) return "a device loop hit its iteration cap";
   return "";
@@ -130,7 +151,10 @@ const char* status_message(int bits) {
 bool valid_spec(const gudni_spec* s, std::string& why) {
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!s) { why = "null spec"; return false; }
-  if (!pow2(s->threads_per_tile) || s->threads_per_tile > (1 << 20)) { why = "threads_per_tile must be a power of two"; return false; }
+  if (!pow2(s->threads_per_tile) || s->threads_per_tile > (1 << gudni::kMaxLog2Tpt)) {
+    why = "threads_per_tile must be a power of two <= 1024";
+    return false;
+  }
   if (s->max_thresholds < 4) { why = "max_thresholds must be >= 4"; return false; }
   if (s->max_shape < 1 || s->max_shape > 64 * 32 - 1) { why = "max_shape must be in [1, 2047]"; return false; }
   if (s->stack_sections < 1 || s->max_shape > 64 * s->stack_sections - 1) {
@@ -152,10 +176,38 @@ int ensure_scratch(gudni_ctx* ctx) {
     if ((e = ctx->status.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "status word");
     if ((e = cudaMemset(ctx->status.ptr, 0, sizeof(int))) != cudaSuccess) return cuda_fail(ctx, e, "status word");
   }
-  if ((e = ctx->overflow_count.reserve(1)) != cudaSuccess) return cuda_fail(ctx, e, "overflow count");
+  if (!ctx->words.ptr) {
+    if ((e = ctx->words.reserve(2)) != cudaSuccess) return cuda_fail(ctx, e, "work counters");
+    if ((e = cudaMemset(ctx->words.ptr, 0, 2 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(ctx, e, "work counters");
+  }
   if (!ctx->counters.ptr) {
     if ((e = ctx->counters.reserve(4)) != cudaSuccess) return cuda_fail(ctx, e, "counters");
     if ((e = cudaMemset(ctx->counters.ptr, 0, 4 * sizeof(int64_t))) != cudaSuccess) return cuda_fail(ctx, e, "counters");
+  }
+  return GUDNI_OK;
+}
+
+// Scratch for the full-capacity pass: a fixed pool of slots (at most ~512 MB).
+int ensure_fallback_pool(gudni_ctx* ctx) {
+  if (ctx->fallback_slots) return GUDNI_OK;
+  const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
+  size_t slots = ((size_t)512 << 20) / per_slot;
+  slots = std::min<size_t>(slots, (size_t)ctx->grid * gudni::kRasterBlock);
+  slots = std::max<size_t>(gudni::kRasterBlock, (slots / gudni::kRasterBlock) * gudni::kRasterBlock);
+  cudaError_t e;
+  if ((e = ctx->big_thr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_hdr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  if ((e = ctx->big_idx.reserve(slots * ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
+  ctx->fallback_slots = slots;
+  return GUDNI_OK;
+}
+
+int validate_tiles_host(gudni_ctx* ctx, const gudni_tile_info* tiles, size_t n_tiles, size_t n_shapes) {
+  for (size_t i = 0; i < n_tiles; ++i) {
+    const gudni_tile_info& t = tiles[i];
+    if ((uint64_t)t.shapes.start + t.shapes.length > n_shapes || t.hdepth < 0 || t.hdepth > 24 || t.vdepth < 0 ||
+        t.vdepth > 24 || t.left < 0 || t.top < 0)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(i) + " is malformed");
   }
   return GUDNI_OK;
 }
@@ -166,20 +218,14 @@ int validate_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes, con
   if (!ctx->common_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "gudni_upload_common has not been called");
   if (bitmap_w <= 0 || bitmap_h <= 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "bitmap size must be positive");
   if ((int64_t)bitmap_w * bitmap_h > (int64_t)1 << 31) return fail(ctx, GUDNI_ERR_BAD_INPUT, "bitmap too large");
-  if (compute_depth < 0 || compute_depth > 20 || (1 << compute_depth) != ctx->spec.threads_per_tile)
+  if (compute_depth < 0 || compute_depth > gudni::kMaxLog2Tpt || (1 << compute_depth) != ctx->spec.threads_per_tile)
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "compute_depth must be log2(threads_per_tile)");
   if (n_tiles > 0 && !tiles) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null tiles");
   if (n_shapes > 0 && !shapes) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null shapes");
-  if ((uint64_t)n_tiles * (uint64_t)ctx->spec.threads_per_tile >= (1ull << 32))
-    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many work items in one job");
-  if (host) {
-    for (size_t i = 0; i < n_tiles; ++i) {
-      const gudni_tile_info& t = tiles[i];
-      if ((uint64_t)t.shapes.start + t.shapes.length > n_shapes || t.hdepth < 0 || t.hdepth > 24 ||
-          t.vdepth < 0 || t.vdepth > 24 || t.left < 0 || t.top < 0)
-        return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(i) + " is malformed");
-    }
-  }
+  if (n_tiles >= ((size_t)1 << (32 - gudni::kColumnBits)))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles in one launch");
+  if (n_shapes > 0xFFFFFFFFull) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many shapes");
+  if (host) return validate_tiles_host(ctx, tiles, n_tiles, n_shapes);
   return GUDNI_OK;
 }
 
@@ -207,7 +253,8 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   in.bitmap_w = bitmap_w;
   in.bitmap_h = bitmap_h;
   in.job_index = job_index;
-  in.background = make_float4(background[0], background[1], background[2], background[3]);
+  in.background = background ? make_float4(background[0], background[1], background[2], background[3])
+                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   in.max_shape = ctx->spec.max_shape;
   in.out = d_out;
   in.tile_jobs = nullptr;
@@ -215,65 +262,55 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   return in;
 }
 
-// Scratch for the full-capacity pass: a fixed pool of slots (at most ~512 MB).
-int ensure_fallback_pool(gudni_ctx* ctx) {
-  if (ctx->fallback_slots) return GUDNI_OK;
-  const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
-  size_t slots = ((size_t)512 << 20) / per_slot;
-  slots = std::min<size_t>(slots, (size_t)ctx->grid * gudni::kRasterBlock);
-  slots = std::max<size_t>(gudni::kRasterBlock, (slots / gudni::kRasterBlock) * gudni::kRasterBlock);
-  cudaError_t e;
-  if ((e = ctx->big_thr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  if ((e = ctx->big_hdr.reserve(slots * ctx->spec.max_thresholds)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  if ((e = ctx->big_idx.reserve(slots * ctx->spec.max_shape)) != cudaSuccess) return cuda_fail(ctx, e, "fallback scratch");
-  ctx->fallback_slots = slots;
-  return GUDNI_OK;
-}
-
-// Enqueue the fast pass and the full-capacity pass over the columns the fast pass
-// could not hold.  No host synchronisation: the second launch reads the overflow
-// count on the device.
-int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, cudaStream_t stream) {
+// Enqueue the fast pass over `n_tiles` tiles and the full-capacity pass over the
+// columns that overflowed it.  `max_tpt` is the largest threads-per-tile in the
+// launch (sizes the overflow list).
+int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInfo* scenes,
+            const int32_t* tile_scene, size_t n_scenes, const uint32_t* order, size_t n_tiles, int max_tpt,
+            cudaStream_t stream) {
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
-  const uint32_t n_items = (uint32_t)(n_tiles * (size_t)ctx->spec.threads_per_tile);
-  if (n_items == 0) return GUDNI_OK;
-  cudaError_t e;
+  if (n_tiles == 0) return GUDNI_OK;
+  const size_t max_items = n_tiles * (size_t)max_tpt;
   const bool need_fallback = ctx->working_capacity < ctx->spec.max_thresholds;
+  cudaError_t e;
   if (need_fallback) {
-    if ((e = ctx->overflow_items.reserve(n_items)) != cudaSuccess) return cuda_fail(ctx, e, "overflow list");
-    if ((e = cudaMemsetAsync(ctx->overflow_count.ptr, 0, sizeof(uint32_t), stream)) != cudaSuccess)
-      return cuda_fail(ctx, e, "memset");
+    if ((e = ctx->overflow_items.reserve(max_items)) != cudaSuccess) return cuda_fail(ctx, e, "overflow list");
     if ((rc = ensure_fallback_pool(ctx))) return rc;
   }
-  ColumnLaunch a;
+  if ((e = cudaMemsetAsync(ctx->words.ptr, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess)
+    return cuda_fail(ctx, e, "memset");
+  TileLaunch a;
+  std::memset(&a, 0, sizeof(a));
   a.in = in;
+  a.scenes = scenes;
+  a.tile_scene = tile_scene;
+  a.n_scenes = (uint32_t)n_scenes;
   a.scratch = gudni::ColumnScratch{ctx->thr.ptr, ctx->hdr.ptr, ctx->idx.ptr, ctx->working_capacity,
                                    ctx->spec.max_shape};
-  a.items = nullptr;
-  a.n_items = n_items;
-  a.n_items_dev = nullptr;
+  a.order = order;
+  a.n_tiles = (uint32_t)n_tiles;
+  a.next_tile = ctx->words.ptr + 1;
   a.overflow_items = need_fallback ? ctx->overflow_items.ptr : nullptr;
-  a.overflow_cap = n_items;
-  a.overflow_count = ctx->overflow_count.ptr;
+  a.overflow_cap = (uint32_t)std::min<size_t>(max_items, 0xFFFFFFFFull);
+  a.overflow_count = ctx->words.ptr;
   a.status = ctx->status.ptr;
-  const uint32_t blocks_needed = (n_items + gudni::kRasterBlock - 1) / gudni::kRasterBlock;
-  const int grid = (int)std::min<uint32_t>(blocks_needed, (uint32_t)ctx->grid);
-  if ((e = gudni::launch_columns(a, ctx->sections, grid, stream)) != cudaSuccess)
+  const size_t warps_per_block = gudni::kRasterBlock / 32;
+  const int grid = (int)std::min<size_t>((n_tiles + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
+  if ((e = gudni::launch_raster(a, false, ctx->sections, grid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "raster launch");
   ctx->launches += 1;
   if (!need_fallback) return GUDNI_OK;
-  ColumnLaunch f = a;
+  TileLaunch f = a;
   f.scratch = gudni::ColumnScratch{ctx->big_thr.ptr, ctx->big_hdr.ptr, ctx->big_idx.ptr, ctx->spec.max_thresholds,
                                    ctx->spec.max_shape};
-  f.items = ctx->overflow_items.ptr;
-  f.n_items = n_items;
-  f.n_items_dev = ctx->overflow_count.ptr;
   f.overflow_items = nullptr;
-  f.overflow_cap = 0;
-  f.overflow_count = nullptr;
-  const int fgrid = (int)std::min<size_t>(ctx->fallback_slots / gudni::kRasterBlock, blocks_needed);
-  if ((e = gudni::launch_columns(f, ctx->sections, std::max(fgrid, 1), stream)) != cudaSuccess)
+  f.list = ctx->overflow_items.ptr;
+  f.list_count = ctx->words.ptr;
+  f.list_cap = a.overflow_cap;
+  const int fgrid = (int)std::max<size_t>(1, std::min<size_t>(ctx->fallback_slots / gudni::kRasterBlock,
+                                                              (max_items + gudni::kRasterBlock - 1) / gudni::kRasterBlock));
+  if ((e = gudni::launch_raster(f, true, ctx->sections, fgrid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "fallback launch");
   ctx->launches += 1;
   return GUDNI_OK;
@@ -281,17 +318,12 @@ int enqueue_job(gudni_ctx* ctx, const gudni::RasterInputs& in, size_t n_tiles, c
 
 int read_status(gudni_ctx* ctx, cudaStream_t stream) {
   int bits = 0;
-  if (!ctx->status.ptr) {
-    bits = ctx->pending_status;
-    ctx->pending_status = 0;
-    return bits ? fail(ctx, status_to_code(bits), status_message(bits)) : GUDNI_OK;
+  if (ctx->status.ptr) {
+    cudaError_t e = cudaMemcpyAsync(&bits, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "status read");
   }
-  cudaError_t e = cudaMemcpyAsync(&bits, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status.ptr, 0, sizeof(int), stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "status read");
-  bits |= ctx->pending_status;
-  ctx->pending_status = 0;
   if (bits) return fail(ctx, status_to_code(bits), status_message(bits));
   return GUDNI_OK;
 }
@@ -302,6 +334,45 @@ int upload(gudni_ctx* ctx, DevBuf<T>& buf, const void* src, size_t count, const 
   if (e == cudaSuccess && count) e = cudaMemcpyAsync(buf.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, what);
   return GUDNI_OK;
+}
+
+int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
+                          size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                          const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                          const gudni_radial* radials, size_t n_radials, const float* random_field) {
+  if ((geometry_bytes && !geometry) || (n_substances && !substances) || (picture_bytes && !pictures) ||
+      (n_picture_uses && !picture_uses) || (n_radials && !radials))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null buffer with non-zero size");
+  if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
+  for (size_t i = 0; i < n_picture_uses; ++i) {
+    const gudni_picture_use& u = picture_uses[i];
+    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 ||
+        (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
+  }
+  ctx->common_ready = false;
+  int rc;
+  if ((rc = upload(ctx, ctx->geometry, geometry, geometry_bytes, "geometry upload"))) return rc;
+  if ((rc = upload(ctx, ctx->substances, substances, n_substances, "substance upload"))) return rc;
+  if ((rc = upload(ctx, ctx->pictures, pictures, picture_bytes, "picture upload"))) return rc;
+  if ((rc = upload(ctx, ctx->uses, picture_uses, n_picture_uses, "picture use upload"))) return rc;
+  if ((rc = upload(ctx, ctx->radials, radials, n_radials, "radial upload"))) return rc;
+  ctx->has_random = random_field != nullptr;
+  if (random_field && (rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload")))
+    return rc;
+  ctx->geometry_bytes = geometry_bytes;
+  ctx->n_substances = n_substances;
+  ctx->picture_bytes = picture_bytes;
+  ctx->n_uses = n_picture_uses;
+  ctx->n_radials = n_radials;
+  return GUDNI_OK;
+}
+
+void drop_graph(gudni_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
 }
 
 }  // namespace
@@ -336,7 +407,7 @@ gudni_ctx* gudni_create(const gudni_spec* spec, int device) {
     return nullptr;
   }
   ctx->sections = gudni::sections_for(spec->max_shape);
-  if ((e = gudni::columns_occupancy(ctx->sections, &ctx->blocks_per_sm)) != cudaSuccess || ctx->blocks_per_sm < 1)
+  if ((e = gudni::raster_occupancy(ctx->sections, &ctx->blocks_per_sm)) != cudaSuccess || ctx->blocks_per_sm < 1)
     ctx->blocks_per_sm = 1;
   ctx->grid = ctx->sm_count * ctx->blocks_per_sm;
   ctx->working_capacity = std::min(spec->max_thresholds, 256);
@@ -351,11 +422,15 @@ void gudni_destroy(gudni_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drop_graph(ctx);
   ctx->geometry.release(); ctx->substances.release(); ctx->pictures.release(); ctx->uses.release();
   ctx->radials.release(); ctx->random_field.release(); ctx->shapes.release(); ctx->tiles.release();
-  ctx->out.release(); ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release();
-  ctx->big_hdr.release(); ctx->big_idx.release(); ctx->overflow_items.release();
-  ctx->overflow_count.release(); ctx->status.release(); ctx->counters.release(); ctx->tile_jobs.release();
+  ctx->tile_jobs.release(); ctx->out.release();
+  ctx->b_shapes.release(); ctx->b_tiles.release(); ctx->b_tile_scene.release(); ctx->b_order.release();
+  ctx->b_scenes.release(); ctx->b_out.release();
+  ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release(); ctx->big_hdr.release();
+  ctx->big_idx.release(); ctx->overflow_items.release(); ctx->words.release(); ctx->status.release();
+  ctx->counters.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -371,30 +446,11 @@ int gudni_upload_common(gudni_ctx* ctx, const void* geometry, size_t geometry_by
                         size_t n_radials, const float* random_field) {
   if (!ctx) return GUDNI_ERR_BAD_INPUT;
   cudaSetDevice(ctx->device);
-  if ((geometry_bytes && !geometry) || (n_substances && !substances) || (picture_bytes && !pictures) ||
-      (n_picture_uses && !picture_uses) || (n_radials && !radials))
-    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null buffer with non-zero size");
-  if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
-  for (size_t i = 0; i < n_picture_uses; ++i) {
-    const gudni_picture_use& u = picture_uses[i];
-    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 ||
-        (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
-      return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
-  }
-  ctx->common_ready = false;
-  int rc;
-  if ((rc = upload(ctx, ctx->geometry, geometry, geometry_bytes, "geometry upload"))) return rc;
-  if ((rc = upload(ctx, ctx->substances, substances, n_substances, "substance upload"))) return rc;
-  if ((rc = upload(ctx, ctx->pictures, pictures, picture_bytes, "picture upload"))) return rc;
-  if ((rc = upload(ctx, ctx->uses, picture_uses, n_picture_uses, "picture use upload"))) return rc;
-  if ((rc = upload(ctx, ctx->radials, radials, n_radials, "radial upload"))) return rc;
-  ctx->has_random = random_field != nullptr;
-  if (random_field && (rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload"))) return rc;
-  ctx->geometry_bytes = geometry_bytes;
-  ctx->n_substances = n_substances;
-  ctx->picture_bytes = picture_bytes;
-  ctx->n_uses = n_picture_uses;
-  ctx->n_radials = n_radials;
+  ctx->batch_ready = false;
+  drop_graph(ctx);
+  int rc = upload_common_buffers(ctx, geometry, geometry_bytes, substances, n_substances, pictures, picture_bytes,
+                                 picture_uses, n_picture_uses, radials, n_radials, random_field);
+  if (rc) return rc;
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "upload");
   ctx->common_ready = true;
@@ -419,7 +475,8 @@ int gudni_raster_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
   if ((rc = upload(ctx, ctx->out, out, pixels, "bitmap upload"))) return rc;
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, n_shapes, ctx->tiles.ptr, n_tiles, bitmap_w, bitmap_h,
                                   compute_depth, job_index, background, ctx->out.ptr);
-  if ((rc = enqueue_job(ctx, in, n_tiles, ctx->stream))) return rc;
+  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, ctx->stream)))
+    return rc;
   cudaError_t e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
   return read_status(ctx, ctx->stream);
@@ -434,31 +491,14 @@ int gudni_raster_job_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_
   int rc = validate_job(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, false);
   if (rc) return rc;
   if (!out || !background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null out or background");
-  cudaSetDevice(ctx->device);
   if (((uintptr_t)shapes & 7) != 0 || ((uintptr_t)tiles & 3) != 0 || ((uintptr_t)out & 3) != 0)
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "misaligned device pointer");
+  cudaSetDevice(ctx->device);
   cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
   ctx->last_stream = s;
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth,
                                   job_index, background, out);
-  if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
-  return GUDNI_OK;
-}
-
-int gudni_sync_status(gudni_ctx* ctx) {
-  if (!ctx) return GUDNI_ERR_BAD_INPUT;
-  cudaSetDevice(ctx->device);
-  if (ctx->last_stream && ctx->last_stream != ctx->stream) {
-    cudaError_t e = cudaStreamSynchronize(ctx->last_stream);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream sync");
-  }
-  return read_status(ctx, ctx->stream);
-}
-
-size_t gudni_scratch_bytes(const gudni_ctx* ctx) {
-  if (!ctx) return 0;
-  return ctx->thr.cap * sizeof(float4) + ctx->hdr.cap * 4 + ctx->idx.cap * 4 + ctx->big_thr.cap * sizeof(float4) +
-         ctx->big_hdr.cap * 4 + ctx->big_idx.cap * 4;
+  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, s);
 }
 
 int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs, int32_t bitmap_w,
@@ -484,8 +524,8 @@ int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs
       ctx->h_tile_jobs.push_back((int32_t)j);
     }
   }
-  if ((uint64_t)ctx->h_tiles.size() * (uint64_t)ctx->spec.threads_per_tile >= (1ull << 32))
-    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many work items in one frame");
+  if (ctx->h_tiles.size() >= ((size_t)1 << (32 - gudni::kColumnBits)))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles in one frame");
   cudaSetDevice(ctx->device);
   int rc;
   const size_t pixels = (size_t)bitmap_w * (size_t)bitmap_h;
@@ -497,7 +537,9 @@ int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, ctx->h_shapes.size(), ctx->tiles.ptr, ctx->h_tiles.size(),
                                   bitmap_w, bitmap_h, compute_depth, 0, background, ctx->out.ptr);
   in.tile_jobs = ctx->tile_jobs.ptr;
-  if ((rc = enqueue_job(ctx, in, ctx->h_tiles.size(), ctx->stream))) return rc;
+  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, ctx->h_tiles.size(), ctx->spec.threads_per_tile,
+                    ctx->stream)))
+    return rc;
   e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
   return read_status(ctx, ctx->stream);
@@ -520,15 +562,170 @@ int gudni_raster_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t 
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, 0,
                                   background, out);
   in.tile_jobs = tile_jobs;
-  if ((rc = enqueue_job(ctx, in, n_tiles, s))) return rc;
+  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, s);
+}
+
+int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
+                       size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                       const gudni_picture_use* picture_uses, size_t n_picture_uses, const gudni_radial* radials,
+                       size_t n_radials, const gudni_shape* shapes, size_t n_shapes, const gudni_tile_info* tiles,
+                       const int32_t* tile_scene, const float* tile_cost, size_t n_tiles,
+                       const gudni_batch_scene* scenes, size_t n_scenes, size_t out_pixels) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  ctx->batch_ready = false;
+  drop_graph(ctx);
+  if ((n_tiles && (!tiles || !tile_scene)) || (n_scenes && !scenes) || (n_shapes && !shapes))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null batch array");
+  if (n_tiles >= ((size_t)1 << (32 - gudni::kColumnBits))) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles");
+  int rc = validate_tiles_host(ctx, tiles, n_tiles, n_shapes);
+  if (rc) return rc;
+  int max_tpt = 1;
+  std::vector<gudni::SceneInfo> sc(n_scenes);
+  for (size_t i = 0; i < n_scenes; ++i) {
+    const gudni_batch_scene& b = scenes[i];
+    if (b.bitmap_w <= 0 || b.bitmap_h <= 0 || b.compute_depth < 0 || b.compute_depth > gudni::kMaxLog2Tpt ||
+        b.out_offset + (uint64_t)b.bitmap_w * (uint64_t)b.bitmap_h > out_pixels)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "batch scene " + std::to_string(i) + " is malformed");
+    sc[i].bitmap_w = b.bitmap_w;
+    sc[i].bitmap_h = b.bitmap_h;
+    sc[i].log2_tpt = b.compute_depth;
+    sc[i].job_index = b.job_index;
+    sc[i].out_offset = b.out_offset;
+    std::memcpy(sc[i].background, b.background, sizeof(sc[i].background));
+    max_tpt = std::max(max_tpt, 1 << b.compute_depth);
+  }
+  for (size_t t = 0; t < n_tiles; ++t)
+    if (tile_scene[t] < 0 || (size_t)tile_scene[t] >= n_scenes)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(t) + " names no scene");
+  // schedule: most expensive tiles first (longest-processing-time order)
+  std::vector<uint32_t> order(n_tiles);
+  std::iota(order.begin(), order.end(), 0u);
+  if (tile_cost) {
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return tile_cost[a] > tile_cost[b]; });
+  }
+  if ((rc = upload_common_buffers(ctx, geometry, geometry_bytes, substances, n_substances, pictures, picture_bytes,
+                                  picture_uses, n_picture_uses, radials, n_radials, nullptr)))
+    return rc;
+  if ((rc = upload(ctx, ctx->b_shapes, shapes, n_shapes, "batch shapes"))) return rc;
+  if ((rc = upload(ctx, ctx->b_tiles, tiles, n_tiles, "batch tiles"))) return rc;
+  if ((rc = upload(ctx, ctx->b_tile_scene, tile_scene, n_tiles, "batch tile scenes"))) return rc;
+  if ((rc = upload(ctx, ctx->b_order, order.data(), n_tiles, "batch order"))) return rc;
+  if ((rc = upload(ctx, ctx->b_scenes, sc.data(), n_scenes, "batch scenes"))) return rc;
+  cudaError_t e = ctx->b_out.reserve(out_pixels);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->b_out.ptr, 0, out_pixels * 4, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch upload");
+  if ((rc = ensure_scratch(ctx))) return rc;
+  if (ctx->working_capacity < ctx->spec.max_thresholds) {
+    if ((e = ctx->overflow_items.reserve(n_tiles * (size_t)max_tpt)) != cudaSuccess) return cuda_fail(ctx, e, "overflow list");
+    if ((rc = ensure_fallback_pool(ctx))) return rc;
+  }
+  ctx->common_ready = true;
+  ctx->batch_tiles = n_tiles;
+  ctx->batch_shapes = n_shapes;
+  ctx->batch_scenes = n_scenes;
+  ctx->batch_pixels = out_pixels;
+  ctx->batch_ready = true;
   return GUDNI_OK;
+}
+
+static int batch_enqueue(gudni_ctx* ctx, cudaStream_t s) {
+  gudni::RasterInputs in = inputs(ctx, ctx->b_shapes.ptr, ctx->batch_shapes, ctx->b_tiles.ptr, ctx->batch_tiles, 1,
+                                  1, 0, 0, nullptr, ctx->b_out.ptr);
+  int max_tpt = 1 << gudni::kMaxLog2Tpt;
+  if (ctx->overflow_items.cap && ctx->batch_tiles) max_tpt = (int)std::min<size_t>(max_tpt, ctx->overflow_items.cap / ctx->batch_tiles);
+  return enqueue(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr, ctx->batch_scenes, ctx->b_order.ptr,
+                 ctx->batch_tiles, max_tpt, s);
+}
+
+int gudni_batch_render(gudni_ctx* ctx, int use_graph, void* stream) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!ctx->batch_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "gudni_batch_upload has not been called");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  if (!use_graph || ctx->counters_on) return batch_enqueue(ctx, s);
+  if (!ctx->graph_exec) {
+    // capture the launch sequence once on the context's own stream
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    const uint64_t launches = ctx->launches;
+    int rc = batch_enqueue(ctx, ctx->stream);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    ctx->launches = launches;  // counted when replayed
+    ctx->graph = g;
+    if ((e = cudaGraphInstantiate(&ctx->graph_exec, g, 0)) != cudaSuccess) {
+      drop_graph(ctx);
+      return cuda_fail(ctx, e, "graph instantiate");
+    }
+  }
+  cudaError_t e = cudaGraphLaunch(ctx->graph_exec, s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
+  ctx->launches += ctx->working_capacity < ctx->spec.max_thresholds ? 2 : 1;
+  return GUDNI_OK;
+}
+
+int gudni_batch_render_tiles(gudni_ctx* ctx, size_t first_tile, size_t n_tiles, void* stream) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!ctx->batch_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "gudni_batch_upload has not been called");
+  if (first_tile > ctx->batch_tiles || n_tiles > ctx->batch_tiles - first_tile)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile range outside the batch");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  gudni::RasterInputs in = inputs(ctx, ctx->b_shapes.ptr, ctx->batch_shapes, ctx->b_tiles.ptr + first_tile, n_tiles,
+                                  1, 1, 0, 0, nullptr, ctx->b_out.ptr);
+  int max_tpt = 1 << gudni::kMaxLog2Tpt;
+  if (ctx->overflow_items.cap && ctx->batch_tiles) max_tpt = (int)std::min<size_t>(max_tpt, ctx->overflow_items.cap / ctx->batch_tiles);
+  return enqueue(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr + first_tile, ctx->batch_scenes, nullptr,
+                 n_tiles, max_tpt, s);
+}
+
+const uint32_t* gudni_batch_output(const gudni_ctx* ctx) { return ctx ? ctx->b_out.ptr : nullptr; }
+
+int gudni_batch_download(gudni_ctx* ctx, uint32_t* out) {
+  if (!ctx || !out) return GUDNI_ERR_BAD_INPUT;
+  if (!ctx->batch_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "no batch");
+  cudaSetDevice(ctx->device);
+  if (ctx->last_stream && ctx->last_stream != ctx->stream) {
+    cudaError_t e = cudaStreamSynchronize(ctx->last_stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream sync");
+  }
+  cudaError_t e = cudaMemcpyAsync(out, ctx->b_out.ptr, ctx->batch_pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batch read-back");
+  return read_status(ctx, ctx->stream);
+}
+
+int gudni_sync_status(gudni_ctx* ctx) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  if (ctx->last_stream && ctx->last_stream != ctx->stream) {
+    cudaError_t e = cudaStreamSynchronize(ctx->last_stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "stream sync");
+  }
+  return read_status(ctx, ctx->stream);
+}
+
+size_t gudni_scratch_bytes(const gudni_ctx* ctx) {
+  if (!ctx) return 0;
+  return ctx->thr.cap * sizeof(float4) + ctx->hdr.cap * 4 + ctx->idx.cap * 4 + ctx->big_thr.cap * sizeof(float4) +
+         ctx->big_hdr.cap * 4 + ctx->big_idx.cap * 4;
 }
 
 int gudni_enable_counters(gudni_ctx* ctx, int enable) {
   if (!ctx) return GUDNI_ERR_BAD_INPUT;
   cudaSetDevice(ctx->device);
-  cudaError_t e = ctx->counters.reserve(4);
-  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->counters.ptr, 0, 4 * sizeof(int64_t), ctx->stream);  // reset
+  int rc = ensure_scratch(ctx);
+  if (rc) return rc;
+  cudaError_t e = cudaMemsetAsync(ctx->counters.ptr, 0, 4 * sizeof(int64_t), ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
   ctx->counters_on = enable != 0;
@@ -538,8 +735,9 @@ int gudni_enable_counters(gudni_ctx* ctx, int enable) {
 int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]) {
   if (!ctx || !out) return GUDNI_ERR_BAD_INPUT;
   cudaSetDevice(ctx->device);
-  cudaError_t e = ctx->counters.reserve(4);
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int rc = ensure_scratch(ctx);
+  if (rc) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(out, ctx->counters.ptr, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemset(ctx->counters.ptr, 0, 4 * sizeof(int64_t));
   if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");

@@ -1,25 +1,27 @@
 // Raster kernels (sm_103a).
 //
-// raster_columns_kernel fuses the reference's three launches (generateThresholds,
-// sortThresholds, renderThresholds; OpenCL/CallKernels.hs:124-174) into one: each
-// thread runs whole columns start to finish, so the threshold queue never makes the
-// generate -> sort -> render round trips through global memory that the reference's
-// three kernels make.
+// The reference makes three launches per job (generateThresholds, sortThresholds,
+// renderThresholds; OpenCL/CallKernels.hs:124-174) and round-trips every column's
+// threshold queue and shape state through global memory between them.  Here one
+// thread runs a whole column start to finish (raster_device.cuh), and two kernels
+// schedule the columns:
 //
-// Launch shape: a persistent grid (SMs x resident blocks) strides over the job's
-// work items (tile x column, the reference's NDRange), consecutive threads taking
-// consecutive columns of one tile so a warp walks the same strands together.  Each
-// resident thread owns a scratch slot: a threshold queue of `capacity` entries and
-// the shape-index table of its column.
+// raster_tiles_kernel -- the fast pass.  A persistent grid of warps pulls tiles from
+//   a work counter (one atomicAdd per tile, lane 0), optionally in a cost-descending
+//   order, and runs the tile's columns on its lanes (32 consecutive columns at a time:
+//   the lanes walk the same strands and write one row segment per pixel row).  Tiles
+//   may belong to different scenes of a batch, each with its own canvas, output,
+//   background and threads per tile.  Every thread owns a scratch slot (a queue of
+//   `capacity` entries and the shape-index table of its column).
 //
-// Capacity: the fast pass uses a small working capacity.  A column that needs more
-// is recorded in an overflow list and re-run by a second launch of the same kernel
-// with the spec's full max_thresholds; the second launch reads the list's length on
-// the device, so the pair is enqueued without a host round trip (and can be captured
-// in a CUDA graph).  The result does not depend on the capacity, only on whether it
-// suffices.  A column that exceeds max_thresholds raises
-// kStatusOverflow (the reference silently writes past its slab there,
-// Kernels.cl:375-380, 1096-1103).
+// raster_list_kernel -- the full-capacity pass.  Columns that overflowed the fast
+//   pass's small working capacity were appended to a list; this kernel, launched
+//   right after on the same stream, reads the list's length on the device and re-runs
+//   them with the spec's max_thresholds.  The result does not depend on the capacity,
+//   only on whether it suffices, and no host round trip separates the two launches
+//   (the pair can be captured in a CUDA graph).  A column that exceeds max_thresholds
+//   raises kStatusOverflow (the reference silently writes past its slab there,
+//   Kernels.cl:375-380, 1096-1103).
 
 #include <cuda_runtime.h>
 
@@ -34,57 +36,113 @@ __device__ __forceinline__ bool tileOk(const gudni_tile_info& ti, uint32_t n_sha
          (uint64_t)ti.shapes.start + (uint64_t)ti.shapes.length <= (uint64_t)n_shapes;
 }
 
+// The inputs of tile `tile`: the shared piles plus its scene's canvas, output,
+// background, threads per tile and job index.
+__device__ __forceinline__ RasterInputs sceneInputs(const RasterInputs& base, const SceneInfo* scenes,
+                                                    const int32_t* tile_scene, uint32_t n_scenes, int tile,
+                                                    int& status, bool& ok) {
+  RasterInputs in = base;
+  ok = true;
+  if (scenes) {
+    const uint32_t s = (uint32_t)tile_scene[tile];
+    if (s >= n_scenes) {
+      status |= kStatusBadInput;
+      ok = false;
+      return in;
+    }
+    const SceneInfo sc = scenes[s];
+    in.bitmap_w = sc.bitmap_w;
+    in.bitmap_h = sc.bitmap_h;
+    in.log2_tpt = sc.log2_tpt;
+    in.job_index = sc.job_index;
+    in.out = base.out + sc.out_offset;
+    in.background = make_float4(sc.background[0], sc.background[1], sc.background[2], sc.background[3]);
+  } else if (base.tile_jobs) {
+    in.job_index = base.tile_jobs[tile];
+  }
+  return in;
+}
+
+// One column, start to finish.  Returns true when the queue overflowed `cap`.
 template <int SECTIONS>
-__global__ void __launch_bounds__(kRasterBlock) raster_columns_kernel(ColumnLaunch a) {
+__device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_tile_info& ti, int column,
+                                          float4* thr, uint32_t* hdr, int cap, uint32_t* idx, int& status) {
+  const ColumnState c = initColumn(in, ti, column, in.job_index);
+  if (!c.active) return false;
+  Queue q{thr, hdr, cap, cap, false};
+  ShapeStack<SECTIONS> stack;
+  stack.clear();
+  const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, idx, status);
+  if (q.overflow) return true;
+  if (in.counters) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[2]), (unsigned long long)q.length());
+    atomicMax(reinterpret_cast<unsigned long long*>(&in.counters[3]), (unsigned long long)bits);
+  }
+  renderColumn<SECTIONS>(in, c, q, stack, idx, status, (int)bits);
+  return q.overflow;
+}
+
+template <int SECTIONS>
+__global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nslots = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
   float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
   uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
   uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
-  const uint32_t tmask = (1u << a.in.log2_tpt) - 1u;
   int status = 0;
-  uint32_t n_items = a.n_items;
-  if (a.n_items_dev) n_items = min(n_items, *a.n_items_dev);
-  for (uint32_t w = slot; w < n_items; w += nslots) {
-    const uint32_t item = a.items ? a.items[w] : w;
-    const int tile = (int)(item >> a.in.log2_tpt);
-    const int column = (int)(item & tmask);
-    const gudni_tile_info ti = a.in.tiles[tile];
-    if (!tileOk(ti, a.in.n_shapes)) {
+  for (;;) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(a.next_tile, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= a.n_tiles) break;
+    const int tile = (int)(a.order ? a.order[k] : k);
+    bool ok;
+    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
+    if (!ok) continue;
+    const gudni_tile_info ti = in.tiles[tile];
+    if (!tileOk(ti, in.n_shapes) || in.log2_tpt < 0 || in.log2_tpt > kMaxLog2Tpt) {
       status |= kStatusBadInput;
       continue;
     }
-    const ColumnState c = initColumn(a.in, ti, column, a.in.tile_jobs ? a.in.tile_jobs[tile] : a.in.job_index);
-    if (!c.active) continue;
-    Queue q{thr, hdr, a.scratch.capacity, a.scratch.capacity, false};
-    ShapeStack<SECTIONS> stack;
-    stack.clear();
-    const uint32_t bits = buildThresholds<SECTIONS>(a.in, c, q, stack, idx, status);
-    if (a.in.counters && !q.overflow) {
-      atomicAdd(reinterpret_cast<unsigned long long*>(&a.in.counters[2]), (unsigned long long)q.length());
-      atomicMax(reinterpret_cast<unsigned long long*>(&a.in.counters[3]), (unsigned long long)bits);
-    }
-    if (!q.overflow) renderColumn<SECTIONS>(a.in, c, q, stack, idx, status);
-    if (q.overflow) {
-      if (a.overflow_items) {
-        const uint32_t k = atomicAdd(a.overflow_count, 1u);
-        if (k < a.overflow_cap) {
-          a.overflow_items[k] = item;
+    const int tpt = 1 << in.log2_tpt;
+    for (int column = lane; column < tpt; column += 32) {
+      if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) {
+        if (a.overflow_items) {
+          const uint32_t n = atomicAdd(a.overflow_count, 1u);
+          if (n < a.overflow_cap) {
+            a.overflow_items[n] = ((uint32_t)tile << kColumnBits) | (uint32_t)column;
+          } else {
+            status |= kStatusOverflow;
+          }
         } else {
           status |= kStatusOverflow;
         }
-      } else {
-        status |= kStatusOverflow;
       }
     }
   }
   if (status) atomicOr(a.status, status);
 }
 
-template <int S>
-static cudaError_t launch_s(const ColumnLaunch& a, int grid, cudaStream_t stream) {
-  raster_columns_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
-  return cudaGetLastError();
+template <int SECTIONS>
+__global__ void __launch_bounds__(kRasterBlock) raster_list_kernel(TileLaunch a) {
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nslots = gridDim.x * blockDim.x;
+  float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
+  uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
+  uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
+  int status = 0;
+  const uint32_t n_items = min(*a.list_count, a.list_cap);
+  for (uint32_t w = slot; w < n_items; w += nslots) {
+    const uint32_t item = a.list[w];
+    const int tile = (int)(item >> kColumnBits);
+    const int column = (int)(item & ((1u << kColumnBits) - 1u));
+    bool ok;
+    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
+    if (!ok) continue;
+    const gudni_tile_info ti = in.tiles[tile];
+    if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) status |= kStatusOverflow;
+  }
+  if (status) atomicOr(a.status, status);
 }
 
 int sections_for(int max_shape) {
@@ -94,27 +152,37 @@ int sections_for(int max_shape) {
   return s;
 }
 
-cudaError_t launch_columns(const ColumnLaunch& a, int sections, int grid, cudaStream_t stream) {
+template <int S>
+static cudaError_t launch_s(const TileLaunch& a, bool list, int grid, cudaStream_t stream) {
+  if (list) {
+    raster_list_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+  } else {
+    raster_tiles_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream) {
   switch (sections) {
-    case 1: return launch_s<1>(a, grid, stream);
-    case 2: return launch_s<2>(a, grid, stream);
-    case 4: return launch_s<4>(a, grid, stream);
-    case 8: return launch_s<8>(a, grid, stream);
-    case 16: return launch_s<16>(a, grid, stream);
-    case 32: return launch_s<32>(a, grid, stream);
+    case 1: return launch_s<1>(a, list, grid, stream);
+    case 2: return launch_s<2>(a, list, grid, stream);
+    case 4: return launch_s<4>(a, list, grid, stream);
+    case 8: return launch_s<8>(a, list, grid, stream);
+    case 16: return launch_s<16>(a, list, grid, stream);
+    case 32: return launch_s<32>(a, list, grid, stream);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t columns_occupancy(int sections, int* blocks_per_sm) {
+cudaError_t raster_occupancy(int sections, int* blocks_per_sm) {
   const void* fn = nullptr;
   switch (sections) {
-    case 1: fn = (const void*)raster_columns_kernel<1>; break;
-    case 2: fn = (const void*)raster_columns_kernel<2>; break;
-    case 4: fn = (const void*)raster_columns_kernel<4>; break;
-    case 8: fn = (const void*)raster_columns_kernel<8>; break;
-    case 16: fn = (const void*)raster_columns_kernel<16>; break;
-    case 32: fn = (const void*)raster_columns_kernel<32>; break;
+    case 1: fn = (const void*)raster_tiles_kernel<1>; break;
+    case 2: fn = (const void*)raster_tiles_kernel<2>; break;
+    case 4: fn = (const void*)raster_tiles_kernel<4>; break;
+    case 8: fn = (const void*)raster_tiles_kernel<8>; break;
+    case 16: fn = (const void*)raster_tiles_kernel<16>; break;
+    case 32: fn = (const void*)raster_tiles_kernel<32>; break;
     default: return cudaErrorInvalidValue;
   }
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kRasterBlock, 0);

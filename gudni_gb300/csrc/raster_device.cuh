@@ -444,8 +444,10 @@ __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int 
 template <int SECTIONS>
 __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
                                                  const uint32_t* shapeIdx, int px, int py, int& status,
-                                                 int64_t& texels) {
-  int topBit = in.max_shape;
+                                                 int64_t& texels, int topStart) {
+  // The reference starts at MAXSHAPE (K:1453); no bit at or above the column's
+  // assigned shape-bit count is ever set, so starting there finds the same bits.
+  int topBit = topStart;
   float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float4 next = base;
   bool done = false;
@@ -594,7 +596,8 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 // K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
 template <int SECTIONS>
 __device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
-                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status) {
+                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
+                                             int shapeBits) {
   Parse p;
   p.current = 0;
   p.numActive = 0;
@@ -633,7 +636,7 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       }
       p.sStartX = p.sEndX;
       p.sEndX = nextX;
-      const float4 color = determineColor(in, stack, shapeIdx, px, py, status, texels);
+      const float4 color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits);
       float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
       if (in.stochastic != 0.0f) {  // getRandom K:1608-1613
         cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);

@@ -184,6 +184,54 @@ int gudni_raster_tiles_device(gudni_ctx* ctx,
                               int32_t frame_number, const float background[4],
                               uint32_t* out, void* stream);
 
+/* ------------------------------------------------------------------ batches */
+
+/* One scene of a batch (40 bytes). */
+typedef struct gudni_batch_scene {
+    int32_t bitmap_w, bitmap_h;
+    int32_t compute_depth;          /* log2 threads per tile of this scene's spec */
+    int32_t job_index;
+    uint64_t out_offset;            /* first pixel of the scene in the batch output */
+    float background[4];
+} gudni_batch_scene;
+
+/* Upload a batch of scenes rendered together by gudni_batch_render (no counterpart in
+ * the reference, which renders one scene per frame): the scenes' common piles
+ * concatenated (geometry, substances, pictures, picture uses, radial gradients, with
+ * every shape's geo_start, every tag's substance id and every substance's picture /
+ * gradient id rebased into the concatenation), their shape piles concatenated, their
+ * tile piles concatenated with each tile's shape slice rebased, the scene of every
+ * tile, and the scene table.  Tiles are scheduled in descending `tile_cost` (NULL:
+ * input order).  All scenes share the context's max_shape; threads per tile may
+ * differ per scene.  Host pointers.  Replaces the context's common buffers. */
+int gudni_batch_upload(gudni_ctx* ctx,
+                       const void* geometry, size_t geometry_bytes,
+                       const float* substances, size_t n_substances,
+                       const uint8_t* pictures, size_t picture_bytes,
+                       const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                       const gudni_radial* radials, size_t n_radials,
+                       const gudni_shape* shapes, size_t n_shapes,
+                       const gudni_tile_info* tiles, const int32_t* tile_scene,
+                       const float* tile_cost, size_t n_tiles,
+                       const gudni_batch_scene* scenes, size_t n_scenes,
+                       size_t out_pixels);
+
+/* Render the uploaded batch into the context's batch output, in one persistent
+ * launch (plus the full-capacity pass for overflowing columns) enqueued on `stream`.
+ * With use_graph != 0 the launch sequence is captured into a CUDA graph on first use
+ * and replayed afterwards. */
+int gudni_batch_render(gudni_ctx* ctx, int use_graph, void* stream);
+
+/* Render only tiles [first_tile, first_tile + n_tiles) of the uploaded batch, in
+ * input order, as an ordinary launch pair: the plain one-launch-per-scene path over
+ * the same resident piles, for comparison with gudni_batch_render. */
+int gudni_batch_render_tiles(gudni_ctx* ctx, size_t first_tile, size_t n_tiles, void* stream);
+
+/* Device address of the batch output (out_pixels BGRA words), and a blocking copy
+ * of it to host memory. */
+const uint32_t* gudni_batch_output(const gudni_ctx* ctx);
+int gudni_batch_download(gudni_ctx* ctx, uint32_t* out);
+
 /* Work counters of the next launches, for measurement: when enabled, kernels add
  * [0] sections scanned, [1] picture texels read, [2] thresholds generated,
  * [3] largest shape-bit count of a column.  gudni_read_counters returns and clears
