@@ -80,6 +80,12 @@ struct gudni_ctx {
   size_t n_radials = 0;
   DevBuf<float> random_field;
   bool has_random = false;
+  DevBuf<uint4> strand_table;
+  DevBuf<uint32_t> strand_first;
+  size_t n_strands = 0;
+  size_t n_units = 0;
+  std::vector<uint4> h_strand_table;
+  std::vector<uint32_t> h_strand_first;
 
   // per-job / per-frame staging
   DevBuf<gudni_shape> shapes;
@@ -259,6 +265,10 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   in.out = d_out;
   in.tile_jobs = nullptr;
   in.counters = ctx->counters_on ? ctx->counters.ptr : nullptr;
+  in.strand_table = ctx->n_strands ? ctx->strand_table.ptr : nullptr;
+  in.n_strands = (uint32_t)ctx->n_strands;
+  in.strand_first = ctx->strand_first.ptr;
+  in.n_units = (uint32_t)ctx->n_units;
   return in;
 }
 
@@ -336,6 +346,8 @@ int upload(gudni_ctx* ctx, DevBuf<T>& buf, const void* src, size_t count, const 
   return GUDNI_OK;
 }
 
+int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes);
+
 int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
                           size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
                           const gudni_picture_use* picture_uses, size_t n_picture_uses,
@@ -360,11 +372,44 @@ int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_
   ctx->has_random = random_field != nullptr;
   if (random_field && (rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload")))
     return rc;
+  if ((rc = build_strand_table(ctx, static_cast<const uint8_t*>(geometry), geometry_bytes))) return rc;
   ctx->geometry_bytes = geometry_bytes;
   ctx->n_substances = n_substances;
   ctx->picture_bytes = picture_bytes;
   ctx->n_uses = n_picture_uses;
   ctx->n_radials = n_radials;
+  return GUDNI_OK;
+}
+
+// Walk the geometry pile strand by strand from its first byte (the pile is the
+// strands of every shape back to back: Raster/Serialize.hs:76-84, Enclosure.hs:76-80)
+// and record each strand's offset, size and the left/right x its range test reads.
+// The walk stops at the first malformed header; shapes starting past that point keep
+// the kernel's checked per-strand path.
+int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes) {
+  ctx->n_strands = 0;
+  ctx->n_units = bytes / 16;
+  ctx->h_strand_table.clear();
+  ctx->h_strand_first.assign(ctx->n_units, gudni::kNoStrand);
+  size_t off = 0;
+  while (off + 32 <= bytes) {
+    uint16_t size;
+    std::memcpy(&size, geo + off, 2);
+    if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > bytes) break;
+    if (ctx->h_strand_table.size() >= 0xFFFFFFF0ull || off / 8 > 0xFFFFFFFFull) break;
+    uint32_t lx, rx;
+    std::memcpy(&rx, geo + off + 8, 4);
+    std::memcpy(&lx, geo + off + 16, 4);
+    if (off % 16 == 0) ctx->h_strand_first[off / 16] = (uint32_t)ctx->h_strand_table.size();
+    ctx->h_strand_table.push_back(make_uint4((uint32_t)(off / 8), size, lx, rx));
+    off += (size_t)size * 8;
+  }
+  int rc;
+  if ((rc = upload(ctx, ctx->strand_table, ctx->h_strand_table.data(), ctx->h_strand_table.size(), "strand table")))
+    return rc;
+  if ((rc = upload(ctx, ctx->strand_first, ctx->h_strand_first.data(), ctx->h_strand_first.size(), "strand map")))
+    return rc;
+  ctx->n_strands = ctx->h_strand_table.size();
   return GUDNI_OK;
 }
 
@@ -425,6 +470,7 @@ void gudni_destroy(gudni_ctx* ctx) {
   drop_graph(ctx);
   ctx->geometry.release(); ctx->substances.release(); ctx->pictures.release(); ctx->uses.release();
   ctx->radials.release(); ctx->random_field.release(); ctx->shapes.release(); ctx->tiles.release();
+  ctx->strand_table.release(); ctx->strand_first.release();
   ctx->tile_jobs.release(); ctx->out.release();
   ctx->b_shapes.release(); ctx->b_tiles.release(); ctx->b_tile_scene.release(); ctx->b_order.release();
   ctx->b_scenes.release(); ctx->b_out.release();

@@ -74,7 +74,19 @@ struct RasterInputs {
   uint32_t* out;                 // bitmap_w * bitmap_h BGRA words
   const int32_t* tile_jobs;      // optional per-tile job index (frame launches)
   int64_t* counters;             // optional work counters (see gudni_enable_counters)
+  // Strand table of the geometry pile (optional; see StrandEntry).
+  const uint4* strand_table;     // one entry per strand
+  uint32_t n_strands;
+  const uint32_t* strand_first;  // per 16-byte unit of the pile: strand index starting there
+  uint32_t n_units;              // geometry_bytes / 16
 };
+
+// A strand table entry (16 bytes, one load): x = byte offset / 8 of the strand in the
+// geometry pile, y = its size in 8-byte units, z = bits of the strand's left x,
+// w = bits of its right x -- the two floats the column range test reads
+// (checkInRange, Kernels.cl:1360-1363).  strand_first maps a shape's geo_start to
+// the index of its first strand (kNoStrand where no strand starts).
+constexpr uint32_t kNoStrand = 0xFFFFFFFFu;
 
 __device__ __forceinline__ float cl_min(float x, float y) { return y < x ? y : x; }
 __device__ __forceinline__ float cl_max(float x, float y) { return x < y ? y : x; }
@@ -322,6 +334,30 @@ __device__ __forceinline__ void searchTree(Trav& t, const float4* tree, int tree
   }
 }
 
+// traverseTree K:1378-1408 + spawnThresholds for one strand of `size` 8-byte units.
+__device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* strand, uint32_t size, float2 d,
+                                                 uint32_t shapeBit, bool& added, bool& enclosedByStrand,
+                                                 int& status) {
+  const int treeSize = ((int)size - 4) / 2;
+  const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
+  const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
+  Trav l;
+  l.right = make_float2(rp.x - d.x, rp.y - d.y);
+  l.left = make_float2(lc.x - d.x, lc.y - d.y);
+  l.control = make_float2(lc.z - d.x, lc.w - d.y);
+  l.xPos = 0.0f;
+  l.index = 0;
+  if (l.left.x <= kRight && l.right.x > kLeft) {  // checkInRange K:1360-1363
+    Trav r = l;
+    l.xPos = cl_max(kLeft, l.left.x);
+    r.xPos = cl_min(kRight, l.right.x);
+    const float4* tree = reinterpret_cast<const float4*>(strand + 32);
+    searchTree(l, tree, treeSize, d, true);
+    searchTree(r, tree, treeSize, d, false);
+    spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status);
+  }
+}
+
 // buildThresholdArray K:1540-1595 with traverseTree K:1378-1408.
 // Returns the number of shape bits assigned; shape indices go to `shapeIdx`.
 template <int SECTIONS>
@@ -336,42 +372,43 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
     const gudni_shape shape = in.shapes[shapeIndex];
     bool added = false;
     bool enclosedByShape = false;
-    size_t off = (size_t)shape.geo_start * 16;
-    for (uint32_t k = 0; k < shape.num_strands; ++k) {
-      if (off + 32 > in.geometry_bytes) {
-        status |= kStatusBadInput;
-        break;
-      }
-      const uint8_t* strand = in.geometry + off;
-      const uint32_t size = (uint32_t)(*reinterpret_cast<const uint16_t*>(strand));
-      // a serialized strand is 2k+2 eight-byte units (k >= 1 curves); an odd size
-      // would misalign the float4 reads of every strand after it
-      if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > in.geometry_bytes) {
-        status |= kStatusBadInput;
-        break;
-      }
-      bool enclosedByStrand = false;
-      const int treeSize = ((int)size - 4) / 2;
-      const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
-      const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
-      Trav l;
-      l.right = make_float2(rp.x - d.x, rp.y - d.y);
-      l.left = make_float2(lc.x - d.x, lc.y - d.y);
-      l.control = make_float2(lc.z - d.x, lc.w - d.y);
-      l.xPos = 0.0f;
-      l.index = 0;
-      if (l.left.x <= kRight && l.right.x > kLeft) {  // checkInRange K:1360-1363
-        Trav r = l;
-        l.xPos = cl_max(kLeft, l.left.x);
-        r.xPos = cl_min(kRight, l.right.x);
-        const float4* tree = reinterpret_cast<const float4*>(strand + 32);
-        searchTree(l, tree, treeSize, d, true);
-        searchTree(r, tree, treeSize, d, false);
-        spawnThresholds(g, shapeBits, l, r, added, enclosedByStrand, status);
+    uint32_t first = kNoStrand;
+    if (in.strand_table && shape.geo_start < in.n_units) first = in.strand_first[shape.geo_start];
+    if (first != kNoStrand && (uint64_t)first + shape.num_strands <= in.n_strands) {
+      // Strand table: the range test reads one independent entry per strand; only
+      // strands that cross the column touch the strand heap.  A strand that does not
+      // cross it spawns nothing and leaves the enclosure unchanged.
+      for (uint32_t k = 0; k < shape.num_strands; ++k) {
+        const uint4 e = in.strand_table[first + k];
+        const float lx = __uint_as_float(e.z) - d.x;
+        const float rx = __uint_as_float(e.w) - d.x;
+        if (!(lx <= kRight && rx > kLeft)) continue;
+        bool enclosedByStrand = false;
+        strandThresholds(g, in.geometry + (size_t)e.x * 8, e.y, d, shapeBits, added, enclosedByStrand, status);
         if (q.overflow) return shapeBits;
+        enclosedByShape = enclosedByShape != enclosedByStrand;
       }
-      off += (size_t)size * 8;
-      enclosedByShape = enclosedByShape != enclosedByStrand;
+    } else {
+      size_t off = (size_t)shape.geo_start * 16;
+      for (uint32_t k = 0; k < shape.num_strands; ++k) {
+        if (off + 32 > in.geometry_bytes) {
+          status |= kStatusBadInput;
+          break;
+        }
+        const uint8_t* strand = in.geometry + off;
+        const uint32_t size = (uint32_t)(*reinterpret_cast<const uint16_t*>(strand));
+        // a serialized strand is 2k+2 eight-byte units (k >= 1 curves); an odd size
+        // would misalign the float4 reads of every strand after it
+        if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > in.geometry_bytes) {
+          status |= kStatusBadInput;
+          break;
+        }
+        bool enclosedByStrand = false;
+        strandThresholds(g, strand, size, d, shapeBits, added, enclosedByStrand, status);
+        if (q.overflow) return shapeBits;
+        off += (size_t)size * 8;
+        enclosedByShape = enclosedByShape != enclosedByStrand;
+      }
     }
     if (enclosedByShape) stack.flip(shapeBits);
     if (added || enclosedByShape) {
