@@ -55,6 +55,14 @@ struct DevBuf {
 
 }  // namespace
 
+namespace gudni {
+// Error text reported by gudni_last_error(NULL) for calls made without a context.
+void set_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> lock(g_create_mutex);
+  g_create_error = msg;
+}
+}  // namespace gudni
+
 struct gudni_ctx {
   gudni_spec spec;
   int device = 0;

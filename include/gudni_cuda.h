@@ -239,6 +239,48 @@ int gudni_batch_download(gudni_ctx* ctx, uint32_t* out);
 int gudni_enable_counters(gudni_ctx* ctx, int enable);
 int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
 
+/* ------------------------------------------------- no-allocation entry point */
+
+/* Size of the device scratch that gudni_raster_job_noalloc uses: a fixed array
+ * compiled into the library, held by every GPU that loads it until the process
+ * exits. */
+#define GUDNI_NOALLOC_SCRATCH_BYTES (64u << 20)
+/* Threshold queue capacity per column in gudni_raster_job_noalloc. */
+#define GUDNI_NOALLOC_CAPACITY 512
+
+/* Rasterize one job without allocating any device memory.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc -- code running inside
+ * another framework's memory pool or a frame-pacing loop that forbids allocation,
+ * a sandboxed plugin without allocation rights, or a real-time path where an
+ * allocation's implicit synchronisation is not allowed.  Every buffer is supplied
+ * by the caller as a DEVICE pointer: the common piles (geometry, substances,
+ * pictures, picture uses, radial gradients), the job's shape and tile piles, and
+ * `out` (bitmap_w*bitmap_h BGRA words; only the job's tiles are written).  The
+ * per-column threshold queues live in the library's fixed device scratch of
+ * GUDNI_NOALLOC_SCRATCH_BYTES, with a queue capacity of GUDNI_NOALLOC_CAPACITY
+ * thresholds per column (min with spec->max_thresholds); a column that needs more
+ * returns GUDNI_ERR_THRESHOLD_OVERFLOW, and a max_shape too large for the scratch
+ * returns GUDNI_ERR_BAD_INPUT.  No context is needed; the spec supplies max_shape
+ * and threads per tile.
+ *
+ * The first call on a device looks up the scratch's device address (with that device
+ * current); make that first call before any stream capture.  Every call shares the
+ * one scratch array, so calls whose launches overlap on the GPU race: issue them on
+ * one stream, or serialise them.  The call enqueues on `stream` (NULL = the legacy
+ * default stream) and waits for it to read the device status.  Error messages are
+ * read with gudni_last_error(NULL). */
+int gudni_raster_job_noalloc(const gudni_spec* spec,
+                             const void* geometry, size_t geometry_bytes,
+                             const float* substances, size_t n_substances,
+                             const uint8_t* pictures, size_t picture_bytes,
+                             const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                             const gudni_radial* radials, size_t n_radials,
+                             const gudni_shape* shapes, size_t n_shapes,
+                             const gudni_tile_info* tiles, size_t n_tiles,
+                             int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth,
+                             int32_t job_index, const float background[4],
+                             uint32_t* out, void* stream);
+
 /* Number of kernel launches this context has issued. */
 uint64_t gudni_launch_count(const gudni_ctx* ctx);
 
