@@ -33,13 +33,15 @@ inline P2 between(float t, P2 v0, P2 v1) {  // Deknob.hs:40-41
 }
 
 // findSplit (Deknob.hs:61-79): bisect the parameter while one half keeps bulging in
-// the knob's direction.  Returns (mid0, onCurve, mid1).
-Bez find_split(bool left, const Bez& z) {
+// the knob's direction.  Returns (mid0, onCurve, mid1); *t_out receives the split
+// parameter.
+Bez find_split(bool left, const Bez& z, float* t_out) {
   float bottom = 0.0f, top = 1.0f, t = kSplit;
   for (;;) {
     P2 mid0 = between(t, z.a, z.c);
     P2 mid1 = between(t, z.c, z.b);
     P2 on = between(t, mid0, mid1);
+    *t_out = t;
     if (top - bottom <= kIota) return Bez{mid0, on, mid1};
     bool mid1_stays = left ? (mid1.x < on.x) : (mid1.x > on.x);
     if (mid1_stays) {
@@ -59,16 +61,39 @@ Bez find_split(bool left, const Bez& z) {
   }
 }
 
+// Provenance of a serialized point: a fixed linear combination of at most three
+// points of the flattened scene (index = 2 * pair + 0 for the on-curve point, + 1 for
+// the off-curve point).  Used to carry gradients from the geometry pile back to the
+// scene's control points.
+struct Prov {
+  int32_t src[3];
+  float w[3];
+};
+inline Prov prov1(int32_t a) { return Prov{{a, -1, -1}, {1.0f, 0.0f, 0.0f}}; }
+struct BezProv { Prov a, c, b; };
+
 // fixKnob (Deknob.hs:85-100)
-void fix_knob(const Bez& z, std::vector<Bez>& out) {
+void fix_knob(const Bez& z, std::vector<Bez>& out, const BezProv* zp, std::vector<BezProv>* outp) {
   bool left = z.c.x < z.a.x && z.c.x < z.b.x;
   bool right = !left && (z.c.x > z.a.x && z.c.x > z.b.x);
   if (left || right) {
-    Bez s = find_split(left, z);
+    float t = kSplit;
+    Bez s = find_split(left, z, &t);
     out.push_back(Bez{z.a, s.a, s.c});
     out.push_back(Bez{s.c, s.b, z.b});
+    if (outp) {
+      // mid0 = (1-t) a + t c, mid1 = (1-t) c + t b, on = (1-t)^2 a + 2t(1-t) c + t^2 b
+      const int32_t ia = zp->a.src[0], ic = zp->c.src[0], ib = zp->b.src[0];
+      const float u = 1.0f - t;
+      Prov mid0{{ia, ic, -1}, {u, t, 0.0f}};
+      Prov mid1{{ic, ib, -1}, {u, t, 0.0f}};
+      Prov on{{ia, ic, ib}, {u * u, 2.0f * t * u, t * t}};
+      outp->push_back(BezProv{zp->a, mid0, on});
+      outp->push_back(BezProv{on, mid1, zp->b});
+    }
   } else {
     out.push_back(z);
+    if (outp) outp->push_back(*zp);
   }
 }
 
@@ -161,18 +186,28 @@ inline bool connectable(const Bez& a, const Bez& b) {  // Strand.hs:77-81
   return ha == hb && ha != 0;
 }
 
+struct ProvSink {
+  std::vector<int32_t> src;     // 3 per serialized point
+  std::vector<float> w;         // 3 per serialized point
+  std::vector<uint32_t> where;  // float index of the point's x in the geometry pile
+};
+
 // Append the serialized strands of one outline (curve pairs) to `geo`; returns the
-// number of strands.  splitShape / outlineToStrands, Strand.hs:153-178.
-uint32_t outline_to_strands(const float* pairs, int n_pairs, std::vector<uint8_t>& geo) {
+// number of strands.  splitShape / outlineToStrands, Strand.hs:153-178.  With `prov`,
+// also records the provenance of every point written (pair indices from `pair0`).
+uint32_t outline_to_strands(const float* pairs, int n_pairs, std::vector<uint8_t>& geo, ProvSink* prov = nullptr,
+                            int32_t pair0 = 0) {
   if (n_pairs < 2) return 0;
   // pairsToBeziers (overNeighbors makeBezier), then replaceKnobs
   std::vector<Bez> beziers;
+  std::vector<BezProv> bprov;
   beziers.reserve(n_pairs + 8);
   for (int i = 0; i < n_pairs; ++i) {
     int j = (i + 1) % n_pairs;
     Bez z{P2{pairs[4 * i], pairs[4 * i + 1]}, P2{pairs[4 * i + 2], pairs[4 * i + 3]},
           P2{pairs[4 * j], pairs[4 * j + 1]}};
-    fix_knob(z, beziers);
+    BezProv zp{prov1(2 * (pair0 + i)), prov1(2 * (pair0 + i) + 1), prov1(2 * (pair0 + j))};
+    fix_knob(z, beziers, &zp, prov ? &bprov : nullptr);
   }
   // splitIntoStrands: the fold's final accumulator comes first, then the strands in
   // the order they were closed (Strand.hs:98-102).
@@ -189,24 +224,37 @@ uint32_t outline_to_strands(const float* pairs, int n_pairs, std::vector<uint8_t
   const ReorderTable& table = reorder_table();
   uint32_t count = 0;
   std::vector<P2> pts;
+  std::vector<Prov> ppts;
   std::vector<Bez> chunk;
+  std::vector<BezProv> pchunk;
   for (auto& run : runs) {
     // splitTooLarge 16 (Strand.hs:105-109)
     for (int s = run.first; s < run.second; s += kMaxStrandCurves) {
       int e = std::min(run.second, s + kMaxStrandCurves);
       chunk.assign(beziers.begin() + s, beziers.begin() + e);
+      if (prov) pchunk.assign(bprov.begin() + s, bprov.begin() + e);
       // reverseIfBackwards (Strand.hs:137-143)
       if (chunk.front().a.x > chunk.back().b.x) {
         std::reverse(chunk.begin(), chunk.end());
         for (auto& z : chunk) std::swap(z.a, z.b);
+        if (prov) {
+          std::reverse(pchunk.begin(), pchunk.end());
+          for (auto& z : pchunk) std::swap(z.a, z.b);
+        }
       }
       // beziersToPoints (Strand.hs:130-134)
       pts.clear();
-      for (auto& z : chunk) {
-        pts.push_back(z.a);
-        pts.push_back(z.c);
+      ppts.clear();
+      for (size_t k = 0; k < chunk.size(); ++k) {
+        pts.push_back(chunk[k].a);
+        pts.push_back(chunk[k].c);
+        if (prov) {
+          ppts.push_back(pchunk[k].a);
+          ppts.push_back(pchunk[k].c);
+        }
       }
       pts.push_back(chunk.back().b);
+      if (prov) ppts.push_back(pchunk.back().b);
       const int len = (int)pts.size();
       const std::vector<int>& row = table.rows[len / 2];
       // header: u16 size in 8-byte units, u16 0, u32 0 (Strand.hs:201-206)
@@ -216,6 +264,12 @@ uint32_t outline_to_strands(const float* pairs, int n_pairs, std::vector<uint8_t
       geo.insert(geo.end(), hdr, hdr + 8);
       for (int i = 0; i < len; ++i) {
         const P2& p = pts[row[i]];
+        if (prov) {
+          const Prov& q = ppts[row[i]];
+          prov->src.insert(prov->src.end(), q.src, q.src + 3);
+          prov->w.insert(prov->w.end(), q.w, q.w + 3);
+          prov->where.push_back((uint32_t)(geo.size() / 4));
+        }
         uint8_t b[8];
         std::memcpy(b, &p.x, 4);
         std::memcpy(b + 4, &p.y, 4);
@@ -418,6 +472,7 @@ class TileTree {
 // ---------------------------------------------------------------- frame
 
 struct gudni_frame {
+  ProvSink prov;
   std::vector<uint8_t> geometry;
   std::vector<float> substances;
   std::vector<gudni_picture_use> picture_uses;
@@ -538,7 +593,7 @@ gudni_frame* gudni_serialize(const gudni_scene_desc* s, const gudni_spec* spec) 
       for (int o = o0; o < o1; ++o) {
         int p0 = s->outline_pair_start[o];
         strands += outline_to_strands(s->pairs + 4 * p0, s->outline_pair_start[o + 1] - p0,
-                                      f->geometry);
+                                      f->geometry, &f->prov, p0);
       }
       ShapeEntry e;
       e.tag = make_tag(kind, s->shape_compound[sh], substance_id);
@@ -608,6 +663,11 @@ const gudni_shape* gudni_frame_job_shapes(const gudni_frame* f, size_t j) { retu
 size_t gudni_frame_job_n_tiles(const gudni_frame* f, size_t j) { return f->jobs[j].tiles.size(); }
 const gudni_tile_info* gudni_frame_job_tiles(const gudni_frame* f, size_t j) { return f->jobs[j].tiles.data(); }
 int32_t gudni_frame_job_columns(const gudni_frame* f, size_t j) { return f->jobs[j].columns; }
+size_t gudni_frame_n_points(const gudni_frame* f) { return f->prov.where.size(); }
+const int32_t* gudni_frame_point_sources(const gudni_frame* f) { return f->prov.src.data(); }
+const float* gudni_frame_point_weights(const gudni_frame* f) { return f->prov.w.data(); }
+const uint32_t* gudni_frame_point_offsets(const gudni_frame* f) { return f->prov.where.data(); }
+
 void gudni_frame_stats(const gudni_frame* f, int64_t out[8]) {
   for (int i = 0; i < 8; ++i) out[i] = f->stats[i];
 }

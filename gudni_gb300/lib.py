@@ -118,6 +118,12 @@ def load_host():
         lib.gudni_frame_job_columns.restype = C.c_int32
         lib.gudni_frame_job_columns.argtypes = [C.c_void_p, C.c_size_t]
         lib.gudni_frame_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+        lib.gudni_frame_n_points.restype = C.c_size_t
+        lib.gudni_frame_n_points.argtypes = [C.c_void_p]
+        for name in ("point_offsets", "point_sources", "point_weights"):
+            fn = getattr(lib, "gudni_frame_" + name)
+            fn.restype = C.c_void_p
+            fn.argtypes = [C.c_void_p]
         _host = lib
     return _host
 

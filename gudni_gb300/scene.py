@@ -416,6 +416,11 @@ class Frame:
     random_field: np.ndarray   # float32 (4096,)
     jobs: List[Job]
     stats: dict
+    # provenance of the geometry pile's points (see gudni_frame_point_*)
+    point_offsets: Optional[np.ndarray] = None   # uint32 (n,)
+    point_sources: Optional[np.ndarray] = None   # int32 (n, 3)
+    point_weights: Optional[np.ndarray] = None   # float32 (n, 3)
+    n_pairs: int = 0
 
     @property
     def compute_depth(self) -> int:
@@ -477,6 +482,10 @@ def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndar
             shapes = L._copy(lib.gudni_frame_job_shapes(h, j), lib.gudni_frame_job_n_shapes(h, j), L.SHAPE_DTYPE)
             tiles = L._copy(lib.gudni_frame_job_tiles(h, j), lib.gudni_frame_job_n_tiles(h, j), L.TILE_DTYPE)
             jobs.append(Job(shapes, tiles, int(lib.gudni_frame_job_columns(h, j))))
+        npts = lib.gudni_frame_n_points(h)
+        p_off = L._copy(lib.gudni_frame_point_offsets(h), npts, np.uint32)
+        p_src = L._copy(lib.gudni_frame_point_sources(h), 3 * npts, np.int32).reshape(-1, 3)
+        p_w = L._copy(lib.gudni_frame_point_weights(h), 3 * npts, np.float32).reshape(-1, 3)
         st = (C.c_int64 * 8)()
         lib.gudni_frame_stats(h, st)
         stats = dict(zip(["shapes", "excluded", "strands", "tiles", "splits", "max_tile_shapes",
@@ -487,7 +496,8 @@ def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndar
         random_field = default_random_field()
     return Frame(flat.canvas_w, flat.canvas_h, spec, flat.background.copy(), geo,
                  subs.reshape(-1, 4), flat.pictures.copy(), uses, rads,
-                 np.ascontiguousarray(random_field, dtype=np.float32), jobs, stats)
+                 np.ascontiguousarray(random_field, dtype=np.float32), jobs, stats,
+                 p_off, p_src, p_w, int(flat.pairs.shape[0]))
 
 
 def concatenated_piles(frame: Frame):
@@ -506,3 +516,20 @@ def concatenated_piles(frame: Frame):
     return (np.concatenate(shapes) if shapes else np.zeros(0, L.SHAPE_DTYPE),
             np.concatenate(tiles) if tiles else np.zeros(0, L.TILE_DTYPE),
             np.concatenate(jobs) if jobs else np.zeros(0, np.int32))
+
+
+def pair_gradient(frame: Frame, grad_geometry: np.ndarray) -> np.ndarray:
+    """Carry a gradient over the geometry pile's floats back to the scene's curve
+    pairs ((n_pairs, 4): onCurve x, y, offCurve x, y) through the serializer's point
+    provenance (knob splits are fixed linear combinations)."""
+    g = np.zeros((frame.n_pairs * 2, 2), np.float64)
+    off = frame.point_offsets.astype(np.int64)
+    gx = np.asarray(grad_geometry, np.float64)[off]
+    gy = np.asarray(grad_geometry, np.float64)[off + 1]
+    for j in range(3):
+        src = frame.point_sources[:, j]
+        w = frame.point_weights[:, j].astype(np.float64)
+        m = src >= 0
+        np.add.at(g[:, 0], src[m], w[m] * gx[m])
+        np.add.at(g[:, 1], src[m], w[m] * gy[m])
+    return g.reshape(frame.n_pairs, 4)

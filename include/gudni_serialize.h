@@ -87,6 +87,17 @@ size_t gudni_frame_job_n_tiles(const gudni_frame* f, size_t job);
 const gudni_tile_info* gudni_frame_job_tiles(const gudni_frame* f, size_t job);
 int32_t gudni_frame_job_columns(const gudni_frame* f, size_t job);
 
+/* Provenance of every point in the geometry pile, in pile order: the float index of
+ * its x in the pile, and its value as a fixed combination of at most three scene
+ * points (index 2*pair for a pair's on-curve point, 2*pair+1 for its off-curve point,
+ * -1 unused) with the given weights -- knob splits (Raster/Deknob.hs:61-108) create
+ * points that are such combinations.  Used to carry geometry gradients back to the
+ * scene's control points. */
+size_t gudni_frame_n_points(const gudni_frame* f);
+const uint32_t* gudni_frame_point_offsets(const gudni_frame* f);  /* n_points */
+const int32_t* gudni_frame_point_sources(const gudni_frame* f);   /* 3 * n_points */
+const float* gudni_frame_point_weights(const gudni_frame* f);     /* 3 * n_points */
+
 /* Counters of the serialized frame: [0] shapes kept, [1] shapes excluded,
  * [2] strands, [3] leaf tiles, [4] tile splits, [5] max shapes in a tile,
  * [6] max strands in a tile, [7] total tile-shape references. */

@@ -24,11 +24,15 @@ SRC = os.path.join(HERE, "raster_oracle.cpp")
 HDR = os.path.join(ROOT, "include", "gudni_cuda.h")
 
 
+ADJ_SRC = os.path.join(HERE, "adjoint_oracle.cpp")
+
+
 def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.isfile(LIB) or max(os.path.getmtime(SRC), os.path.getmtime(HDR)) > os.path.getmtime(LIB):
+    srcs = [SRC, ADJ_SRC]
+    if force or not os.path.isfile(LIB) or max(os.path.getmtime(p) for p in srcs + [HDR]) > os.path.getmtime(LIB):
         cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
-               "-fPIC", "-shared", SRC, "-o", LIB]
+               "-fPIC", "-shared"] + srcs + ["-o", LIB]
         subprocess.run(cmd, check=True)
     return LIB
 
@@ -51,6 +55,10 @@ def _load():
         lib.oracle_raster_job.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_float,
                                           vp, C.c_int, C.POINTER(OracleStats)]
+        sz = C.c_size_t
+        lib.oracle_adjoint_job.restype = C.c_int
+        lib.oracle_adjoint_job.argtypes = [vp, sz, vp, sz, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
         _lib = lib
     return _lib
 
@@ -126,3 +134,39 @@ def ref_render_frame(frame, max_thresholds: int, n_threads: int = 0) -> np.ndarr
         if rc != 0:
             raise RuntimeError(f"reference kernels failed: {rc}")
     return out
+
+
+def _adjoint(frame, target, max_thresholds, n_threads):
+    lib = _load()
+    spec = frame.spec
+    img = np.zeros((frame.canvas_h, frame.canvas_w, 4), np.float32)
+    g_geo = np.zeros(frame.geometry.size // 4, np.float64)
+    g_sub = np.zeros(4 * len(frame.substances), np.float64)
+    bg = np.ascontiguousarray(frame.background, dtype=np.float32)
+    tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+    maxt = max_thresholds or spec.max_thresholds
+    for job in frame.jobs:
+        rc = lib.oracle_adjoint_job(_p(frame.geometry), frame.geometry.size, _p(frame.substances), len(frame.substances),
+                                    _p(frame.pictures), _p(frame.picture_uses), _p(frame.radials), _p(job.shapes),
+                                    _p(job.tiles), len(job.tiles), spec.threads_per_tile, frame.compute_depth,
+                                    frame.canvas_w, frame.canvas_h, _p(bg), maxt, spec.max_shape, _p(img),
+                                    _p(tgt), _p(g_geo) if tgt is not None else None,
+                                    _p(g_sub) if tgt is not None else None, n_threads)
+        if rc != 0:
+            raise RuntimeError(f"oracle adjoint failed: {rc}")
+    return img, g_geo, g_sub
+
+
+def render_float(frame, n_threads: int = 0, max_thresholds: Optional[int] = None) -> np.ndarray:
+    """(H, W, 4) float image: RGB before the byte conversion and the pixel's total
+    section area."""
+    img, _, _ = _adjoint(frame, None, max_thresholds, n_threads)
+    return img
+
+
+def loss_and_gradient(frame, target: np.ndarray, n_threads: int = 0, max_thresholds: Optional[int] = None):
+    """FP64 reference of L = sum (I_rgb - T_rgb)^2 and its gradient with respect to
+    every float of the geometry pile and every substance colour."""
+    img, g_geo, g_sub = _adjoint(frame, target, max_thresholds, n_threads)
+    d = img[..., :3].astype(np.float64) - np.asarray(target, np.float64)[..., :3]
+    return float(np.sum(d * d)), g_geo, g_sub.reshape(-1, 4), img
