@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-sample-frames", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="page4k", choices=sorted(WORKLOADS))
+    ap.add_argument("--scenes", type=int, default=256)
     return ap.parse_args()
 
 
@@ -60,6 +61,8 @@ WORKLOADS = {
     # the small CPU-runnable plain workload: 512x512, 64 random shapes of 8-32 segments
     "random512": ("random_512x512_shapes64",
                   "Mpixels/s (plain single-frame raster, 512x512 64 shapes, <=1 LSB RGBA8)"),
+    # the batched form (run_batch)
+    "batch256": ("batch_mix_256_scenes", "frames/s (batched raster, 256-scene mix, <=1 LSB RGBA8)"),
 }
 
 
@@ -247,10 +250,111 @@ def run_reference(args):
     return 0
 
 
+BATCH_MAX_SHAPE = 2047        # up to 2000 canvas-wide shapes per scene touch every column
+BATCH_MAX_THRESHOLDS = 32768
+BATCH_STRANDS_PER_TILE = 1 << 24  # no strand-count tile splitting
+
+
+def run_batch(args):
+    """The batched form: 256 scenes (sides log-uniform 64-1024 px, 10-2000 random shapes
+    of 8-32 segments) in one persistent launch replayed from a CUDA graph, tile size and
+    threads per tile per canvas-size bucket from the autotuner; against one launch pair
+    per scene over the same resident piles."""
+    import torch
+    from gudni_gb300 import autotune as A
+    from gudni_gb300 import batch as B
+    from gudni_gb300 import lib as L
+
+    torch.cuda.set_device(0)
+    # columns of the large scenes hold ~1000 thresholds: give the fast pass room for them
+    os.environ.setdefault("GUDNI_WORKING_CAPACITY", "2048")
+    t0 = time.perf_counter()
+    flats = __import__("gudni_gb300.scenes", fromlist=["batch_mix"]).batch_mix(seed=2, n_scenes=args.scenes)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    choice = A.autotune(flats, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE, samples=1, reps=2,
+                        candidates=((16, 32), (32, 32), (32, 64), (32, 128)))
+    t_tune = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    frames = A.serialize_tuned(flats, choice, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
+    batch = B.build_batch(frames)
+    t_ser = time.perf_counter() - t0
+    spec = A.spec_for(32, 32, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
+    r = B.BatchRasterizer(spec)
+    r.upload(batch)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    torch.cuda.set_stream(stream)
+
+    def timed(fn, steps):
+        ts = []
+        for _ in range(steps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            flush.zero_()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return ts
+
+    h = stream.cuda_stream
+    for _ in range(args.warmup):
+        r.render(use_graph=True, stream=h)
+        r.render_each_scene(stream=h)
+    r.sync_status()
+    launches0 = r.launch_count()
+    with ClockSampler(0) as clocks:
+        bt = timed(lambda: r.render(use_graph=True, stream=h), args.steps)
+    r.sync_status()
+    pt = timed(lambda: r.render_each_scene(stream=h), args.steps)
+    r.sync_status()
+    launches = r.launch_count() - launches0
+    batched_ms = sum(bt) / len(bt)
+    plain_ms = sum(pt) / len(pt)
+    pixels = batch.out_pixels
+    n = len(frames)
+    out = r.download()
+    parity = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        imgs = batch.images(out)
+        order = np.argsort([f.canvas_w * f.canvas_h * f.stats["shapes"] for f in frames])[:16]
+        worst, exact = 0, 1.0
+        for i in order:
+            want = O.render_frame(frames[i])
+            d = np.abs(imgs[i].view(np.uint8).astype(np.int16) - want.view(np.uint8).astype(np.int16))
+            worst = max(worst, int(d.max()))
+            exact = min(exact, float(np.mean(np.all(d.reshape(-1, 4) == 0, axis=1))))
+        parity = {"scenes_checked": len(order), "max_lsb": worst, "min_exact_pixel_frac": exact}
+    line = {"metric": "frames/s (batched raster, 256-scene mix, <=1 LSB RGBA8)", "value": n / (batched_ms / 1000),
+            "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": batched_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batch_mix_{n}_scenes", "scenes": n, "pixels": int(pixels),
+                       "tiles": int(len(batch.tiles)), "shapes": int(sum(f.stats["shapes"] for f in frames)),
+                       "max_shape": BATCH_MAX_SHAPE, "max_thresholds": BATCH_MAX_THRESHOLDS,
+                       "autotune": {str(k): list(v) for k, v in choice.items()},
+                       "l2": "flushed between steps (256 MB write)", "data": "synthetic, seeded"},
+            "mpixels_per_s": pixels / (batched_ms / 1000) / 1e6,
+            "plain_per_scene": {"ms_per_batch": plain_ms, "frames_per_s": n / (plain_ms / 1000),
+                                "launches_per_batch": 2 * n},
+            "batched_over_plain": plain_ms / batched_ms,
+            "gpu_launches": int(launches), "clocks": clocks.summary(), "parity_vs_oracle": parity,
+            "host_s": {"generate": t_gen, "autotune": t_tune, "serialize": t_ser}}
+    print(json.dumps(line))
+    r.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch256":
+        return run_batch(args)
 
     import torch
 

@@ -74,6 +74,7 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
   stack.clear();
   const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, idx, status);
   if (q.overflow) return true;
+  sortQueue(q);
   if (in.counters) {
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[2]), (unsigned long long)q.length());
     atomicMax(reinterpret_cast<unsigned long long*>(&in.counters[3]), (unsigned long long)bits);

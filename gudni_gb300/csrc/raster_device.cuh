@@ -9,10 +9,10 @@
 // square root), so results are bit-identical to the reference kernels evaluated with
 // IEEE semantics.
 //
-// Ordering: instead of a bubble sort after generation, each threshold is inserted
-// into its sorted place as it is generated (the reference's own insertThreshold,
-// K:1105-1124).  Both produce the unique stable order of the comparator K:1940-1951
-// over the reversed push order, so the queue the render scan sees is identical.
+// Ordering: thresholds are pushed as the reference pushes them, then sorted with a
+// stable insertion or merge sort instead of the reference's bubble sort.  All produce
+// the unique stable order of the comparator K:1940-1951 over the reversed push order,
+// so the queue the render scan sees is identical.
 //
 // Safety: every loop is bounded; strand, shape, substance and picture reads are
 // bounds-checked against the uploaded buffers; violations set a status bit and skip
@@ -140,6 +140,16 @@ struct Queue {
   __device__ __forceinline__ void set(int i, float4 t) { thr[start + i] = t; }
   __device__ __forceinline__ void setH(int i, uint32_t h) { hdr[start + i] = h; }
   __device__ __forceinline__ void pop() { start += 1; }
+  // pushThreshold K:1096-1103: the new entry goes to the front (unsorted)
+  __device__ __forceinline__ void push(uint32_t h, float4 t) {
+    if (start == 0) {
+      overflow = true;
+      return;
+    }
+    start -= 1;
+    hdr[start] = h;
+    thr[start] = t;
+  }
   // insertThreshold K:1105-1124: the new entry goes in front of the first entry it is
   // not strictly below.
   __device__ __forceinline__ void insert(uint32_t h, float4 t) {
@@ -290,7 +300,7 @@ __device__ __forceinline__ void addLineSegment(GenState& g, float2 left, float2 
       enclosed = true;
     } else {
       added = true;
-      g.q->insert(h, t);
+      g.q->push(h, t);
     }
   }
 }
@@ -419,6 +429,75 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
   return shapeBits;
 }
 
+// sortThresholdArray K:1962-1976 replacement: the reference bubble-sorts the queue;
+// its comparator is a strict weak order, so any stable sort gives the same order.
+// Short queues: insertion sort in place.  Longer ones: bottom-up merge sort using the
+// free part of the column's slab below the queue as the second buffer (when it is
+// large enough), O(n log n) instead of O(n^2).
+__device__ __forceinline__ void sortQueue(Queue& q) {
+  const int n = q.length();
+  const int s = q.start;
+  float4* T = q.thr;
+  uint32_t* H = q.hdr;
+  if (n < 32 || s < n) {
+    for (int i = s + 1; i < q.cap; ++i) {
+      const float4 t = T[i];
+      const uint32_t h = H[i];
+      int j = i - 1;
+      while (j >= s && isBelow(H[j], T[j], h, t)) {
+        T[j + 1] = T[j];
+        H[j + 1] = H[j];
+        --j;
+      }
+      T[j + 1] = t;
+      H[j + 1] = h;
+    }
+    return;
+  }
+  // ping-pong between [s, s+n) and [s-n, s)
+  int src = s, dst = s - n;
+  for (int width = 1; width < n; width *= 2) {
+    for (int lo = 0; lo < n; lo += 2 * width) {
+      const int mid = min(lo + width, n), hi = min(lo + 2 * width, n);
+      int a = lo, b = mid, o = lo;
+      while (a < mid && b < hi) {
+        // take the right run's head only when the left head is strictly below it
+        if (isBelow(H[src + a], T[src + a], H[src + b], T[src + b])) {
+          T[dst + o] = T[src + b];
+          H[dst + o] = H[src + b];
+          ++b;
+        } else {
+          T[dst + o] = T[src + a];
+          H[dst + o] = H[src + a];
+          ++a;
+        }
+        ++o;
+      }
+      while (a < mid) {
+        T[dst + o] = T[src + a];
+        H[dst + o] = H[src + a];
+        ++a;
+        ++o;
+      }
+      while (b < hi) {
+        T[dst + o] = T[src + b];
+        H[dst + o] = H[src + b];
+        ++b;
+        ++o;
+      }
+    }
+    const int t = src;
+    src = dst;
+    dst = t;
+  }
+  if (src != s) {
+    for (int i = 0; i < n; ++i) {
+      T[s + i] = T[src + i];
+      H[s + i] = H[src + i];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ render
 __device__ __forceinline__ float4 composite(float4 fg, float4 bg) {  // K:878-887
   float alphaOut = fg.w + bg.w * (1.0f - fg.w);
@@ -477,14 +556,21 @@ __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int 
   return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// Whether a newly met substance with compound bits `comp` is composited
+// (lastIsSet for a new substance, K:1496).
+__device__ __forceinline__ bool lastIsSetFor(uint64_t comp) {
+  return comp == GUDNI_TAG_ADD || comp == GUDNI_TAG_CONTINUE;
+}
+
 // determineColor K:1447-1513
 template <int SECTIONS>
 __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
                                                  const uint32_t* shapeIdx, int px, int py, int& status,
-                                                 int64_t& texels, int topStart) {
+                                                 int64_t& texels, int topStart, bool& positional) {
   // The reference starts at MAXSHAPE (K:1453); no bit at or above the column's
   // assigned shape-bit count is ever set, so starting there finds the same bits.
   int topBit = topStart;
+  positional = false;
   float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float4 next = base;
   bool done = false;
@@ -514,7 +600,9 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
         }
         shouldComposite = false;
       } else {
-        next = readColor(in, px, py, sid, tag & GUDNI_TAG_SUBSTANCE_MASK, status, texels);
+        const uint64_t type = tag & GUDNI_TAG_SUBSTANCE_MASK;
+        next = readColor(in, px, py, sid, type, status, texels);
+        positional = positional || (type != GUDNI_TAG_SOLID && lastIsSetFor(comp));
         lastIsSet = comp == GUDNI_TAG_ADD || comp == GUDNI_TAG_CONTINUE;
       }
       lastId = sid;
@@ -526,6 +614,48 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
   }
   return base;
 }
+
+// Memo of determineColor.  The section colour is a pure function of the shape-stack
+// bits and, when a picture or gradient layer was composited, of the pixel position
+// (the column fixes x, so the row y).  The same stack states recur from section to
+// section (every vertical slice restarts from the left-border state, interior pixels
+// repeat the previous pixel's state), so a few entries keyed by the full stack words
+// serve most sections.  Lookups compare every word: results are exactly those of a
+// fresh determineColor.
+template <int SECTIONS>
+struct ColorCache {
+  static constexpr int N = 4;
+  uint64_t key[N][SECTIONS];
+  int row[N];      // -1: colour independent of position; else the pixel row it holds for
+  float4 color[N];
+  int next;
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int e = 0; e < N; ++e) row[e] = -2;  // -2: empty
+    next = 0;
+  }
+  __device__ __forceinline__ bool find(const ShapeStack<SECTIONS>& st, int py, float4& out) const {
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+      bool same = row[e] != -2 && (row[e] == -1 || row[e] == py);
+#pragma unroll
+      for (int w = 0; w < SECTIONS; ++w) same = same && key[e][w] == st.w[w];
+      if (same) {
+        out = color[e];
+        return true;
+      }
+    }
+    return false;
+  }
+  __device__ __forceinline__ void put(const ShapeStack<SECTIONS>& st, int py, bool positional, float4 c) {
+    const int e = next;
+    next = (next + 1) & (N - 1);
+#pragma unroll
+    for (int w = 0; w < SECTIONS; ++w) key[e][w] = st.w[w];
+    row[e] = positional ? py : -1;
+    color[e] = c;
+  }
+};
 
 struct Parse {
   int current, numActive;
@@ -652,6 +782,8 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   uint32_t* outp = in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
   int64_t sections = 0;
   int64_t texels = 0;
+  ColorCache<SECTIONS> cache;
+  cache.clear();
   for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
     int guard = 0;
@@ -673,7 +805,12 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       }
       p.sStartX = p.sEndX;
       p.sEndX = nextX;
-      const float4 color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits);
+      float4 color;
+      if (!cache.find(stack, py, color)) {
+        bool positional;
+        color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, positional);
+        cache.put(stack, py, positional, color);
+      }
       float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
       if (in.stochastic != 0.0f) {  // getRandom K:1608-1613
         cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);
