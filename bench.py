@@ -63,10 +63,15 @@ WORKLOADS = {
                   "Mpixels/s (plain single-frame raster, 512x512 64 shapes, <=1 LSB RGBA8)"),
     # the batched form (run_batch)
     "batch256": ("batch_mix_256_scenes", "frames/s (batched raster, 256-scene mix, <=1 LSB RGBA8)"),
+    # the differentiable form (run_adjoint): 1024x1024, 500 random shapes of 16 segments
+    "adjoint1024": ("random_1024x1024_shapes500_seg16",
+                    "Mpixels/s (fwd+adjoint, 1024x1024 500 shapes, grads vs FP64 reference)"),
 }
 
 
-def make_frame(workload: str = "page4k"):
+def make_frame(workload: str = "page4k", baked: bool = False):
+    """The workload's serialized frame.  baked=True expresses each radial gradient as
+    a picture (scene.bake_radials), the form the reference kernels can render."""
     from gudni_gb300 import lib as L
     from gudni_gb300 import scene as S
     from gudni_gb300 import scenes as G
@@ -74,7 +79,37 @@ def make_frame(workload: str = "page4k"):
     spec = L.make_spec(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
                        stack_sections=8)
     flat = G.glyph_page(seed=1) if workload == "page4k" else G.random_shapes(seed=0)
+    if baked:
+        flat = S.bake_radials(flat)
     return S.serialize_flat(flat, spec)
+
+
+def reference_runner(workload: str, frame):
+    """A callable rendering the workload once on the host cores, and what it is: the
+    reference's own kernels (oracle/_ref) on the workload with radial gradients baked
+    into pictures, else the oracle restatement on the workload itself.  Also returns
+    the reference image and the oracle image, for the parity note."""
+    from oracle import oracle as O
+    want = O.render_frame(frame)
+    fn, kind, img = (lambda: O.render_frame(frame)), "port", want  # noqa: E731
+    if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
+        try:
+            ref_frame = make_frame(workload, baked=True) if len(frame.radials) else frame
+            st = {}
+            O.render_frame(ref_frame, stats=st)
+            cap = int(st["max_queue"]) + 16  # the reference writes past a full slab
+            img = O.ref_render_frame(ref_frame, max_thresholds=cap)  # build + warm
+            fn = lambda: O.ref_render_frame(ref_frame, max_thresholds=cap)  # noqa: E731
+            kind = "reference"
+        except Exception as e:  # noqa: BLE001
+            print(f"reference kernels unavailable ({e}); timing the oracle", file=sys.stderr)
+            fn, kind, img = (lambda: O.render_frame(frame)), "port", want  # noqa: E731
+    return fn, kind, img, want
+
+
+def lsb_parity(a, b):
+    d = np.abs(a.view(np.uint8).astype(np.int16) - b.view(np.uint8).astype(np.int16))
+    return {"max_lsb": int(d.max()), "exact_pixel_frac": float(np.mean(np.all(d.reshape(-1, 4) == 0, axis=1)))}
 
 
 def config_dict(frame, workload="page4k"):
@@ -187,48 +222,29 @@ def profile_traffic(workload):
     return None, None
 
 
-def cpu_baseline(frame, frames: int):
+def cpu_baseline(workload, frame, frames: int):
     """The reference kernels (or the oracle restatement) on all host cores, one frame
-    per sample; returns (Mpixels/s, kind, cores, image)."""
-    from oracle import oracle as O
+    per sample; returns (Mpixels/s, kind, cores, oracle image, seconds per frame,
+    reference-vs-oracle parity)."""
     cores = os.cpu_count() or 1
-    st = {}
-    img = O.render_frame(frame, stats=st)  # oracle pass: sizes the reference's slabs, parity image
-    kind = "port"
-    fn = lambda: O.render_frame(frame)  # noqa: E731
-    try:
-        if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
-            cap = int(st["max_queue"]) + 16
-            O.ref_render_frame(frame, max_thresholds=cap)  # build + warm
-            fn = lambda: O.ref_render_frame(frame, max_thresholds=cap)  # noqa: E731
-            kind = "reference"
-    except Exception:
-        kind = "port"
+    fn, kind, img, want = reference_runner(workload, frame)
     t0 = time.perf_counter()
     for _ in range(frames):
         fn()
     dt = (time.perf_counter() - t0) / frames
-    return frame.canvas_w * frame.canvas_h / dt / 1e6, kind, cores, img, dt
+    return frame.canvas_w * frame.canvas_h / dt / 1e6, kind, cores, want, dt, lsb_parity(img, want)
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    if args.workload not in ("page4k", "random512"):
+        print(json.dumps({"impl": "reference", "unavailable": f"workload {args.workload} has no reference "
+                          "counterpart (the reference renders one scene per call and has no adjoint)"}))
+        return 0
     frame = make_frame(args.workload)
-    from oracle import oracle as O
-    st = {}
-    O.render_frame(frame, stats=st)
-    cap = int(st["max_queue"]) + 16
-    kind = "port"
-    fn = lambda: O.render_frame(frame)  # noqa: E731
-    if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
-        try:
-            O.ref_render_frame(frame, max_thresholds=cap)
-            fn = lambda: O.ref_render_frame(frame, max_thresholds=cap)  # noqa: E731
-            kind = "reference"
-        except Exception:
-            kind = "port"
+    fn, kind, img, want = reference_runner(args.workload, frame)
     for _ in range(args.warmup):
         fn()
     times = []
@@ -240,12 +256,15 @@ def run_reference(args):
     v = frame.canvas_w * frame.canvas_h / (ms / 1000) / 1e6
     cores = os.cpu_count() or 1
     sample = "one full frame per step (all jobs), OpenMP over all host cores"
+    if kind == "reference" and len(frame.radials):
+        sample += "; radial gradients baked into pictures (the reference has no radial substance)"
     line = {"impl": "reference", "metric": WORKLOADS[args.workload][1], "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_dict(frame, args.workload),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "parity_reference_vs_oracle": lsb_parity(img, want)}
     print(json.dumps(line))
     return 0
 
@@ -349,12 +368,133 @@ def run_batch(args):
     return 0
 
 
+ADJ_SPEC = dict(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=511, stack_sections=8,
+                max_strands_per_tile=1 << 24)  # 500 canvas-wide shapes: no strand-count tile splitting
+
+
+def adjoint_scene(jitter_px: float = 0.0):
+    """1024x1024 canvas, 500 random shapes of 16 quadratic segments (seeded); the
+    target copy has every control point jittered by N(0, jitter_px)."""
+    from gudni_gb300 import scenes as G
+    flat = G.random_shapes(seed=3, width=1024, height=1024, n_shapes=500, seg_lo=16, seg_hi=16)
+    if jitter_px:
+        rng = np.random.default_rng(4)
+        flat.pairs = (flat.pairs + rng.normal(0, jitter_px, flat.pairs.shape)).astype(np.float32)
+    return flat
+
+
+def run_adjoint(args):
+    """The differentiable form: forward raster vs one fwd+adjoint launch on the same
+    frame; gradients checked against the FP64 reference adjoint and against central
+    differences (h = 1e-2 px) of the loss on the largest point-gradient entries."""
+    import torch
+    from gudni_gb300 import adjoint as A
+    from gudni_gb300 import lib as L
+    from gudni_gb300 import scene as S
+    from gudni_gb300.raster import Rasterizer
+
+    torch.cuda.set_device(0)
+    spec = L.make_spec(**ADJ_SPEC)
+    frame = S.serialize_flat(adjoint_scene(), spec)
+    tframe = S.serialize_flat(adjoint_scene(4.0), spec)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    r = Rasterizer(spec)
+    with torch.cuda.stream(stream):
+        tr = A.FrameAdjoint(r, tframe)
+        _, timg, _, _ = tr.loss_and_gradient(np.zeros((1024, 1024, 4), np.float32))
+        target = timg.clone()
+        target[..., 3] = 0
+        fa = A.FrameAdjoint(r, frame)
+        out = torch.zeros(1024 * 1024, dtype=torch.int32, device=dev)
+
+        def forward():
+            r.raster_tiles_device(frame, fa.shapes.data_ptr(), fa.n_shapes, fa.tiles.data_ptr(),
+                                  fa.tile_jobs.data_ptr(), fa.n_tiles, out.data_ptr(), stream=stream.cuda_stream)
+
+        def fwd_adjoint():
+            fa.enqueue(target)
+
+        def timed(fn, steps):
+            ts = []
+            for _ in range(steps):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                flush.zero_()
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+            return ts
+
+        for _ in range(args.warmup):
+            forward()
+            fwd_adjoint()
+        r.sync_status()
+        launches0 = r.launch_count()
+        with ClockSampler(0) as clocks:
+            ft = timed(forward, args.steps)
+            at = timed(fwd_adjoint, args.steps)
+        r.sync_status()
+        launches = r.launch_count() - launches0
+        fwd_ms, adj_ms = statistics.median(ft), statistics.median(at)
+        loss, img, gg, gs = fa.loss_and_gradient(target)
+        gg, gs = gg.cpu().numpy().astype(np.float64), gs.cpu().numpy().astype(np.float64)
+        img = img.cpu().numpy()
+        tnp = target.cpu().numpy()
+    check = {}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        loss_ref, g_geo, g_sub, _ = O.loss_and_gradient(frame, tnp)
+        t_ref = time.perf_counter() - t0
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        check["fp64_reference"] = {"geometry_rel_err": rel(gg, g_geo), "substance_rel_err": rel(gs.ravel(),
+                                                                                              g_sub.ravel()),
+                                   "loss": float(loss), "loss_fp64": loss_ref, "host_s": t_ref}
+        # central differences of the GPU loss at h = 1e-2 px on the 8 largest point entries
+        gp = S.pair_gradient(frame, gg)
+        idx = np.argsort(-np.abs(gp.ravel()))[:8]
+        h = 1e-2
+        fd_rel = []
+        with torch.cuda.stream(stream):
+            for k in idx:
+                p, c = divmod(int(k), 4)
+                vals = []
+                for sgn in (1, -1):
+                    fl = adjoint_scene()
+                    fl.pairs[p, c] += sgn * h
+                    f2 = S.serialize_flat(fl, spec)
+                    vals.append(float(A.FrameAdjoint(r, f2).loss_and_gradient(target)[0]))
+                fd = (vals[0] - vals[1]) / (2 * h)
+                fd_rel.append(abs(gp[p, c] - fd) / max(abs(fd), 1e-12))
+        check["central_differences_h1e-2"] = {"entries": len(fd_rel), "median_rel_err": float(np.median(fd_rel)),
+                                              "max_rel_err": float(np.max(fd_rel))}
+    pixels = 1024 * 1024
+    line = {"metric": WORKLOADS["adjoint1024"][1], "value": pixels / (adj_ms / 1000) / 1e6, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": adj_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["adjoint1024"][0], "canvas": [1024, 1024], "shapes": 500,
+                       "segments": 16, "target": "same scene, control points jittered N(0, 4 px)",
+                       "tiles": int(frame.n_tiles), **ADJ_SPEC, "l2": "flushed between steps (256 MB write)",
+                       "data": "synthetic, seeded"},
+            "forward_ms": fwd_ms, "fwd_adjoint_ms": adj_ms, "fwd_adjoint_over_forward": adj_ms / fwd_ms,
+            "gpu_launches": int(launches), "clocks": clocks.summary(), "gradient_check": check}
+    print(json.dumps(line))
+    r.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch256":
         return run_batch(args)
+    if args.workload == "adjoint1024":
+        return run_adjoint(args)
 
     import torch
 
@@ -506,12 +646,13 @@ def main():
                      "sections_per_s": counters["sections"] / (ms / 1000)},
             "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)}}
     if world == 1 and not args.no_cpu_baseline:
-        v, kind, cores, img, dt = cpu_baseline(frame, args.cpu_sample_frames)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
-                                "sample": f"{args.cpu_sample_frames} full frame(s), {dt:.2f} s each"}
-        d = np.abs(gpu_img.view(np.uint8).astype(np.int16) - img.view(np.uint8).astype(np.int16))
-        line["parity_vs_oracle"] = {"max_lsb": int(d.max()),
-                                    "exact_pixel_frac": float(np.mean(np.all(d.reshape(-1, 4) == 0, axis=1)))}
+        v, kind, cores, img, dt, ref_parity = cpu_baseline(args.workload, frame, args.cpu_sample_frames)
+        sample = f"{args.cpu_sample_frames} full frame(s), {dt:.2f} s each"
+        if kind == "reference" and len(frame.radials):
+            sample += "; radial gradients baked into pictures (the reference has no radial substance)"
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+        line["parity_vs_oracle"] = lsb_parity(gpu_img, img)
+        line["parity_reference_vs_oracle"] = ref_parity
     print(json.dumps(line))
     r.close()
     return 0

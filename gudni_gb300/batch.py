@@ -48,6 +48,8 @@ class Batch:
     frames: list              # the source frames
     frame_offsets: np.ndarray  # first output pixel of each frame
     frame_tiles: list          # (first tile, tile count) of each frame
+    frame_geo_offsets: np.ndarray = None  # first byte of each frame in the geometry pile
+    frame_sub_offsets: np.ndarray = None  # first substance of each frame
 
     def images(self, out: np.ndarray) -> List[np.ndarray]:
         """Split the batch output into per-frame (H, W) images."""
@@ -75,7 +77,7 @@ def build_batch(frames) -> Batch:
     geo, subs, pics, uses, rads = [], [], [], [], []
     shapes, tiles, tile_scene, costs, scenes = [], [], [], [], []
     geo_off = sub_off = pic_off = use_off = rad_off = shape_off = out_off = 0
-    frame_offsets, frame_tiles = [], []
+    frame_offsets, frame_tiles, frame_geo, frame_sub = [], [], [], []
     tile_count = 0
     for fi, f in enumerate(frames):
         if f.geometry.size % 16:
@@ -99,6 +101,8 @@ def build_batch(frames) -> Batch:
         rads.append(f.radials)
         pics.append(f.pictures)
         frame_offsets.append(out_off)
+        frame_geo.append(geo_off)
+        frame_sub.append(sub_off)
         first_tile = tile_count
         for ji, job in enumerate(f.jobs):
             sh = job.shapes.copy()
@@ -135,7 +139,8 @@ def build_batch(frames) -> Batch:
         radials=cat(rads, L.RADIAL_DTYPE), shapes=cat(shapes, L.SHAPE_DTYPE), tiles=cat(tiles, L.TILE_DTYPE),
         tile_scene=cat(tile_scene, np.int32), tile_cost=cat(costs, np.float32),
         scenes=np.concatenate(scenes) if scenes else np.zeros(0, BATCH_SCENE_DTYPE), out_pixels=int(out_off),
-        frames=list(frames), frame_offsets=np.asarray(frame_offsets, np.int64), frame_tiles=frame_tiles)
+        frames=list(frames), frame_offsets=np.asarray(frame_offsets, np.int64), frame_tiles=frame_tiles,
+        frame_geo_offsets=np.asarray(frame_geo, np.int64), frame_sub_offsets=np.asarray(frame_sub, np.int64))
 
 
 class BatchRasterizer(Rasterizer):
@@ -191,3 +196,28 @@ class BatchRasterizer(Rasterizer):
     def render_images(self, use_graph: bool = True) -> List[np.ndarray]:
         self.render(use_graph)
         return self.batch.images(self.download())
+
+    def adjoint(self, target, image, grad_geometry, grad_substances, stream: int = 0) -> None:
+        """Enqueue the adjoint of every scene of the batch in one launch
+        (gudni_batch_adjoint) on `stream` (0: torch's current stream).  All four are
+        device tensors: target and image
+        (out_pixels, 4) float32 at the scenes' output offsets, grad_geometry
+        (geometry bytes / 4,) and grad_substances (n_substances, 4) float32, ADDED to."""
+        import torch
+        b = self.batch
+        for t, shape in ((target, (b.out_pixels, 4)), (image, (b.out_pixels, 4)),
+                         (grad_geometry, (b.geometry.size // 4,)), (grad_substances, (len(b.substances), 4))):
+            assert t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and tuple(t.shape) == shape
+        if not stream:
+            stream = L.current_stream_handle()
+        self._check(self.lib.gudni_batch_adjoint(self.ctx, target.data_ptr(), image.data_ptr(),
+                                                 grad_geometry.data_ptr(), grad_substances.data_ptr(),
+                                                 stream or None))
+
+    def frame_slices(self, i: int):
+        """(geometry float slice, substance slice) of frame i in the batch gradients."""
+        b = self.batch
+        f = b.frames[i]
+        g0 = int(b.frame_geo_offsets[i]) // 4
+        s0 = int(b.frame_sub_offsets[i])
+        return slice(g0, g0 + f.geometry.size // 4), slice(s0, s0 + len(f.substances))

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint_kernels.h"
 #include "gudni_cuda.h"
 #include "raster_kernels.h"
 
@@ -132,6 +133,19 @@ struct gudni_ctx {
   DevBuf<int> status;
   DevBuf<int64_t> counters;
   bool counters_on = false;
+
+  // adjoint scratch: slots x capacity thresholds, provenance and line records
+  int adj_grid = 0;
+  int adj_capacity = 0;
+  DevBuf<float4> a_thr;
+  DevBuf<uint32_t> a_hdr;
+  DevBuf<int4> a_prov;
+  DevBuf<uint8_t> a_lines;
+  DevBuf<float4> a_line_grad;
+  DevBuf<uint32_t> a_idx;
+  DevBuf<float4> a_bit_grad;
+  DevBuf<float4> a_layers;
+  DevBuf<int32_t> a_layer_bits;
   uint64_t launches = 0;
   cudaStream_t last_stream = nullptr;
 };
@@ -428,6 +442,92 @@ void drop_graph(gudni_ctx* ctx) {
   ctx->graph = nullptr;
 }
 
+// Adjoint scratch, sized once: one slot per resident thread (capped so the whole
+// stays within ~6 GB), each holding `capacity` thresholds with their provenance and
+// line records, per-shape-bit index and colour-gradient words, and the composited
+// layers of one section (at most max_shape + 1).
+int ensure_adjoint_scratch(gudni_ctx* ctx) {
+  if (ctx->adj_grid) return GUDNI_OK;
+  int rc = ensure_scratch(ctx);  // status word
+  if (rc) return rc;
+  int cap = std::min(ctx->spec.max_thresholds, 1024);
+  if (const char* env = std::getenv("GUDNI_ADJOINT_CAPACITY")) {
+    const int v = std::atoi(env);
+    if (v >= 4) cap = std::min(ctx->spec.max_thresholds, v);
+  }
+  int bps = 1;
+  if (gudni::adjoint_occupancy(ctx->sections, &bps) != cudaSuccess || bps < 1) bps = 1;
+  const size_t per_slot = (size_t)cap * (sizeof(float4) + 4 + sizeof(int4) + gudni::adjoint_line_bytes() +
+                                         sizeof(float4)) +
+                          (size_t)ctx->spec.max_shape * (4 + sizeof(float4)) +
+                          (size_t)(ctx->spec.max_shape + 1) * (2 * sizeof(float4) + 4);
+  size_t slots = (size_t)ctx->sm_count * (size_t)bps * gudni::kAdjointBlock;
+  slots = std::min(slots, ((size_t)6 << 30) / per_slot);
+  slots = std::max<size_t>(gudni::kAdjointBlock, (slots / gudni::kAdjointBlock) * gudni::kAdjointBlock);
+  cudaError_t e;
+  if ((e = ctx->a_thr.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_hdr.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_prov.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_lines.reserve(slots * cap * gudni::adjoint_line_bytes())) != cudaSuccess ||
+      (e = ctx->a_line_grad.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_idx.reserve(slots * (size_t)ctx->spec.max_shape)) != cudaSuccess ||
+      (e = ctx->a_bit_grad.reserve(slots * (size_t)ctx->spec.max_shape)) != cudaSuccess ||
+      (e = ctx->a_layers.reserve(slots * 2 * (size_t)(ctx->spec.max_shape + 1))) != cudaSuccess ||
+      (e = ctx->a_layer_bits.reserve(slots * (size_t)(ctx->spec.max_shape + 1))) != cudaSuccess)
+    return cuda_fail(ctx, e, "adjoint scratch");
+  ctx->adj_capacity = cap;
+  ctx->adj_grid = (int)(slots / gudni::kAdjointBlock);
+  return GUDNI_OK;
+}
+
+int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInfo* scenes,
+                    const int32_t* tile_scene, size_t n_scenes, const uint32_t* order, size_t n_tiles,
+                    const float* target, float* image, float* grad_geometry, float* grad_substances,
+                    cudaStream_t stream) {
+  int rc = ensure_adjoint_scratch(ctx);
+  if (rc) return rc;
+  if (n_tiles == 0) return GUDNI_OK;
+  cudaError_t e = cudaMemsetAsync(ctx->words.ptr, 0, 2 * sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
+  gudni::AdjointLaunch a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = in;
+  a.in.counters = nullptr;
+  a.scenes = scenes;
+  a.tile_scene = tile_scene;
+  a.n_scenes = (uint32_t)n_scenes;
+  a.order = order;
+  a.n_tiles = (uint32_t)n_tiles;
+  a.next_tile = ctx->words.ptr + 1;
+  a.capacity = ctx->adj_capacity;
+  a.thr = ctx->a_thr.ptr;
+  a.hdr = ctx->a_hdr.ptr;
+  a.prov = ctx->a_prov.ptr;
+  a.lines = ctx->a_lines.ptr;
+  a.line_grad = ctx->a_line_grad.ptr;
+  a.idx = ctx->a_idx.ptr;
+  a.bit_grad = ctx->a_bit_grad.ptr;
+  a.layers = ctx->a_layers.ptr;
+  a.layer_bits = ctx->a_layer_bits.ptr;
+  a.image = reinterpret_cast<float4*>(image);
+  a.target = reinterpret_cast<const float4*>(target);
+  a.grad_geometry = grad_geometry;
+  a.grad_substances = grad_substances;
+  a.status = ctx->status.ptr;
+  const size_t warps_per_block = gudni::kAdjointBlock / 32;
+  const int grid = (int)std::min<size_t>((n_tiles + warps_per_block - 1) / warps_per_block, (size_t)ctx->adj_grid);
+  if ((e = gudni::launch_adjoint(a, ctx->sections, grid, stream)) != cudaSuccess)
+    return cuda_fail(ctx, e, "adjoint launch");
+  ctx->launches += 1;
+  return GUDNI_OK;
+}
+
+bool adjoint_pointers_ok(const float* target, const float* image, const float* grad_geometry,
+                         const float* grad_substances) {
+  return target && image && grad_geometry && grad_substances && ((uintptr_t)target & 15) == 0 &&
+         ((uintptr_t)image & 15) == 0 && ((uintptr_t)grad_geometry & 3) == 0 && ((uintptr_t)grad_substances & 3) == 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -485,6 +585,9 @@ void gudni_destroy(gudni_ctx* ctx) {
   ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release(); ctx->big_hdr.release();
   ctx->big_idx.release(); ctx->overflow_items.release(); ctx->words.release(); ctx->status.release();
   ctx->counters.release();
+  ctx->a_thr.release(); ctx->a_hdr.release(); ctx->a_prov.release(); ctx->a_lines.release();
+  ctx->a_line_grad.release(); ctx->a_idx.release(); ctx->a_bit_grad.release(); ctx->a_layers.release();
+  ctx->a_layer_bits.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -799,5 +902,42 @@ int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]) {
 }
 
 uint64_t gudni_launch_count(const gudni_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int gudni_adjoint_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
+                               const gudni_tile_info* tiles, const int32_t* tile_jobs, size_t n_tiles,
+                               int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth, const float background[4],
+                               const float* target, float* image, float* grad_geometry, float* grad_substances,
+                               void* stream) {
+  int rc = validate_job(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, false);
+  if (rc) return rc;
+  if (!background) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null background");
+  if (!adjoint_pointers_ok(target, image, grad_geometry, grad_substances))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null or misaligned target, image or gradient pointer");
+  if (((uintptr_t)shapes & 7) != 0 || ((uintptr_t)tiles & 3) != 0 || ((uintptr_t)tile_jobs & 3) != 0)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "misaligned device pointer");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, 0,
+                                  background, nullptr);
+  in.tile_jobs = tile_jobs;
+  return enqueue_adjoint(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, target, image, grad_geometry,
+                         grad_substances, s);
+}
+
+int gudni_batch_adjoint(gudni_ctx* ctx, const float* target, float* image, float* grad_geometry,
+                        float* grad_substances, void* stream) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!ctx->batch_ready) return fail(ctx, GUDNI_ERR_NOT_READY, "gudni_batch_upload has not been called");
+  if (!adjoint_pointers_ok(target, image, grad_geometry, grad_substances))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null or misaligned target, image or gradient pointer");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  ctx->last_stream = s;
+  gudni::RasterInputs in = inputs(ctx, ctx->b_shapes.ptr, ctx->batch_shapes, ctx->b_tiles.ptr, ctx->batch_tiles, 1,
+                                  1, 0, 0, nullptr, nullptr);
+  return enqueue_adjoint(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr, ctx->batch_scenes, ctx->b_order.ptr,
+                         ctx->batch_tiles, target, image, grad_geometry, grad_substances, s);
+}
 
 }  // extern "C"

@@ -48,6 +48,39 @@ struct TileLaunch {
   int* status;                  // kStatus* bits
 };
 
+__device__ __forceinline__ bool tileOk(const gudni_tile_info& ti, uint32_t n_shapes) {
+  return ti.hdepth >= 0 && ti.hdepth <= 24 && ti.vdepth >= 0 && ti.vdepth <= 24 && ti.left >= 0 &&
+         ti.top >= 0 && ti.right >= ti.left && ti.bottom >= ti.top &&
+         (uint64_t)ti.shapes.start + (uint64_t)ti.shapes.length <= (uint64_t)n_shapes;
+}
+
+// The inputs of tile `tile`: the shared piles plus its scene's canvas, output,
+// background, threads per tile and job index.
+__device__ __forceinline__ RasterInputs sceneInputs(const RasterInputs& base, const SceneInfo* scenes,
+                                                    const int32_t* tile_scene, uint32_t n_scenes, int tile,
+                                                    int& status, bool& ok) {
+  RasterInputs in = base;
+  ok = true;
+  if (scenes) {
+    const uint32_t s = (uint32_t)tile_scene[tile];
+    if (s >= n_scenes) {
+      status |= kStatusBadInput;
+      ok = false;
+      return in;
+    }
+    const SceneInfo sc = scenes[s];
+    in.bitmap_w = sc.bitmap_w;
+    in.bitmap_h = sc.bitmap_h;
+    in.log2_tpt = sc.log2_tpt;
+    in.job_index = sc.job_index;
+    in.out = base.out + sc.out_offset;
+    in.background = make_float4(sc.background[0], sc.background[1], sc.background[2], sc.background[3]);
+  } else if (base.tile_jobs) {
+    in.job_index = base.tile_jobs[tile];
+  }
+  return in;
+}
+
 int sections_for(int max_shape);
 cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream);
 cudaError_t raster_occupancy(int sections, int* blocks_per_sm);

@@ -186,8 +186,23 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_read_counters.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.gudni_launch_count.restype = C.c_uint64
     lib.gudni_launch_count.argtypes = [vp]
+    lib.gudni_adjoint_tiles_device.restype = C.c_int
+    lib.gudni_adjoint_tiles_device.argtypes = [vp, vp, sz, vp, vp, sz, i32, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.gudni_batch_adjoint.restype = C.c_int
+    lib.gudni_batch_adjoint.argtypes = [vp, vp, vp, vp, vp, vp]
     _cuda = lib
     return lib
+
+
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the runtime's handle for the legacy default stream
+
+
+def current_stream_handle() -> int:
+    """torch's current CUDA stream as a handle the C ABI can take.  A null stream
+    argument means the context's own (non-blocking) stream there, so torch's legacy
+    default stream, whose handle is 0, is passed as cudaStreamLegacy instead."""
+    import torch
+    return torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
 
 
 def ptr(a) -> int | None:

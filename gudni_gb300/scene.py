@@ -390,6 +390,62 @@ def flatten(scene: Scene, canvas_w: int, canvas_h: int) -> FlatScene:
     )
 
 
+def bake_radials(flat: FlatScene) -> FlatScene:
+    """The same scene with every radial-gradient substance replaced by an RGBA8
+    picture of the gradient over its shapes' bounding box: the reference's only route
+    for a gradient (a PictureFunction evaluated on the host into a bitmap,
+    Figure/Picture.hs:59-73), whose kernels know solid colours and pictures only
+    (Kernels.cl readColor, K:1411-1442).  Texels are the gradient at integer pixel
+    positions, as the radial substance evaluates it, rounded to 8 bits, so the two
+    renderings agree within one LSB per channel."""
+    kinds = flat.substance_kind.copy()
+    pics = flat.substance_picture.copy()
+    pxf = flat.substance_picture_xform.copy()
+    sizes = [tuple(s) for s in flat.picture_size.reshape(-1, 2)]
+    offsets = list(flat.picture_offset.astype(np.int64))
+    chunks = [flat.pictures]
+    off = int(flat.pictures.size)
+    pts = flat.pairs.reshape(-1, 2)
+    for i in np.nonzero(kinds == 2)[0]:
+        s0, s1 = flat.substance_shape_start[i], flat.substance_shape_start[i + 1]
+        o0, o1 = flat.shape_outline_start[s0], flat.shape_outline_start[s1]
+        p0, p1 = flat.outline_pair_start[o0], flat.outline_pair_start[o1]
+        p = pts[2 * p0:2 * p1]
+        if p.size == 0:
+            x0 = y0 = 0
+            x1 = y1 = 1
+        else:
+            x0 = int(np.clip(np.floor(p[:, 0].min()), 0, flat.canvas_w - 1))
+            y0 = int(np.clip(np.floor(p[:, 1].min()), 0, flat.canvas_h - 1))
+            x1 = int(np.clip(np.ceil(p[:, 0].max()) + 1, x0 + 1, flat.canvas_w))
+            y1 = int(np.clip(np.ceil(p[:, 1].max()) + 1, y0 + 1, flat.canvas_h))
+        g = flat.substance_radial[i]
+        ys, xs = np.mgrid[y0:y1, x0:x1].astype(np.float32)
+        dx = xs - np.float32(g["center_x"])
+        dy = ys - np.float32(g["center_y"])
+        t = np.minimum(np.sqrt(dx * dx + dy * dy) / np.float32(g["radius"]), np.float32(1.0))
+        inner, outer = g["inner"].astype(np.float32), g["outer"].astype(np.float32)
+        rgba = inner[None, None, :] + (outer - inner)[None, None, :] * t[..., None]
+        texels = np.clip(np.round(rgba * np.float32(255.0)), 0, 255).astype(np.uint8)
+        kinds[i] = 1
+        pics[i] = len(sizes)
+        pxf[i] = (np.float32(x0), np.float32(y0), np.float32(1.0))
+        sizes.append((x1 - x0, y1 - y0))
+        offsets.append(off)
+        chunks.append(texels.reshape(-1))
+        off += texels.size
+    return FlatScene(
+        canvas_w=flat.canvas_w, canvas_h=flat.canvas_h, background=flat.background,
+        substance_kind=kinds, substance_color=flat.substance_color, substance_picture=pics,
+        substance_picture_xform=np.ascontiguousarray(pxf, dtype=np.float32),
+        substance_radial=np.zeros(len(kinds), dtype=L.RADIAL_DTYPE),
+        substance_shape_start=flat.substance_shape_start, shape_compound=flat.shape_compound,
+        shape_outline_start=flat.shape_outline_start, outline_pair_start=flat.outline_pair_start,
+        pairs=flat.pairs, pictures=np.concatenate(chunks),
+        picture_size=np.asarray(sizes, dtype=np.int32).reshape(-1, 2),
+        picture_offset=np.asarray(offsets, dtype=np.int32))
+
+
 # ------------------------------------------------------------------ serialized frame
 
 

@@ -239,6 +239,34 @@ int gudni_batch_download(gudni_ctx* ctx, uint32_t* out);
 int gudni_enable_counters(gudni_ctx* ctx, int enable);
 int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
 
+/* ------------------------------------------------------------------ adjoint */
+
+/* Gradients of the per-pixel L2 loss L = sum_p sum_{c in RGB} (I_c(p) - T_c(p))^2,
+ * where I(p) is the pixel colour before the byte conversion (the reference's
+ * accumulated colour / area, Kernels.cl:2017), with respect to every float of the
+ * geometry pile and every solid substance colour.  No counterpart in the reference.
+ *
+ * Frame form, device pointers, enqueued on `stream`: the frame's shape and tile piles
+ * as for gudni_raster_tiles_device; `target` and `image` are bitmap_w*bitmap_h float4
+ * (image receives I rgb and the pixel's section-area sum in .w); `grad_geometry`
+ * (geometry_bytes/4 floats) and `grad_substances` (4 floats per substance) are ADDED
+ * to.  Thresholds are recomputed in the backward pass, not stored.  A column that
+ * needs more than the adjoint's working capacity (min(max_thresholds, 1024), or
+ * GUDNI_ADJOINT_CAPACITY) raises GUDNI_ERR_THRESHOLD_OVERFLOW. */
+int gudni_adjoint_tiles_device(gudni_ctx* ctx,
+                               const gudni_shape* shapes, size_t n_shapes,
+                               const gudni_tile_info* tiles, const int32_t* tile_jobs, size_t n_tiles,
+                               int32_t bitmap_w, int32_t bitmap_h, int32_t compute_depth,
+                               const float background[4],
+                               const float* target, float* image,
+                               float* grad_geometry, float* grad_substances, void* stream);
+
+/* Batch form: every scene of the uploaded batch (gudni_batch_upload) in one
+ * persistent launch; target and image hold out_pixels float4 at the scenes' output
+ * offsets; gradients index the batch's concatenated piles. */
+int gudni_batch_adjoint(gudni_ctx* ctx, const float* target, float* image,
+                        float* grad_geometry, float* grad_substances, void* stream);
+
 /* ------------------------------------------------- no-allocation entry point */
 
 /* Size of the device scratch that gudni_raster_job_noalloc uses: a fixed array

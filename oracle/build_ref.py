@@ -83,7 +83,8 @@ def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: in
     Returns the library path, or None when the reference checkout is absent."""
     lib = library_name(max_shape, sections)
     cpp = os.path.join(OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp")
-    if os.path.isfile(lib) and not force:
+    deps = [os.path.join(HERE, "ref_driver.inc"), os.path.join(HERE, "ref_shim.h")]
+    if os.path.isfile(lib) and not force and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in deps):
         return lib
     if os.path.isfile(os.path.join(reference, KERNELS_REL)):
         cpp = generate(reference, max_shape, sections)
@@ -91,7 +92,7 @@ def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: in
         # neither the reference checkout nor a translation unit generated from it
         return None
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
-           "-fPIC", "-shared", "-w", "-I", HERE, cpp, "-o", lib]
+           "-fPIC", "-shared", "-w", "-Wno-psabi", "-I", HERE, cpp, "-o", lib]
     subprocess.run(cmd, check=True)
     return lib
 

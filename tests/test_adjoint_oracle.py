@@ -1,0 +1,135 @@
+"""The FP64 reference adjoint (oracle/adjoint_oracle.cpp) against the raster oracle
+and against central differences of the loss."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from gudni_gb300 import lib as L  # noqa: E402
+from gudni_gb300 import scene as S  # noqa: E402
+from gudni_gb300 import scenes as G  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+SPEC = L.make_spec(32, 32, 4096, 127, 8)
+
+
+def small_scene(seed=5, w=64, h=48, n=6):
+    return G.random_shapes(seed=seed, width=w, height=h, n_shapes=n, seg_lo=6, seg_hi=10)
+
+
+def to_bytes(img):
+    """The reference's colour -> BGRA8 conversion (convert_uchar_sat_rtz of 255*c,
+    alpha 255) applied to the adjoint's float image."""
+    def tb(v):
+        v = v.astype(np.float32) * np.float32(255.0)
+        return np.where(~(v > 0), 0, np.where(v >= 255, 255, np.floor(v))).astype(np.uint32)
+    r, g, b = tb(img[..., 0]), tb(img[..., 1]), tb(img[..., 2])
+    return b | (g << 8) | (r << 16) | np.uint32(255 << 24)
+
+
+def jittered_target(make, sigma, seed=1):
+    rng = np.random.default_rng(seed)
+    t = make()
+    t.pairs = (t.pairs + rng.normal(0, sigma, t.pairs.shape)).astype(np.float32)
+    return O.render_float(S.serialize_flat(t, SPEC))
+
+
+def loss_of(flat, target):
+    im = O.render_float(S.serialize_flat(flat, SPEC))
+    d = im[..., :3].astype(np.float64) - target[..., :3]
+    return float(np.sum(d * d))
+
+
+@pytest.mark.parametrize("seed", [5, 6, 7])
+def test_adjoint_forward_is_the_raster_forward(seed):
+    """The adjoint's float image, converted to bytes, is the raster oracle's image."""
+    frame = S.serialize_flat(small_scene(seed), SPEC)
+    img = O.render_float(frame)
+    assert np.array_equal(to_bytes(img), O.render_frame(frame))
+
+
+def test_adjoint_forward_glyph_page():
+    """Same on a page with subtraction, textures and radial gradients."""
+    frame = S.serialize_flat(G.glyph_page(seed=3, width=256, height=192, n_glyphs=60, n_shapes=30), SPEC)
+    img = O.render_float(frame)
+    b = O.render_frame(frame)
+    # texture and gradient colours go through the same arithmetic; allow the odd
+    # pixel whose colour sits on a byte boundary
+    assert np.mean(to_bytes(img) == b) > 0.999
+
+
+def test_colour_gradient_matches_central_differences():
+    make = small_scene
+    target = jittered_target(make, 2.0)
+    frame = S.serialize_flat(make(), SPEC)
+    _, _, g_sub, _ = O.loss_and_gradient(frame, target)
+    h = 1e-3
+    checked = 0
+    for sid in range(len(frame.substances)):
+        for ch in range(4):
+            if abs(g_sub[sid, ch]) < 1e-2 * np.abs(g_sub).max():
+                continue
+            fp, fm = make(), make()
+            fp.substance_color[sid, ch] += h
+            fm.substance_color[sid, ch] -= h
+            fd = (loss_of(fp, target) - loss_of(fm, target)) / (2 * h)
+            assert abs(fd - g_sub[sid, ch]) <= 1e-3 * abs(fd) + 1e-4, (sid, ch, fd, g_sub[sid, ch])
+            checked += 1
+    assert checked >= 8
+
+
+def test_geometry_gradient_matches_central_differences():
+    """Point gradients against central differences at h = 1e-2 px and 1e-3 px.
+
+    The loss is piecewise smooth, and not continuous, in the points: a curve is
+    rendered as the lines of its column-local bifurcation (Kernels.cl:1233-1258), whose
+    depth and branch change with the points, so the lines jump by up to the flatness
+    bound when an event is crossed.  A central difference that straddles such an event
+    picks up jump / 2h; the adjoint is the derivative of the piece the forward pass
+    is on.  So the test bounds the median relative error over the largest entries and
+    the share of entries within 10 %, not every entry."""
+    make = small_scene
+    target = jittered_target(make, 2.0)
+    frame = S.serialize_flat(make(), SPEC)
+    _, g_geo, _, _ = O.loss_and_gradient(frame, target)
+    gp = S.pair_gradient(frame, g_geo)
+    idx = np.argsort(-np.abs(gp.ravel()))[:16]
+    for h, med_tol in ((1e-2, 0.05), (1e-3, 0.01)):
+        a, f = [], []
+        for k in idx:
+            p, c = divmod(int(k), 4)
+            fp, fm = make(), make()
+            fp.pairs[p, c] += h
+            fm.pairs[p, c] -= h
+            f.append((loss_of(fp, target) - loss_of(fm, target)) / (2 * h))
+            a.append(gp[p, c])
+        a, f = np.asarray(a), np.asarray(f)
+        rel = np.abs(a - f) / np.maximum(np.abs(f), 1e-9)
+        assert np.median(rel) <= med_tol, (h, rel)
+        assert np.mean(rel <= 0.10) >= 0.75, (h, rel)
+
+
+def test_pair_gradient_sums_knob_splits():
+    """pair_gradient is the transpose of the serializer's point provenance: moving a
+    scene point by e moves each pile point by weight * e, so <g_pile, d pile> equals
+    <pair_gradient(g_pile), e>."""
+    flat = small_scene()
+    frame = S.serialize_flat(flat, SPEC)
+    rng = np.random.default_rng(3)
+    g = rng.normal(size=frame.geometry.size // 4)
+    gp = S.pair_gradient(frame, g)
+    p, c = 3, 1
+    e = 1e-2
+    flat2 = small_scene()
+    flat2.pairs[p, c] += e
+    frame2 = S.serialize_flat(flat2, SPEC)
+    if frame2.geometry.size != frame.geometry.size:
+        pytest.skip("the move changed the pile layout")
+    d = frame2.geometry.view(np.float32).astype(np.float64) - frame.geometry.view(np.float32).astype(np.float64)
+    # only point floats move (headers and sizes are equal bit patterns)
+    lhs = float(np.dot(g, np.nan_to_num(d)))
+    assert abs(lhs - gp[p, c] * e) <= 1e-4 * max(1.0, abs(lhs))

@@ -121,3 +121,40 @@ def test_radial_matches_baked_texture():
     # the baked picture quantizes the colour to 8 bits before compositing, so about
     # half the pixels land one LSB apart; none may be further
     assert_parity(a, b, max_lsb=1, min_exact=0.3)
+
+
+def test_bake_radials_matches_radial_substance():
+    """A glyph page with radial gradients renders within one LSB of the same page with
+    each gradient baked into a picture (scene.bake_radials, the form the reference
+    kernels can take)."""
+    flat = G.glyph_page(seed=3, width=256, height=192, n_glyphs=60, n_shapes=30)
+    assert np.any(flat.substance_kind == 2)
+    baked = S.bake_radials(flat)
+    assert not np.any(baked.substance_kind == 2)
+    spec = L.make_spec(32, 32, 4096, 127, 8)
+    a = O.render_frame(S.serialize_flat(flat, spec))
+    b = O.render_frame(S.serialize_flat(baked, spec))
+    from conftest import assert_parity
+    assert_parity(a, b, max_lsb=1, min_exact=0.5)
+
+
+@needs_ref
+def test_reference_kernels_refuse_radial_tags():
+    """The reference kernels read a radial tag as a picture reference with an arbitrary
+    usage index; the driver refuses such a job instead of running it."""
+    flat = G.glyph_page(seed=3, width=256, height=192, n_glyphs=60, n_shapes=30)
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 127, 8))
+    assert len(frame.radials)
+    with pytest.raises(RuntimeError):
+        O.ref_render_frame(frame, max_thresholds=4096)
+
+
+@needs_ref
+def test_reference_kernels_on_baked_page():
+    """The reference kernels on the baked page equal the oracle on the baked page."""
+    flat = S.bake_radials(G.glyph_page(seed=3, width=256, height=192, n_glyphs=60, n_shapes=30))
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 127, 8))
+    st = {}
+    a = O.render_frame(frame, stats=st)
+    b = O.ref_render_frame(frame, max_thresholds=st["max_queue"] + 8)
+    assert np.array_equal(a, b)

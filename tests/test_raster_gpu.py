@@ -137,7 +137,7 @@ def test_device_pointer_path():
             ti = torch.from_numpy(job.tiles.view(np.uint8).copy()).to(dev)
             keep += [sh, ti]
             r.raster_job_device(frame, j, sh.data_ptr(), ti.data_ptr(), out.data_ptr(),
-                                stream=torch.cuda.current_stream().cuda_stream)
+                                stream=L.current_stream_handle())
         r.sync_status()
         torch.cuda.synchronize()
     got = out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
