@@ -285,8 +285,6 @@ def run_batch(args):
     from gudni_gb300 import lib as L
 
     torch.cuda.set_device(0)
-    # columns of the large scenes hold ~1000 thresholds: give the fast pass room for them
-    os.environ.setdefault("GUDNI_WORKING_CAPACITY", "2048")
     t0 = time.perf_counter()
     flats = __import__("gudni_gb300.scenes", fromlist=["batch_mix"]).batch_mix(seed=2, n_scenes=args.scenes)
     t_gen = time.perf_counter() - t0

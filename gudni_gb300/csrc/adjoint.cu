@@ -87,8 +87,42 @@ struct AdjQueue {
     thr[start + cursor] = t;
     prov[start + cursor] = p;
   }
-  // stable insertion sort (the order the forward pass's sort produces)
+  __device__ __forceinline__ void move(int to, int from) {
+    thr[to] = thr[from];
+    hdr[to] = hdr[from];
+    prov[to] = prov[from];
+  }
+  // stable sort (the order the forward pass's sort produces): bottom-up merge sort
+  // through the free slab space below the queue when it has room, else insertion sort
   __device__ __forceinline__ void sort() {
+    const int n = cap - start;
+    if (n >= 32 && start >= n) {
+      int src = start, dst = start - n;
+      for (int width = 1; width < n; width *= 2) {
+        for (int lo = 0; lo < n; lo += 2 * width) {
+          const int mid = min(lo + width, n), hi = min(lo + 2 * width, n);
+          int a = lo, b = mid, o = lo;
+          while (a < mid && b < hi) {
+            if (isBelow(hdr[src + a], thr[src + a], hdr[src + b], thr[src + b])) {
+              move(dst + o, src + b);
+              ++b;
+            } else {
+              move(dst + o, src + a);
+              ++a;
+            }
+            ++o;
+          }
+          while (a < mid) move(dst + o++, src + a++);
+          while (b < hi) move(dst + o++, src + b++);
+        }
+        const int t = src;
+        src = dst;
+        dst = t;
+      }
+      if (src != start)
+        for (int i = 0; i < n; ++i) move(start + i, src + i);
+      return;
+    }
     for (int i = start + 1; i < cap; ++i) {
       const float4 t = thr[i];
       const uint32_t h = hdr[i];
@@ -220,15 +254,22 @@ __device__ __forceinline__ void addLineP(AdjGen& g, const EP& A, const EP& B, ui
   }
 }
 
+// `above`: as spawnThresholds -- the strand lies wholly above the column, only the
+// enclosure flag can change, and the intercepts are not computed.
+__device__ __forceinline__ EP aboveEP(float x) {
+  EP e = pointEP(make_float2(x, -1.0f), x, -1);
+  return e;
+}
+
 __device__ __forceinline__ void spawnP(AdjGen& g, uint32_t bit, Trav& l, Trav& r, bool& added, bool& enclosed,
-                                       int& status) {
-  const EP yl = (l.left.x >= kLeft) ? pointEP(l.left, l.xPos, l.oL) : interceptEP(l, status);
+                                       int& status, bool above) {
+  const EP yl = (l.left.x >= kLeft) ? pointEP(l.left, l.xPos, l.oL) : (above ? aboveEP(l.xPos) : interceptEP(l, status));
   bool leftWing = false;
   if ((l.right.x < kRight) && (l.right.x > kLeft)) {
     addLineP(g, yl, pointEP(l.right, l.right.x, l.oR), bit, added, enclosed);
     leftWing = true;
   }
-  const EP yr = (r.right.x <= kRight) ? pointEP(r.right, r.xPos, r.oR) : interceptEP(r, status);
+  const EP yr = (r.right.x <= kRight) ? pointEP(r.right, r.xPos, r.oR) : (above ? aboveEP(r.xPos) : interceptEP(r, status));
   bool rightWing = false;
   if ((r.left.x > kLeft) && (r.left.x < kRight) && (l.index != r.index)) {
     addLineP(g, pointEP(r.left, r.left.x, r.oL), yr, bit, added, enclosed);
@@ -262,6 +303,36 @@ __device__ __forceinline__ void searchP(Trav& t, const float4* tree, int32_t tre
   }
 }
 
+// traverseTree + spawnThresholds for one strand at byte offset `off` of the pile
+__device__ __forceinline__ void strandP(const RasterInputs& in, AdjGen& g, size_t off, uint32_t size, float2 d,
+                                        uint32_t bits, bool& added, bool& encStrand, int& status, bool above) {
+  const uint8_t* strand = in.geometry + off;
+  const int32_t sb = (int32_t)(off / 4);
+  const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
+  const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
+  Trav l;
+  l.right = make_float2(rp.x - d.x, rp.y - d.y);
+  l.left = make_float2(lc.x - d.x, lc.y - d.y);
+  l.control = make_float2(lc.z - d.x, lc.w - d.y);
+  l.oR = sb + 2;
+  l.oL = sb + 4;
+  l.oC = sb + 6;
+  l.xPos = 0.0f;
+  l.index = 0;
+  if (l.left.x <= kRight && l.right.x > kLeft) {
+    Trav r = l;
+    l.xPos = cl_max(kLeft, l.left.x);
+    r.xPos = cl_min(kRight, l.right.x);
+    const float4* tree = reinterpret_cast<const float4*>(strand + 32);
+    const int treeSize = ((int)size - 4) / 2;
+    searchP(l, tree, sb + 8, treeSize, d, true);
+    searchP(r, tree, sb + 8, treeSize, d, false);
+    spawnP(g, bits, l, r, added, encStrand, status, above);
+  }
+}
+
+// buildThresholdArray with provenance; the same strand-table range test and y
+// culling as the forward generation (buildThresholds), so the decisions match.
 template <int SECTIONS>
 __device__ __forceinline__ uint32_t generateP(const RasterInputs& in, const ColumnState& c, AdjGen& g,
                                               ShapeStack<SECTIONS>& stack, uint32_t* shapeIdx, int& status) {
@@ -271,44 +342,40 @@ __device__ __forceinline__ uint32_t generateP(const RasterInputs& in, const Colu
     const uint32_t si = c.shapeStart + (uint32_t)n;
     const gudni_shape shape = in.shapes[si];
     bool added = false, encShape = false;
-    size_t off = (size_t)shape.geo_start * 16;
-    for (uint32_t k = 0; k < shape.num_strands; ++k) {
-      if (off + 32 > in.geometry_bytes) {
-        status |= kStatusBadInput;
-        break;
-      }
-      const uint8_t* strand = in.geometry + off;
-      const uint32_t size = (uint32_t)(*reinterpret_cast<const uint16_t*>(strand));
-      if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > in.geometry_bytes) {
-        status |= kStatusBadInput;
-        break;
-      }
-      const int32_t sb = (int32_t)(off / 4);
-      const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
-      const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
-      bool encStrand = false;
-      Trav l;
-      l.right = make_float2(rp.x - d.x, rp.y - d.y);
-      l.left = make_float2(lc.x - d.x, lc.y - d.y);
-      l.control = make_float2(lc.z - d.x, lc.w - d.y);
-      l.oR = sb + 2;
-      l.oL = sb + 4;
-      l.oC = sb + 6;
-      l.xPos = 0.0f;
-      l.index = 0;
-      if (l.left.x <= kRight && l.right.x > kLeft) {
-        Trav r = l;
-        l.xPos = cl_max(kLeft, l.left.x);
-        r.xPos = cl_min(kRight, l.right.x);
-        const float4* tree = reinterpret_cast<const float4*>(strand + 32);
-        const int treeSize = ((int)size - 4) / 2;
-        searchP(l, tree, sb + 8, treeSize, d, true);
-        searchP(r, tree, sb + 8, treeSize, d, false);
-        spawnP(g, bits, l, r, added, encStrand, status);
+    uint32_t first = kNoStrand;
+    if (in.strand_table && shape.geo_start < in.n_units) first = in.strand_first[shape.geo_start];
+    if (first != kNoStrand && (uint64_t)first + shape.num_strands <= in.n_strands) {
+      for (uint32_t k = 0; k < shape.num_strands; ++k) {
+        const uint4 e = in.strand_table[first + k];
+        const float lx = __uint_as_float(e.z) - d.x;
+        const float rx = __uint_as_float(e.w) - d.x;
+        if (!(lx <= kRight && rx > kLeft)) continue;
+        const float2 yr = in.strand_y[first + k];
+        if (yr.x - d.y >= c.floatHeight + 1.0f) continue;
+        const bool above = yr.y - d.y <= -1.0f;
+        bool encStrand = false;
+        strandP(in, g, (size_t)e.x * 8, e.y, d, bits, added, encStrand, status, above);
         if (g.q->overflow) return bits;
+        encShape = encShape != encStrand;
       }
-      off += (size_t)size * 8;
-      encShape = encShape != encStrand;
+    } else {
+      size_t off = (size_t)shape.geo_start * 16;
+      for (uint32_t k = 0; k < shape.num_strands; ++k) {
+        if (off + 32 > in.geometry_bytes) {
+          status |= kStatusBadInput;
+          break;
+        }
+        const uint32_t size = (uint32_t)(*reinterpret_cast<const uint16_t*>(in.geometry + off));
+        if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > in.geometry_bytes) {
+          status |= kStatusBadInput;
+          break;
+        }
+        bool encStrand = false;
+        strandP(in, g, off, size, d, bits, added, encStrand, status, false);
+        if (g.q->overflow) return bits;
+        off += (size_t)size * 8;
+        encShape = encShape != encStrand;
+      }
     }
     if (encShape) stack.flip(bits);
     if (added || encShape) {
@@ -323,13 +390,16 @@ __device__ __forceinline__ uint32_t generateP(const RasterInputs& in, const Colu
 // in front of it, and its shape bit (kSolidLayer set for a solid colour; -1 for the
 // background).  Every layer is a distinct substance of a distinct shape bit or the
 // background, so a column with `bits` shape bits has at most bits + 1 layers.
-// Returns the layer count, or -1 past `cap` layers.
+// Returns the layer count, or -1 past `cap` layers; `stopBit` and `positional` as for
+// determineColor's memo (the lowest bit read; whether a picture or gradient layer was
+// composited).
 constexpr int32_t kSolidLayer = 0x40000000;
 
 template <int SECTIONS>
 __device__ __forceinline__ int layersOf(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
                                         const uint32_t* shapeIdx, int px, int py, int topStart, float4* next,
-                                        float4* front, int32_t* bitOf, int cap, float4& color, int& status) {
+                                        float4* front, int32_t* bitOf, int cap, float4& color, bool& positional,
+                                        int& stopBit, int& status) {
   int64_t texels = 0;
   int topBit = topStart;
   float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -340,6 +410,7 @@ __device__ __forceinline__ int layersOf(const RasterInputs& in, const ShapeStack
   uint64_t lastId = ~0ull;
   bool lastIsContinue = true, lastIsSet = false;
   int K = 0;
+  positional = false;
   while (!done) {
     bool shouldComposite = true;
     topBit = stack.findTop(topBit);
@@ -376,12 +447,14 @@ __device__ __forceinline__ int layersOf(const RasterInputs& in, const ShapeStack
       next[K] = nx;
       front[K] = base;
       bitOf[K] = (nsolid && nbit >= 0) ? (nbit | kSolidLayer) : nbit;
+      positional = positional || (nbit >= 0 && !nsolid);
       ++K;
       base = composite(base, nx);
       if (base.w == 1.0f) done = true;
     }
   }
   color = base;
+  stopBit = topBit;
   return K;
 }
 
@@ -434,6 +507,7 @@ __device__ __forceinline__ void addY(float4* lg, int32_t src, float g) {
 __device__ __forceinline__ void chainEP(const EP& e, float gx, float gy, const float* pile, float2 d, float* gGeo) {
   if (gx == 0.0f && gy == 0.0f) return;
   if (e.kind == 0) {
+    if (e.pt < 0) return;  // a stand-in end point (never on a kept line)
     atomicAdd(&gGeo[e.pt], gx);
     atomicAdd(&gGeo[e.pt + 1], gy);
     return;
@@ -499,10 +573,38 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   int32_t srcY0 = kConst, srcY1 = kConst, srcX0 = kConst, srcX1 = kConst;
   const int px = c.deltaX;
   int py = c.deltaY;
+  // Section colours are memoised exactly as in the forward scan (the layers read
+  // from the top down to `colorStop` only); while they hold, the colour gradient of
+  // successive sections is linear in the same chain, so their areas are summed in
+  // `chainArea` and the chain runs once per layer list and pixel.
+  float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  bool colorOk = false, colorPositional = false;
+  int colorStop = 0, K = 0;
+  float chainArea = 0.0f;
+  float gI[3] = {0.0f, 0.0f, 0.0f}, I[3] = {0.0f, 0.0f, 0.0f}, A = 1.0f;
+  auto flushChain = [&]() {
+    if (grad && chainArea != 0.0f && K > 0) {
+      float4 d = make_float4(gI[0] * chainArea / A, gI[1] * chainArea / A, gI[2] * chainArea / A, 0.0f);
+      for (int k = K - 1; k >= 0; --k) {
+        float4 df, db;
+        compositeAdjoint(s.front[k], s.layer[k], d, df, db);
+        const int32_t lb = s.layerBit[k];
+        if (lb >= 0 && (lb & kSolidLayer)) {
+          float4& bg = s.bitGrad[lb & ~kSolidLayer];
+          bg.x += db.x;
+          bg.y += db.y;
+          bg.z += db.z;
+          bg.w += db.w;
+        }
+        d = df;
+      }
+    }
+    chainArea = 0.0f;
+  };
   for (float pixelY = 1.0f; pixelY <= c.floatHeight; pixelY += 1.0f) {
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, area = 0.0f;
+    if (colorPositional) colorOk = false;
     const size_t pix = (size_t)py * (size_t)in.bitmap_w + (size_t)px;
-    float gI[3] = {0.0f, 0.0f, 0.0f}, I[3] = {0.0f, 0.0f, 0.0f}, A = 1.0f;
     if (grad) {
       const float4 im = image[pix], tg = target[pix];
       I[0] = im.x;
@@ -641,12 +743,16 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       srcX0 = srcX1;
       sx1 = nextX;
       srcX1 = nextXSrc;
-      float4 col;
-      const int K = layersOf<SECTIONS>(in, stack, s.idx, px, py, bits, s.layer, s.front, s.layerBit, s.layerCap,
-                                       col, status);
-      if (K < 0) {
-        status |= kStatusIterLimit;
-        return;
+      if (!colorOk || stack.hiFlip >= colorStop) {
+        flushChain();
+        K = layersOf<SECTIONS>(in, stack, s.idx, px, py, bits, s.layer, s.front, s.layerBit, s.layerCap, col,
+                               colorPositional, colorStop, status);
+        if (K < 0) {
+          status |= kStatusIterLimit;
+          return;
+        }
+        colorOk = true;
+        stack.clearFlips();
       }
       const float a = (sx1 - sx0) * (sy1 - sy0);
       acc0 += col.x * a;
@@ -681,25 +787,12 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
         dy1 += 0.5f * dym;
         addY(s.lineGrad, srcY0, dy0);
         addY(s.lineGrad, srcY1, dy1);
-        // colour: back through the composite chain
-        float4 d = make_float4(gI[0] * a / A, gI[1] * a / A, gI[2] * a / A, 0.0f);
-        for (int k = K - 1; k >= 0; --k) {
-          float4 df, db;
-          compositeAdjoint(s.front[k], s.layer[k], d, df, db);
-          const int32_t lb = s.layerBit[k];
-          if (lb >= 0 && (lb & kSolidLayer)) {
-            float4& bg = s.bitGrad[lb & ~kSolidLayer];
-            bg.x += db.x;
-            bg.y += db.y;
-            bg.z += db.z;
-            bg.w += db.w;
-          }
-          d = df;
-        }
+        chainArea += a;  // colour: back through the composite chain at the next flush
       }
       if (current < numActive) stack.pass(q.hdr[q.start + current]);
       current += 1;
     }
+    flushChain();  // dL/dI changes with the pixel
     if (!grad) image[pix] = make_float4(acc0 / area, acc1 / area, acc2 / area, area);
     sx0 = kLeft;
     srcX0 = kConst;
@@ -778,8 +871,9 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
     uint32_t k = 0;
     if (lane == 0) k = atomicAdd(a.next_tile, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= a.n_tiles) break;
-    const int tile = (int)(a.order ? a.order[k] : k);
+    if (k >= a.n_units) break;
+    int tile, chunk;
+    unitOf(a.units, a.chunk_log2, k, tile, chunk);
     bool ok;
     RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
     if (!ok) continue;
@@ -791,7 +885,8 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
     // image and target of this tile's scene (float4 per pixel, same offsets as out)
     const size_t base = a.scenes ? (size_t)a.scenes[a.tile_scene[tile]].out_offset : 0;
     const int tpt = 1 << in.log2_tpt;
-    for (int column = lane; column < tpt; column += 32) {
+    const int column = chunk * 32 + lane;
+    if (column < tpt) {
       if (adjointColumn<SECTIONS>(in, ti, column, s, a.image + base, a.target + base, a.grad_geometry,
                                   a.grad_substances, status))
         status |= kStatusOverflow;

@@ -14,8 +14,9 @@ struct AdjointLaunch {
   const SceneInfo* scenes;
   const int32_t* tile_scene;
   uint32_t n_scenes;
-  const uint32_t* order;
-  uint32_t n_tiles;
+  const uint32_t* units;  // optional unit list, as for the raster fast pass
+  uint32_t n_units;
+  int chunk_log2;
   uint32_t* next_tile;
   int capacity;           // thresholds (and lines) per column
   float4* thr;            // slots * capacity

@@ -90,10 +90,12 @@ struct gudni_ctx {
   DevBuf<float> random_field;
   bool has_random = false;
   DevBuf<uint4> strand_table;
+  DevBuf<float2> strand_y;            // per strand: lowest and highest point y
   DevBuf<uint32_t> strand_first;
   size_t n_strands = 0;
   size_t n_units = 0;
   std::vector<uint4> h_strand_table;
+  std::vector<float2> h_strand_y;
   std::vector<uint32_t> h_strand_first;
 
   // per-job / per-frame staging
@@ -111,10 +113,12 @@ struct gudni_ctx {
   size_t batch_shapes = 0;
   size_t batch_scenes = 0;
   size_t batch_pixels = 0;
+  size_t batch_units = 0;
+  int batch_chunk_log2 = 0;           // largest over the batch's scenes
   DevBuf<gudni_shape> b_shapes;
   DevBuf<gudni_tile_info> b_tiles;
   DevBuf<int32_t> b_tile_scene;
-  DevBuf<uint32_t> b_order;
+  DevBuf<uint32_t> b_order;           // work units, cost-descending
   DevBuf<gudni::SceneInfo> b_scenes;
   DevBuf<uint32_t> b_out;
   cudaGraph_t graph = nullptr;
@@ -215,11 +219,11 @@ int ensure_scratch(gudni_ctx* ctx) {
   return GUDNI_OK;
 }
 
-// Scratch for the full-capacity pass: a fixed pool of slots (at most ~512 MB).
+// Scratch for the full-capacity pass: a fixed pool of slots (at most ~2 GB).
 int ensure_fallback_pool(gudni_ctx* ctx) {
   if (ctx->fallback_slots) return GUDNI_OK;
   const size_t per_slot = (size_t)ctx->spec.max_thresholds * 20 + (size_t)ctx->spec.max_shape * 4;
-  size_t slots = ((size_t)512 << 20) / per_slot;
+  size_t slots = ((size_t)2 << 30) / per_slot;
   slots = std::min<size_t>(slots, (size_t)ctx->grid * gudni::kRasterBlock);
   slots = std::max<size_t>(gudni::kRasterBlock, (slots / gudni::kRasterBlock) * gudni::kRasterBlock);
   cudaError_t e;
@@ -288,6 +292,7 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   in.tile_jobs = nullptr;
   in.counters = ctx->counters_on ? ctx->counters.ptr : nullptr;
   in.strand_table = ctx->n_strands ? ctx->strand_table.ptr : nullptr;
+  in.strand_y = ctx->n_strands ? ctx->strand_y.ptr : nullptr;
   in.n_strands = (uint32_t)ctx->n_strands;
   in.strand_first = ctx->strand_first.ptr;
   in.n_units = (uint32_t)ctx->n_units;
@@ -296,13 +301,15 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
 
 // Enqueue the fast pass over `n_tiles` tiles and the full-capacity pass over the
 // columns that overflowed it.  `max_tpt` is the largest threads-per-tile in the
-// launch (sizes the overflow list).
+// launch (sizes the overflow list).  Work units: the `units` list (n_units entries),
+// or without one every tile's 32-column chunks in tile order (chunk_log2 per tile).
 int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInfo* scenes,
-            const int32_t* tile_scene, size_t n_scenes, const uint32_t* order, size_t n_tiles, int max_tpt,
-            cudaStream_t stream) {
+            const int32_t* tile_scene, size_t n_scenes, const uint32_t* units, size_t n_units, int chunk_log2,
+            size_t n_tiles, int max_tpt, cudaStream_t stream) {
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
   if (n_tiles == 0) return GUDNI_OK;
+  if (!units) n_units = n_tiles << chunk_log2;
   const size_t max_items = n_tiles * (size_t)max_tpt;
   const bool need_fallback = ctx->working_capacity < ctx->spec.max_thresholds;
   cudaError_t e;
@@ -320,15 +327,16 @@ int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInf
   a.n_scenes = (uint32_t)n_scenes;
   a.scratch = gudni::ColumnScratch{ctx->thr.ptr, ctx->hdr.ptr, ctx->idx.ptr, ctx->working_capacity,
                                    ctx->spec.max_shape};
-  a.order = order;
-  a.n_tiles = (uint32_t)n_tiles;
+  a.units = units;
+  a.n_units = (uint32_t)n_units;
+  a.chunk_log2 = chunk_log2;
   a.next_tile = ctx->words.ptr + 1;
   a.overflow_items = need_fallback ? ctx->overflow_items.ptr : nullptr;
   a.overflow_cap = (uint32_t)std::min<size_t>(max_items, 0xFFFFFFFFull);
   a.overflow_count = ctx->words.ptr;
   a.status = ctx->status.ptr;
   const size_t warps_per_block = gudni::kRasterBlock / 32;
-  const int grid = (int)std::min<size_t>((n_tiles + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
+  const int grid = (int)std::min<size_t>((n_units + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
   if ((e = gudni::launch_raster(a, false, ctx->sections, grid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "raster launch");
   ctx->launches += 1;
@@ -412,6 +420,7 @@ int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes) {
   ctx->n_strands = 0;
   ctx->n_units = bytes / 16;
   ctx->h_strand_table.clear();
+  ctx->h_strand_y.clear();
   ctx->h_strand_first.assign(ctx->n_units, gudni::kNoStrand);
   size_t off = 0;
   while (off + 32 <= bytes) {
@@ -424,10 +433,31 @@ int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes) {
     std::memcpy(&lx, geo + off + 16, 4);
     if (off % 16 == 0) ctx->h_strand_first[off / 16] = (uint32_t)ctx->h_strand_table.size();
     ctx->h_strand_table.push_back(make_uint4((uint32_t)(off / 8), size, lx, rx));
+    // y range of every point of the strand (right end, left end and its control,
+    // then each tree node's point and control); NaN disables culling for the strand
+    float lo = INFINITY, hi = -INFINITY;
+    bool nan = false;
+    auto take = [&](size_t at) {
+      float y;
+      std::memcpy(&y, geo + off + at, 4);
+      if (y != y) nan = true;
+      lo = std::min(lo, y);
+      hi = std::max(hi, y);
+    };
+    take(12);
+    take(20);
+    take(28);
+    for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
+      take(node + 4);
+      take(node + 12);
+    }
+    ctx->h_strand_y.push_back(nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi));
     off += (size_t)size * 8;
   }
   int rc;
   if ((rc = upload(ctx, ctx->strand_table, ctx->h_strand_table.data(), ctx->h_strand_table.size(), "strand table")))
+    return rc;
+  if ((rc = upload(ctx, ctx->strand_y, ctx->h_strand_y.data(), ctx->h_strand_y.size(), "strand y ranges")))
     return rc;
   if ((rc = upload(ctx, ctx->strand_first, ctx->h_strand_first.data(), ctx->h_strand_first.size(), "strand map")))
     return rc;
@@ -481,12 +511,13 @@ int ensure_adjoint_scratch(gudni_ctx* ctx) {
 }
 
 int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInfo* scenes,
-                    const int32_t* tile_scene, size_t n_scenes, const uint32_t* order, size_t n_tiles,
-                    const float* target, float* image, float* grad_geometry, float* grad_substances,
-                    cudaStream_t stream) {
+                    const int32_t* tile_scene, size_t n_scenes, const uint32_t* units, size_t n_units,
+                    int chunk_log2, size_t n_tiles, const float* target, float* image, float* grad_geometry,
+                    float* grad_substances, cudaStream_t stream) {
   int rc = ensure_adjoint_scratch(ctx);
   if (rc) return rc;
   if (n_tiles == 0) return GUDNI_OK;
+  if (!units) n_units = n_tiles << chunk_log2;
   cudaError_t e = cudaMemsetAsync(ctx->words.ptr, 0, 2 * sizeof(uint32_t), stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
   gudni::AdjointLaunch a;
@@ -496,8 +527,9 @@ int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::
   a.scenes = scenes;
   a.tile_scene = tile_scene;
   a.n_scenes = (uint32_t)n_scenes;
-  a.order = order;
-  a.n_tiles = (uint32_t)n_tiles;
+  a.units = units;
+  a.n_units = (uint32_t)n_units;
+  a.chunk_log2 = chunk_log2;
   a.next_tile = ctx->words.ptr + 1;
   a.capacity = ctx->adj_capacity;
   a.thr = ctx->a_thr.ptr;
@@ -515,7 +547,7 @@ int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::
   a.grad_substances = grad_substances;
   a.status = ctx->status.ptr;
   const size_t warps_per_block = gudni::kAdjointBlock / 32;
-  const int grid = (int)std::min<size_t>((n_tiles + warps_per_block - 1) / warps_per_block, (size_t)ctx->adj_grid);
+  const int grid = (int)std::min<size_t>((n_units + warps_per_block - 1) / warps_per_block, (size_t)ctx->adj_grid);
   if ((e = gudni::launch_adjoint(a, ctx->sections, grid, stream)) != cudaSuccess)
     return cuda_fail(ctx, e, "adjoint launch");
   ctx->launches += 1;
@@ -563,7 +595,13 @@ gudni_ctx* gudni_create(const gudni_spec* spec, int device) {
   if ((e = gudni::raster_occupancy(ctx->sections, &ctx->blocks_per_sm)) != cudaSuccess || ctx->blocks_per_sm < 1)
     ctx->blocks_per_sm = 1;
   ctx->grid = ctx->sm_count * ctx->blocks_per_sm;
-  ctx->working_capacity = std::min(spec->max_thresholds, 256);
+  // fast-pass capacity: as much of max_thresholds as ~8 GB of slots allow (at most
+  // 4096); only columns that need more go through the full-capacity pass
+  {
+    const size_t slots = (size_t)ctx->grid * gudni::kRasterBlock;
+    const size_t budget = ((size_t)8 << 30) / (slots * (sizeof(float4) + 4));
+    ctx->working_capacity = (int)std::max<size_t>(64, std::min<size_t>({(size_t)spec->max_thresholds, budget, 4096}));
+  }
   if (const char* env = std::getenv("GUDNI_WORKING_CAPACITY")) {
     int v = std::atoi(env);
     if (v >= 4) ctx->working_capacity = std::min(spec->max_thresholds, v);
@@ -578,7 +616,7 @@ void gudni_destroy(gudni_ctx* ctx) {
   drop_graph(ctx);
   ctx->geometry.release(); ctx->substances.release(); ctx->pictures.release(); ctx->uses.release();
   ctx->radials.release(); ctx->random_field.release(); ctx->shapes.release(); ctx->tiles.release();
-  ctx->strand_table.release(); ctx->strand_first.release();
+  ctx->strand_table.release(); ctx->strand_y.release(); ctx->strand_first.release();
   ctx->tile_jobs.release(); ctx->out.release();
   ctx->b_shapes.release(); ctx->b_tiles.release(); ctx->b_tile_scene.release(); ctx->b_order.release();
   ctx->b_scenes.release(); ctx->b_out.release();
@@ -632,7 +670,8 @@ int gudni_raster_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes,
   if ((rc = upload(ctx, ctx->out, out, pixels, "bitmap upload"))) return rc;
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, n_shapes, ctx->tiles.ptr, n_tiles, bitmap_w, bitmap_h,
                                   compute_depth, job_index, background, ctx->out.ptr);
-  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, ctx->stream)))
+  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, 0, gudni::chunkLog2(compute_depth), n_tiles,
+                    ctx->spec.threads_per_tile, ctx->stream)))
     return rc;
   cudaError_t e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
@@ -655,7 +694,8 @@ int gudni_raster_job_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_
   ctx->last_stream = s;
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth,
                                   job_index, background, out);
-  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, s);
+  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, 0, gudni::chunkLog2(compute_depth), n_tiles,
+                 ctx->spec.threads_per_tile, s);
 }
 
 int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs, int32_t bitmap_w,
@@ -694,8 +734,8 @@ int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs
   gudni::RasterInputs in = inputs(ctx, ctx->shapes.ptr, ctx->h_shapes.size(), ctx->tiles.ptr, ctx->h_tiles.size(),
                                   bitmap_w, bitmap_h, compute_depth, 0, background, ctx->out.ptr);
   in.tile_jobs = ctx->tile_jobs.ptr;
-  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, ctx->h_tiles.size(), ctx->spec.threads_per_tile,
-                    ctx->stream)))
+  if ((rc = enqueue(ctx, in, nullptr, nullptr, 0, nullptr, 0, gudni::chunkLog2(compute_depth), ctx->h_tiles.size(),
+                    ctx->spec.threads_per_tile, ctx->stream)))
     return rc;
   e = cudaMemcpyAsync(out, ctx->out.ptr, pixels * 4, cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "bitmap read-back");
@@ -719,7 +759,8 @@ int gudni_raster_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t 
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, 0,
                                   background, out);
   in.tile_jobs = tile_jobs;
-  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, ctx->spec.threads_per_tile, s);
+  return enqueue(ctx, in, nullptr, nullptr, 0, nullptr, 0, gudni::chunkLog2(compute_depth), n_tiles,
+                 ctx->spec.threads_per_tile, s);
 }
 
 int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
@@ -755,12 +796,26 @@ int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   for (size_t t = 0; t < n_tiles; ++t)
     if (tile_scene[t] < 0 || (size_t)tile_scene[t] >= n_scenes)
       return fail(ctx, GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(t) + " names no scene");
-  // schedule: most expensive tiles first (longest-processing-time order)
-  std::vector<uint32_t> order(n_tiles);
-  std::iota(order.begin(), order.end(), 0u);
+  // work units: every tile's 32-column chunks; scheduled most expensive first
+  // (longest-processing-time order, a tile's cost shared by its chunks)
+  std::vector<uint32_t> order;
+  std::vector<float> unit_cost;
+  int chunk_log2_max = 0;
+  for (size_t t = 0; t < n_tiles; ++t) {
+    const int cl = gudni::chunkLog2(scenes[tile_scene[t]].compute_depth);
+    chunk_log2_max = std::max(chunk_log2_max, cl);
+    for (int c = 0; c < (1 << cl); ++c) {
+      order.push_back(((uint32_t)t << gudni::kChunkBits) | (uint32_t)c);
+      unit_cost.push_back(tile_cost ? tile_cost[t] / (float)(1 << cl) : 0.0f);
+    }
+  }
   if (tile_cost) {
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t b) { return tile_cost[a] > tile_cost[b]; });
+    std::vector<uint32_t> idx(order.size());
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return unit_cost[a] > unit_cost[b]; });
+    std::vector<uint32_t> sorted(order.size());
+    for (size_t i = 0; i < idx.size(); ++i) sorted[i] = order[idx[i]];
+    order.swap(sorted);
   }
   if ((rc = upload_common_buffers(ctx, geometry, geometry_bytes, substances, n_substances, pictures, picture_bytes,
                                   picture_uses, n_picture_uses, radials, n_radials, nullptr)))
@@ -768,7 +823,7 @@ int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   if ((rc = upload(ctx, ctx->b_shapes, shapes, n_shapes, "batch shapes"))) return rc;
   if ((rc = upload(ctx, ctx->b_tiles, tiles, n_tiles, "batch tiles"))) return rc;
   if ((rc = upload(ctx, ctx->b_tile_scene, tile_scene, n_tiles, "batch tile scenes"))) return rc;
-  if ((rc = upload(ctx, ctx->b_order, order.data(), n_tiles, "batch order"))) return rc;
+  if ((rc = upload(ctx, ctx->b_order, order.data(), order.size(), "batch work units"))) return rc;
   if ((rc = upload(ctx, ctx->b_scenes, sc.data(), n_scenes, "batch scenes"))) return rc;
   cudaError_t e = ctx->b_out.reserve(out_pixels);
   if (e == cudaSuccess) e = cudaMemsetAsync(ctx->b_out.ptr, 0, out_pixels * 4, ctx->stream);
@@ -784,6 +839,8 @@ int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   ctx->batch_shapes = n_shapes;
   ctx->batch_scenes = n_scenes;
   ctx->batch_pixels = out_pixels;
+  ctx->batch_units = order.size();
+  ctx->batch_chunk_log2 = chunk_log2_max;
   ctx->batch_ready = true;
   return GUDNI_OK;
 }
@@ -794,7 +851,7 @@ static int batch_enqueue(gudni_ctx* ctx, cudaStream_t s) {
   int max_tpt = 1 << gudni::kMaxLog2Tpt;
   if (ctx->overflow_items.cap && ctx->batch_tiles) max_tpt = (int)std::min<size_t>(max_tpt, ctx->overflow_items.cap / ctx->batch_tiles);
   return enqueue(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr, ctx->batch_scenes, ctx->b_order.ptr,
-                 ctx->batch_tiles, max_tpt, s);
+                 ctx->batch_units, 0, ctx->batch_tiles, max_tpt, s);
 }
 
 int gudni_batch_render(gudni_ctx* ctx, int use_graph, void* stream) {
@@ -842,8 +899,9 @@ int gudni_batch_render_tiles(gudni_ctx* ctx, size_t first_tile, size_t n_tiles, 
                                   1, 1, 0, 0, nullptr, ctx->b_out.ptr);
   int max_tpt = 1 << gudni::kMaxLog2Tpt;
   if (ctx->overflow_items.cap && ctx->batch_tiles) max_tpt = (int)std::min<size_t>(max_tpt, ctx->overflow_items.cap / ctx->batch_tiles);
-  return enqueue(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr + first_tile, ctx->batch_scenes, nullptr,
-                 n_tiles, max_tpt, s);
+  // chunks of the batch's widest scene: units past a tile's own columns do nothing
+  return enqueue(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr + first_tile, ctx->batch_scenes, nullptr, 0,
+                 ctx->batch_chunk_log2, n_tiles, max_tpt, s);
 }
 
 const uint32_t* gudni_batch_output(const gudni_ctx* ctx) { return ctx ? ctx->b_out.ptr : nullptr; }
@@ -921,8 +979,8 @@ int gudni_adjoint_tiles_device(gudni_ctx* ctx, const gudni_shape* shapes, size_t
   gudni::RasterInputs in = inputs(ctx, shapes, n_shapes, tiles, n_tiles, bitmap_w, bitmap_h, compute_depth, 0,
                                   background, nullptr);
   in.tile_jobs = tile_jobs;
-  return enqueue_adjoint(ctx, in, nullptr, nullptr, 0, nullptr, n_tiles, target, image, grad_geometry,
-                         grad_substances, s);
+  return enqueue_adjoint(ctx, in, nullptr, nullptr, 0, nullptr, 0, gudni::chunkLog2(compute_depth), n_tiles,
+                         target, image, grad_geometry, grad_substances, s);
 }
 
 int gudni_batch_adjoint(gudni_ctx* ctx, const float* target, float* image, float* grad_geometry,
@@ -937,7 +995,7 @@ int gudni_batch_adjoint(gudni_ctx* ctx, const float* target, float* image, float
   gudni::RasterInputs in = inputs(ctx, ctx->b_shapes.ptr, ctx->batch_shapes, ctx->b_tiles.ptr, ctx->batch_tiles, 1,
                                   1, 0, 0, nullptr, nullptr);
   return enqueue_adjoint(ctx, in, ctx->b_scenes.ptr, ctx->b_tile_scene.ptr, ctx->batch_scenes, ctx->b_order.ptr,
-                         ctx->batch_tiles, target, image, grad_geometry, grad_substances, s);
+                         ctx->batch_units, 0, ctx->batch_tiles, target, image, grad_geometry, grad_substances, s);
 }
 
 }  // extern "C"

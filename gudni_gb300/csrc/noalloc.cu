@@ -170,11 +170,12 @@ extern "C" int gudni_raster_job_noalloc(const gudni_spec* spec, const void* geom
     in.max_shape = spec->max_shape;
     in.out = out;
     a.scratch = gudni::ColumnScratch{thr, hdr, idx, capacity, spec->max_shape};
-    a.n_tiles = (uint32_t)n_tiles;
+    a.chunk_log2 = gudni::chunkLog2(compute_depth);
+    a.n_units = (uint32_t)(n_tiles << a.chunk_log2);
     a.next_tile = next_tile;
     a.status = status;
     const size_t warps_per_block = gudni::kRasterBlock / 32;
-    size_t grid = (n_tiles + warps_per_block - 1) / warps_per_block;
+    size_t grid = ((size_t)a.n_units + warps_per_block - 1) / warps_per_block;
     if (grid > slots / gudni::kRasterBlock) grid = slots / gudni::kRasterBlock;
     if ((e = gudni::launch_raster(a, false, gudni::sections_for(spec->max_shape), (int)grid, s)) != cudaSuccess)
       return fail(GUDNI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

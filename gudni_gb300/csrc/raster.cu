@@ -6,13 +6,14 @@
 // thread runs a whole column start to finish (raster_device.cuh), and two kernels
 // schedule the columns:
 //
-// raster_tiles_kernel -- the fast pass.  A persistent grid of warps pulls tiles from
-//   a work counter (one atomicAdd per tile, lane 0), optionally in a cost-descending
-//   order, and runs the tile's columns on its lanes (32 consecutive columns at a time:
-//   the lanes walk the same strands and write one row segment per pixel row).  Tiles
-//   may belong to different scenes of a batch, each with its own canvas, output,
-//   background and threads per tile.  Every thread owns a scratch slot (a queue of
-//   `capacity` entries and the shape-index table of its column).
+// raster_tiles_kernel -- the fast pass.  A persistent grid of warps pulls work units
+//   -- 32 consecutive columns of one tile -- from a work counter (one atomicAdd per
+//   unit, lane 0), optionally from a cost-descending unit list, and runs the unit's
+//   columns on its lanes (the lanes walk the same strands and write one row segment
+//   per pixel row).  A tile of more than 32 columns is spread over several warps.
+//   Tiles may belong to different scenes of a batch, each with its own canvas,
+//   output, background and threads per tile.  Every thread owns a scratch slot (a
+//   queue of `capacity` entries and the shape-index table of its column).
 //
 // raster_list_kernel -- the full-capacity pass.  Columns that overflowed the fast
 //   pass's small working capacity were appended to a list; this kernel, launched
@@ -62,8 +63,9 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a
     uint32_t k = 0;
     if (lane == 0) k = atomicAdd(a.next_tile, 1u);
     k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= a.n_tiles) break;
-    const int tile = (int)(a.order ? a.order[k] : k);
+    if (k >= a.n_units) break;
+    int tile, chunk;
+    unitOf(a.units, a.chunk_log2, k, tile, chunk);
     bool ok;
     const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
     if (!ok) continue;
@@ -73,7 +75,8 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a
       continue;
     }
     const int tpt = 1 << in.log2_tpt;
-    for (int column = lane; column < tpt; column += 32) {
+    const int column = chunk * 32 + lane;
+    if (column < tpt) {
       if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) {
         if (a.overflow_items) {
           const uint32_t n = atomicAdd(a.overflow_count, 1u);

@@ -76,6 +76,7 @@ struct RasterInputs {
   int64_t* counters;             // optional work counters (see gudni_enable_counters)
   // Strand table of the geometry pile (optional; see StrandEntry).
   const uint4* strand_table;     // one entry per strand
+  const float2* strand_y;        // per strand: lowest and highest point y (absolute)
   uint32_t n_strands;
   const uint32_t* strand_first;  // per 16-byte unit of the pile: strand index starting there
   uint32_t n_units;              // geometry_bytes / 16
@@ -173,27 +174,67 @@ struct Queue {
   }
 };
 
+// The shape stack (ShapeState's shapeBits, K:270-292): one bit per shape of the
+// column, 64 per word.  `nz` marks the non-zero words, so findTop skips empty words
+// with one bit scan instead of a word-by-word walk (the reference walks the words;
+// the bit it finds is the same).  `hiFlip` is the highest bit flipped since the last
+// clearFlips(): the render scan uses it to tell whether a cached section colour
+// still holds.
 template <int SECTIONS>
 struct ShapeStack {
+  static_assert(SECTIONS >= 1 && SECTIONS <= 32, "at most 32 stack words");
   uint64_t w[SECTIONS];
+  uint32_t nz;
+  int hiFlip;
   __device__ __forceinline__ void clear() {
 #pragma unroll
     for (int i = 0; i < SECTIONS; ++i) w[i] = 0ull;
+    nz = 0u;
+    hiFlip = -1;
   }
-  __device__ __forceinline__ void flip(uint32_t bit) { w[bit >> 6] ^= (1ull << (bit & 63)); }
+  __device__ __forceinline__ void clearFlips() { hiFlip = -1; }
+  __device__ __forceinline__ void flip(uint32_t bit) {
+    const int sec = (int)(bit >> 6);
+    const uint64_t m = 1ull << (bit & 63);
+    hiFlip = max(hiFlip, (int)bit);
+    if (SECTIONS <= 8) {
+      // select form: every word stays in a register
+#pragma unroll
+      for (int i = 0; i < SECTIONS; ++i) {
+        if (i == sec) {
+          w[i] ^= m;
+          nz = w[i] ? (nz | (1u << i)) : (nz & ~(1u << i));
+        }
+      }
+    } else {
+      w[sec] ^= m;
+      nz = w[sec] ? (nz | (1u << sec)) : (nz & ~(1u << sec));
+    }
+  }
+  __device__ __forceinline__ uint64_t word(int sec) const {
+    if (SECTIONS <= 8) {
+      uint64_t r = 0ull;
+#pragma unroll
+      for (int i = 0; i < SECTIONS; ++i) r = (i == sec) ? w[i] : r;
+      return r;
+    }
+    return w[sec];
+  }
   __device__ __forceinline__ void pass(uint32_t h) { flip(h & kShapeBitMask); }
   __device__ __forceinline__ void passTop(uint32_t h) { if (hPersistTop(h)) pass(h); }
   __device__ __forceinline__ void passBottom(uint32_t h) { if (hPersistBottom(h)) pass(h); }
-  // findTop K:281-292
+  // findTop K:281-292: the highest set bit below `ignoreAbove`, or -1
   __device__ __forceinline__ int findTop(int ignoreAbove) const {
     int sec = ignoreAbove >> 6;
-    int bits = ignoreAbove & 63;
-    uint64_t s = (~(~0ull << bits)) & w[sec];
-    while (s == 0ull && sec > 0) {
-      sec -= 1;
-      s = w[sec];
+    const int bits = ignoreAbove & 63;
+    uint64_t s = (~(~0ull << bits)) & word(sec);
+    if (s == 0ull) {
+      const uint32_t below = nz & ((1u << sec) - 1u);
+      if (below == 0u) return -1;
+      sec = 31 - __clz((int)below);
+      s = word(sec);
     }
-    return (sec << 6) + (64 - __clzll((long long)s)) - 1;
+    return (sec << 6) + (63 - __clzll((long long)s));
   }
 };
 
@@ -305,16 +346,19 @@ __device__ __forceinline__ void addLineSegment(GenState& g, float2 left, float2 
   }
 }
 
-// spawnThresholds K:1264-1333
+// spawnThresholds K:1264-1333.  `above`: the whole strand lies at least a pixel above
+// the column, so every line it spawns ends above the column top and only the
+// enclosure flag (set by any persistent line, whatever its y) can change; the border
+// intercepts are then not computed (any value above the column gives the same flags).
 __device__ __forceinline__ void spawnThresholds(GenState& g, uint32_t shapeBit, Trav& l, Trav& r, bool& added,
-                                                bool& enclosed, int& status) {
-  float yL = (l.left.x >= kLeft) ? l.left.y : intersectCurve(l, status);
+                                                bool& enclosed, int& status, bool above = false) {
+  float yL = (l.left.x >= kLeft) ? l.left.y : (above ? -1.0f : intersectCurve(l, status));
   bool leftWing = false;
   if ((l.right.x < kRight) && (l.right.x > kLeft)) {
     addLineSegment(g, make_float2(l.xPos, yL), l.right, shapeBit, added, enclosed);
     leftWing = true;
   }
-  float yR = (r.right.x <= kRight) ? r.right.y : intersectCurve(r, status);
+  float yR = (r.right.x <= kRight) ? r.right.y : (above ? -1.0f : intersectCurve(r, status));
   bool rightWing = false;
   if ((r.left.x > kLeft) && (r.left.x < kRight) && (l.index != r.index)) {
     addLineSegment(g, r.left, make_float2(r.xPos, yR), shapeBit, added, enclosed);
@@ -347,7 +391,7 @@ __device__ __forceinline__ void searchTree(Trav& t, const float4* tree, int tree
 // traverseTree K:1378-1408 + spawnThresholds for one strand of `size` 8-byte units.
 __device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* strand, uint32_t size, float2 d,
                                                  uint32_t shapeBit, bool& added, bool& enclosedByStrand,
-                                                 int& status) {
+                                                 int& status, bool above = false) {
   const int treeSize = ((int)size - 4) / 2;
   const float2 rp = *reinterpret_cast<const float2*>(strand + 8);
   const float4 lc = *reinterpret_cast<const float4*>(strand + 16);
@@ -364,7 +408,7 @@ __device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* str
     const float4* tree = reinterpret_cast<const float4*>(strand + 32);
     searchTree(l, tree, treeSize, d, true);
     searchTree(r, tree, treeSize, d, false);
-    spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status);
+    spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status, above);
   }
 }
 
@@ -393,8 +437,17 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
         const float lx = __uint_as_float(e.z) - d.x;
         const float rx = __uint_as_float(e.w) - d.x;
         if (!(lx <= kRight && rx > kLeft)) continue;
+        // y culling with a one-pixel margin (every point a line can end on lies within
+        // the strand's points' y range up to rounding): a strand wholly below the
+        // column spawns only lines whose top is at or below its bottom, which are
+        // dropped and leave the enclosure unchanged; one wholly above needs no
+        // intercepts (spawnThresholds, `above`).
+        const float2 yr = in.strand_y[first + k];
+        if (yr.x - d.y >= c.floatHeight + 1.0f) continue;
+        const bool above = yr.y - d.y <= -1.0f;
         bool enclosedByStrand = false;
-        strandThresholds(g, in.geometry + (size_t)e.x * 8, e.y, d, shapeBits, added, enclosedByStrand, status);
+        strandThresholds(g, in.geometry + (size_t)e.x * 8, e.y, d, shapeBits, added, enclosedByStrand, status,
+                         above);
         if (q.overflow) return shapeBits;
         enclosedByShape = enclosedByShape != enclosedByStrand;
       }
@@ -563,10 +616,14 @@ __device__ __forceinline__ bool lastIsSetFor(uint64_t comp) {
 }
 
 // determineColor K:1447-1513
+//
+// `stopBit` receives the lowest bit position the walk read: the colour is a function
+// of the stack bits at and above it only (below it the walk had reached an opaque
+// composite and stopped), or of every bit (-1) when it reached the background.
 template <int SECTIONS>
 __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
                                                  const uint32_t* shapeIdx, int px, int py, int& status,
-                                                 int64_t& texels, int topStart, bool& positional) {
+                                                 int64_t& texels, int topStart, bool& positional, int& stopBit) {
   // The reference starts at MAXSHAPE (K:1453); no bit at or above the column's
   // assigned shape-bit count is ever set, so starting there finds the same bits.
   int topBit = topStart;
@@ -612,50 +669,9 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
       if (base.w == 1.0f) done = true;
     }
   }
+  stopBit = topBit;
   return base;
 }
-
-// Memo of determineColor.  The section colour is a pure function of the shape-stack
-// bits and, when a picture or gradient layer was composited, of the pixel position
-// (the column fixes x, so the row y).  The same stack states recur from section to
-// section (every vertical slice restarts from the left-border state, interior pixels
-// repeat the previous pixel's state), so a few entries keyed by the full stack words
-// serve most sections.  Lookups compare every word: results are exactly those of a
-// fresh determineColor.
-template <int SECTIONS>
-struct ColorCache {
-  static constexpr int N = 4;
-  uint64_t key[N][SECTIONS];
-  int row[N];      // -1: colour independent of position; else the pixel row it holds for
-  float4 color[N];
-  int next;
-  __device__ __forceinline__ void clear() {
-#pragma unroll
-    for (int e = 0; e < N; ++e) row[e] = -2;  // -2: empty
-    next = 0;
-  }
-  __device__ __forceinline__ bool find(const ShapeStack<SECTIONS>& st, int py, float4& out) const {
-#pragma unroll
-    for (int e = 0; e < N; ++e) {
-      bool same = row[e] != -2 && (row[e] == -1 || row[e] == py);
-#pragma unroll
-      for (int w = 0; w < SECTIONS; ++w) same = same && key[e][w] == st.w[w];
-      if (same) {
-        out = color[e];
-        return true;
-      }
-    }
-    return false;
-  }
-  __device__ __forceinline__ void put(const ShapeStack<SECTIONS>& st, int py, bool positional, float4 c) {
-    const int e = next;
-    next = (next + 1) & (N - 1);
-#pragma unroll
-    for (int w = 0; w < SECTIONS; ++w) key[e][w] = st.w[w];
-    row[e] = positional ? py : -1;
-    color[e] = c;
-  }
-};
 
 struct Parse {
   int current, numActive;
@@ -782,9 +798,16 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   uint32_t* outp = in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
   int64_t sections = 0;
   int64_t texels = 0;
-  ColorCache<SECTIONS> cache;
-  cache.clear();
+  // Section-colour memo, exact: determineColor reads the stack bits from the top
+  // down to `colorStop` and nothing below, so its result holds until a bit at or
+  // above colorStop flips (stack.hiFlip), or, when a picture or gradient layer was
+  // composited, until the pixel row changes.
+  float4 color = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  bool colorOk = false;
+  bool colorPositional = false;
+  int colorStop = 0;
   for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
+    if (colorPositional) colorOk = false;
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
     int guard = 0;
     while ((p.sEndX < kRight) || (p.sEndY < p.pixelY)) {
@@ -805,11 +828,10 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       }
       p.sStartX = p.sEndX;
       p.sEndX = nextX;
-      float4 color;
-      if (!cache.find(stack, py, color)) {
-        bool positional;
-        color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, positional);
-        cache.put(stack, py, positional, color);
+      if (!colorOk || stack.hiFlip >= colorStop) {
+        color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, colorPositional, colorStop);
+        colorOk = true;
+        stack.clearFlips();
       }
       float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
       if (in.stochastic != 0.0f) {  // getRandom K:1608-1613

@@ -10,6 +10,7 @@ namespace gudni {
 constexpr int kRasterBlock = 128;
 constexpr int kColumnBits = 11;   // overflow-list items are (tile << 11) | column
 constexpr int kMaxLog2Tpt = 10;   // up to 1024 threads per tile
+constexpr int kChunkBits = 5;     // work units are (tile << 5) | chunk of 32 columns
 
 struct ColumnScratch {
   float4* thr;       // slots * capacity threshold geometries
@@ -34,9 +35,10 @@ struct TileLaunch {
   const int32_t* tile_scene;    // scene of each tile (with scenes)
   uint32_t n_scenes;
   ColumnScratch scratch;
-  // fast pass
-  const uint32_t* order;        // optional tile order (cost-descending)
-  uint32_t n_tiles;
+  // fast pass: work units of 32 columns of one tile, pulled from a counter
+  const uint32_t* units;        // optional unit list ((tile << kChunkBits) | chunk), cost-descending
+  uint32_t n_units;             // units in the launch
+  int chunk_log2;               // without a list: unit k is tile k >> chunk_log2, chunk k & mask
   uint32_t* next_tile;          // work counter, zero at launch
   uint32_t* overflow_items;     // where columns that overflow `capacity` go
   uint32_t overflow_cap;
@@ -47,6 +49,21 @@ struct TileLaunch {
   uint32_t list_cap;
   int* status;                  // kStatus* bits
 };
+
+// Work unit k of a launch: its tile and its chunk of 32 columns.
+__device__ __forceinline__ void unitOf(const uint32_t* units, int chunk_log2, uint32_t k, int& tile, int& chunk) {
+  if (units) {
+    const uint32_t u = units[k];
+    tile = (int)(u >> kChunkBits);
+    chunk = (int)(u & ((1u << kChunkBits) - 1u));
+  } else {
+    tile = (int)(k >> chunk_log2);
+    chunk = (int)(k & ((1u << chunk_log2) - 1u));
+  }
+}
+
+// log2 of the 32-column chunks of a tile with 2^log2_tpt columns
+__host__ __device__ __forceinline__ int chunkLog2(int log2_tpt) { return log2_tpt > 5 ? log2_tpt - 5 : 0; }
 
 __device__ __forceinline__ bool tileOk(const gudni_tile_info& ti, uint32_t n_shapes) {
   return ti.hdepth >= 0 && ti.hdepth <= 24 && ti.vdepth >= 0 && ti.vdepth <= 24 && ti.left >= 0 &&
