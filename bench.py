@@ -51,7 +51,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="page4k", choices=sorted(WORKLOADS))
     ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--tile", type=int, default=None, help="tile size (default: the workload's)")
+    ap.add_argument("--threads-per-tile", type=int, default=None, help="threads per tile (default: the workload's)")
     return ap.parse_args()
+
+
+def tile_override(args, tile, tpt):
+    """The workload's (tile size, threads per tile) unless given on the command line."""
+    return (args.tile or tile), (args.threads_per_tile or tpt)
 
 
 WORKLOADS = {
@@ -69,14 +76,14 @@ WORKLOADS = {
 }
 
 
-def make_frame(workload: str = "page4k", baked: bool = False):
+def make_frame(workload: str = "page4k", baked: bool = False, tile: int = 32, tpt: int = 32):
     """The workload's serialized frame.  baked=True expresses each radial gradient as
     a picture (scene.bake_radials), the form the reference kernels can render."""
     from gudni_gb300 import lib as L
     from gudni_gb300 import scene as S
     from gudni_gb300 import scenes as G
 
-    spec = L.make_spec(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+    spec = L.make_spec(max_tile_size=tile, threads_per_tile=tpt, max_thresholds=4096, max_shape=127,
                        stack_sections=8)
     flat = G.glyph_page(seed=1) if workload == "page4k" else G.random_shapes(seed=0)
     if baked:
@@ -94,7 +101,8 @@ def reference_runner(workload: str, frame):
     fn, kind, img = (lambda: O.render_frame(frame)), "port", want  # noqa: E731
     if O.ref_available(frame.spec.max_shape, frame.spec.stack_sections):
         try:
-            ref_frame = make_frame(workload, baked=True) if len(frame.radials) else frame
+            ref_frame = (make_frame(workload, baked=True, tile=frame.spec.max_tile_size,
+                                    tpt=frame.spec.threads_per_tile) if len(frame.radials) else frame)
             st = {}
             O.render_frame(ref_frame, stats=st)
             cap = int(st["max_queue"]) + 16  # the reference writes past a full slab
@@ -243,7 +251,7 @@ def run_reference(args):
         print(json.dumps({"impl": "reference", "unavailable": f"workload {args.workload} has no reference "
                           "counterpart (the reference renders one scene per call and has no adjoint)"}))
         return 0
-    frame = make_frame(args.workload)
+    frame = make_frame(args.workload, False, *tile_override(args, 32, 32))
     fn, kind, img, want = reference_runner(args.workload, frame)
     for _ in range(args.warmup):
         fn()
@@ -290,7 +298,7 @@ def run_batch(args):
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
     choice = A.autotune(flats, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE, samples=1, reps=2,
-                        candidates=((16, 32), (32, 32), (32, 64), (32, 128)))
+                        log=lambda m: print(m, file=sys.stderr, flush=True))
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     frames = A.serialize_tuned(flats, choice, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
@@ -392,7 +400,9 @@ def run_adjoint(args):
     from gudni_gb300.raster import Rasterizer
 
     torch.cuda.set_device(0)
-    spec = L.make_spec(**ADJ_SPEC)
+    tile, tpt = tile_override(args, ADJ_SPEC["max_tile_size"], ADJ_SPEC["threads_per_tile"])
+    adj_spec = dict(ADJ_SPEC, max_tile_size=tile, threads_per_tile=tpt)
+    spec = L.make_spec(**adj_spec)
     frame = S.serialize_flat(adjoint_scene(), spec)
     tframe = S.serialize_flat(adjoint_scene(4.0), spec)
     dev = torch.device("cuda", 0)
@@ -476,7 +486,7 @@ def run_adjoint(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS["adjoint1024"][0], "canvas": [1024, 1024], "shapes": 500,
                        "segments": 16, "target": "same scene, control points jittered N(0, 4 px)",
-                       "tiles": int(frame.n_tiles), **ADJ_SPEC, "l2": "flushed between steps (256 MB write)",
+                       "tiles": int(frame.n_tiles), **adj_spec, "l2": "flushed between steps (256 MB write)",
                        "data": "synthetic, seeded"},
             "forward_ms": fwd_ms, "fwd_adjoint_ms": adj_ms, "fwd_adjoint_over_forward": adj_ms / fwd_ms,
             "gpu_launches": int(launches), "clocks": clocks.summary(), "gradient_check": check}
@@ -509,7 +519,7 @@ def main():
     from gudni_gb300 import scene as S
     from gudni_gb300.raster import Rasterizer
 
-    frame = make_frame(args.workload)
+    frame = make_frame(args.workload, False, *tile_override(args, 32, 32))
     shapes, tiles, tile_jobs = S.concatenated_piles(frame)
     r = Rasterizer(frame.spec, device=local)
     r.upload_common(frame)

@@ -16,8 +16,10 @@ from . import batch as B
 from . import lib as L
 from . import scene as S
 
-# (tile size, threads per tile); threads per tile must be >= tile size
-CANDIDATES: Tuple[Tuple[int, int], ...] = ((16, 16), (16, 32), (32, 32), (32, 64), (32, 128), (64, 64))
+# (tile size, threads per tile); threads per tile must be >= tile size.  More threads
+# per tile make shorter columns (more parallel work, more threshold generation);
+# smaller tiles give each column fewer shapes.
+CANDIDATES: Tuple[Tuple[int, int], ...] = ((8, 32), (16, 64), (16, 256), (32, 32), (32, 256))
 BUCKETS: Tuple[int, ...] = (96, 192, 384, 768, 1 << 30)  # upper bound of max(canvas side)
 
 
@@ -34,11 +36,18 @@ def spec_for(tile: int, tpt: int, max_shape: int, max_thresholds: int, strands_p
                        max_shape=max_shape, max_strands_per_tile=strands_per_tile)
 
 
+def scene_cost(f: S.FlatScene) -> float:
+    """A rough work estimate: pixels x shapes."""
+    return float(f.canvas_w) * float(f.canvas_h) * float(len(f.substance_kind))
+
+
 def autotune(flats: Sequence[S.FlatScene], max_shape: int, max_thresholds: int, strands_per_tile: int,
              samples: int = 2, reps: int = 3, candidates=CANDIDATES, device: int = 0,
              log=None) -> Dict[int, Tuple[int, int]]:
     """Return {bucket: (tile, threads_per_tile)}.  Each candidate renders the bucket's
-    sample scenes as one batch; the fastest mean over `reps` replays wins."""
+    sample scenes (its most expensive and, with samples > 1, its median scene by
+    scene_cost) as one batch; the fastest mean over `reps` replays wins.  A candidate
+    whose first render is over three times the best so far is not replayed."""
     by_bucket: Dict[int, List[S.FlatScene]] = {}
     for f in flats:
         by_bucket.setdefault(bucket_of(f.canvas_w, f.canvas_h), []).append(f)
@@ -46,19 +55,23 @@ def autotune(flats: Sequence[S.FlatScene], max_shape: int, max_thresholds: int, 
     base = spec_for(32, 32, max_shape, max_thresholds, strands_per_tile)
     with B.BatchRasterizer(base, device) as r:
         for b, members in sorted(by_bucket.items()):
-            picks = members[:samples]
+            ranked = sorted(members, key=scene_cost)
+            picks = [ranked[-1]] + ([ranked[len(ranked) // 2]] if samples > 1 and len(ranked) > 1 else [])
             best = None
             for tile, tpt in candidates:
                 spec = spec_for(tile, tpt, max_shape, max_thresholds, strands_per_tile)
                 batch = B.build_batch([S.serialize_flat(f, spec) for f in picks])
                 r.upload(batch)
+                t0 = time.perf_counter()
                 r.render(use_graph=False)
                 r.sync_status()
-                t0 = time.perf_counter()
-                for _ in range(reps):
-                    r.render(use_graph=False)
-                r.sync_status()
-                dt = (time.perf_counter() - t0) / reps
+                dt = time.perf_counter() - t0
+                if best is None or dt < 3.0 * best[0]:
+                    t0 = time.perf_counter()
+                    for _ in range(reps):
+                        r.render(use_graph=False)
+                    r.sync_status()
+                    dt = (time.perf_counter() - t0) / reps
                 if log:
                     log(f"bucket {b} tile {tile} tpt {tpt}: {dt * 1e3:.3f} ms")
                 if best is None or dt < best[0]:

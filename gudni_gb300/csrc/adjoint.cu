@@ -327,7 +327,15 @@ __device__ __forceinline__ void strandP(const RasterInputs& in, AdjGen& g, size_
     const int treeSize = ((int)size - 4) / 2;
     searchP(l, tree, sb + 8, treeSize, d, true);
     searchP(r, tree, sb + 8, treeSize, d, false);
-    spawnP(g, bits, l, r, added, encStrand, status, above);
+    // the same hull culling as the forward generation (strandThresholds)
+    const float lo = fminf(fminf(fminf(l.left.y, l.control.y), fminf(l.right.y, r.left.y)),
+                           fminf(r.control.y, r.right.y));
+    const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
+                           fmaxf(r.control.y, r.right.y));
+    const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
+    const bool ordered = sum == sum;
+    if (ordered && lo >= g.c->floatHeight + 1.0f) return;
+    spawnP(g, bits, l, r, added, encStrand, status, above || (ordered && hi <= -1.0f));
   }
 }
 
@@ -821,7 +829,15 @@ __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti,
       for (int i = 0; i < n_lines; ++i) s.lineGrad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       for (uint32_t b = 0; b < bits; ++b) s.bitGrad[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
-    scanP<SECTIONS>(in, c, q, s, stack, (int)bits, image, target, pass == 1, status);
+    if (SECTIONS > 1 && bits <= 64) {  // as the forward scan: a one-word stack
+      ShapeStack<1> one;
+      one.clear();
+      one.w[0] = stack.word(0);
+      one.nz = one.w[0] ? 1u : 0u;
+      scanP<1>(in, c, q, s, one, (int)bits, image, target, pass == 1, status);
+    } else {
+      scanP<SECTIONS>(in, c, q, s, stack, (int)bits, image, target, pass == 1, status);
+    }
     if (q.overflow) return true;
     if (pass == 1) {
       const float2 d = make_float2((float)c.deltaX, (float)c.deltaY);

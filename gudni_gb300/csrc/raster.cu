@@ -47,7 +47,17 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[2]), (unsigned long long)q.length());
     atomicMax(reinterpret_cast<unsigned long long*>(&in.counters[3]), (unsigned long long)bits);
   }
-  renderColumn<SECTIONS>(in, c, q, stack, idx, status, (int)bits);
+  if (SECTIONS > 1 && bits <= 64) {
+    // every shape bit of the column sits in the first stack word: scan with a
+    // one-word stack (flips and findTop on a single register)
+    ShapeStack<1> one;
+    one.clear();
+    one.w[0] = stack.word(0);
+    one.nz = one.w[0] ? 1u : 0u;
+    renderColumn<1>(in, c, q, one, idx, status, (int)bits);
+  } else {
+    renderColumn<SECTIONS>(in, c, q, stack, idx, status, (int)bits);
+  }
   return q.overflow;
 }
 

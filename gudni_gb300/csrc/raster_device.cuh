@@ -174,6 +174,15 @@ struct Queue {
   }
 };
 
+// Queue scans stream through a column's slab, which for dense columns is far larger
+// than the cache share of one thread: loads are issued eight at a time, and the
+// section loop prefetches ahead of its cursor, so that a scan waits on one memory
+// round trip per eight entries instead of per entry.
+constexpr int kScanBlock = 8;
+__device__ __forceinline__ void prefetchL1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // The shape stack (ShapeState's shapeBits, K:270-292): one bit per shape of the
 // column, 64 per word.  `nz` marks the non-zero words, so findTop skips empty words
 // with one bit scan instead of a word-by-word walk (the reference walks the words;
@@ -408,7 +417,16 @@ __device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* str
     const float4* tree = reinterpret_cast<const float4*>(strand + 32);
     searchTree(l, tree, treeSize, d, true);
     searchTree(r, tree, treeSize, d, false);
-    spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status, above);
+    // every line spawnThresholds makes ends on a point of the two curves found or on
+    // an intercept inside their hulls: cull by the hulls' y range (one-pixel margin)
+    const float lo = fminf(fminf(fminf(l.left.y, l.control.y), fminf(l.right.y, r.left.y)),
+                           fminf(r.control.y, r.right.y));
+    const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
+                           fmaxf(r.control.y, r.right.y));
+    const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
+    const bool ordered = sum == sum;  // no NaN among them: the culling below is safe
+    if (ordered && lo >= g.c->floatHeight + 1.0f) return;  // all below the column: dropped, no enclosure
+    spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status, above || (ordered && hi <= -1.0f));
   }
 }
 
@@ -673,57 +691,245 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
   return base;
 }
 
+// Second-level memo for columns whose shape bits fit in one stack word: the last few
+// (word, colour) pairs, exact -- the colour is a function of the word and, when a
+// picture or gradient layer was composited, of the pixel row.
+struct WordCache {
+  static constexpr int N = 4;
+  uint64_t key[N];
+  float4 color[N];
+  int stop[N];
+  int row[N];  // -2 empty, -1 any row, else the pixel row
+  int next;
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int e = 0; e < N; ++e) row[e] = -2;
+    next = 0;
+  }
+  __device__ __forceinline__ int find(uint64_t k, int py) const {
+#pragma unroll
+    for (int e = 0; e < N; ++e)
+      if (row[e] != -2 && key[e] == k && (row[e] == -1 || row[e] == py)) return e;
+    return -1;
+  }
+  __device__ __forceinline__ void put(uint64_t k, int py, bool positional, float4 c, int stopBit) {
+    const int e = next;
+    next = (next + 1) & (N - 1);
+    key[e] = k;
+    color[e] = c;
+    stop[e] = stopBit;
+    row[e] = positional ? py : -1;
+  }
+};
+
 struct Parse {
   int current, numActive;
   float sStartX, sStartY, sEndX, sEndY;
   float pixelY;
 };
 
+// The split of one active threshold at `slicePoint` (sliceActive K:1040-1067): the
+// part above stays in place (returned through ch/cur), the part below is returned in
+// sh/split.
+__device__ __forceinline__ void splitAt(uint32_t& ch, float4& cur, float slicePoint, uint32_t& sh, float4& split) {
+  const float splitX = intersectX(ch, cur, slicePoint);
+  if (hPositive(ch)) {
+    split = make_float4(slicePoint, cur.y, splitX, cur.w);
+    cur = make_float4(cur.x, slicePoint, cur.z, splitX);
+    sh = ch & kUnpersist;
+  } else {
+    split = make_float4(slicePoint, cur.y, cur.z, splitX);
+    cur = make_float4(cur.x, slicePoint, splitX, cur.w);
+    sh = ch;
+    ch = ch & kUnpersist;
+  }
+}
+
 // splitNext K:1069-1077 (countActive K:1007, nextSlicePoint K:1026, sliceActive K:1040)
+//
+// The reference inserts each kept lower part with insertThreshold, which walks from
+// the queue front past every entry the part is strictly below -- all n active entries
+// (their tops are below slicePoint, the part's top) and then the equal-top entries
+// ahead of it.  Done literally that is n steps per part.  Here, when every active top
+// compares below slicePoint and the slab has room, the parts are first collected below
+// the queue, the active block is moved down by their number once, and each part is
+// inserted into the rest of the queue by the same walk started past the active block:
+// the resulting order is the reference's entry for entry.  Otherwise the literal
+// insertion runs.
 __device__ __forceinline__ float splitNext(Queue& q, Parse& p) {
   const int len = q.length();
   float slicePoint = FLT_MAX;
   const float top = q.get(0).x;
   int n = 1;
-  while (n < len) {
-    float t = q.get(n).x;
-    if (t > top) {
-      slicePoint = t;
-      break;
+  bool found = false;
+  for (int n0 = 1; n0 < len && !found; n0 += kScanBlock) {
+    float tb[kScanBlock];
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k) tb[k] = (n0 + k < len) ? q.get(n0 + k).x : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k) {
+      if (!found && n0 + k < len) {
+        if (tb[k] > top) {
+          slicePoint = tb[k];
+          found = true;
+        } else {
+          n = n0 + k + 1;
+        }
+      }
     }
-    n += 1;
   }
   p.numActive = n;
   float sp = slicePoint;
-  for (int i = 0; i < n; ++i) {
-    float bottom = q.get(i).y;
-    if (top < bottom) sp = cl_min(sp, bottom);
+  for (int i0 = 0; i0 < n; i0 += kScanBlock) {
+    float bb[kScanBlock];
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k) bb[k] = (i0 + k < n) ? q.get(i0 + k).y : 0.0f;
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k)
+      if (i0 + k < n && top < bb[k]) sp = cl_min(sp, bb[k]);
   }
   slicePoint = cl_min(slicePoint, sp);
-  for (int cursor = 0; cursor < n; ++cursor) {
-    uint32_t ch = q.getH(cursor);
-    float4 cur = q.get(cursor);
-    if (cur.x < slicePoint && slicePoint < cur.y) {
-      float splitX = intersectX(ch, cur, slicePoint);
-      uint32_t sh;
-      float4 split;
-      if (hPositive(ch)) {
-        split = make_float4(slicePoint, cur.y, splitX, cur.w);
-        cur = make_float4(cur.x, slicePoint, cur.z, splitX);
-        sh = ch & kUnpersist;
-      } else {
-        split = make_float4(slicePoint, cur.y, cur.z, splitX);
-        cur = make_float4(cur.x, slicePoint, splitX, cur.w);
-        sh = ch;
-        ch = ch & kUnpersist;
-      }
-      q.setH(cursor, ch);
-      q.set(cursor, cur);
-      if (tKeep(sh, split)) {
-        q.insert(sh, split);
-        if (q.overflow) return slicePoint;
+  bool batched = q.start >= 2 * n;
+  for (int i = 0; batched && i < n; ++i) batched = q.get(i).x < slicePoint;
+  if (!batched) {
+    for (int cursor = 0; cursor < n; ++cursor) {
+      uint32_t ch = q.getH(cursor);
+      float4 cur = q.get(cursor);
+      if (cur.x < slicePoint && slicePoint < cur.y) {
+        uint32_t sh;
+        float4 split;
+        splitAt(ch, cur, slicePoint, sh, split);
+        q.setH(cursor, ch);
+        q.set(cursor, cur);
+        if (tKeep(sh, split)) {
+          q.insert(sh, split);
+          if (q.overflow) return slicePoint;
+        }
       }
     }
+    return slicePoint;
+  }
+  // split in place, parts to [start - n - m, start - n), part j at start - n - 1 - j
+  const int s0 = q.start;
+  int m = 0;
+  for (int cursor = 0; cursor < n; ++cursor) {
+    if ((cursor & (kScanBlock - 1)) == 0 && cursor + kScanBlock < n) {
+      prefetchL1(&q.thr[s0 + cursor + kScanBlock]);
+      prefetchL1(&q.hdr[s0 + cursor + kScanBlock]);
+    }
+    uint32_t ch = q.hdr[s0 + cursor];
+    float4 cur = q.thr[s0 + cursor];
+    if (cur.x < slicePoint && slicePoint < cur.y) {
+      uint32_t sh;
+      float4 split;
+      splitAt(ch, cur, slicePoint, sh, split);
+      q.hdr[s0 + cursor] = ch;
+      q.thr[s0 + cursor] = cur;
+      if (tKeep(sh, split)) {
+        q.hdr[s0 - n - 1 - m] = sh;
+        q.thr[s0 - n - 1 - m] = split;
+        ++m;
+      }
+    }
+  }
+  if (m == 0) return slicePoint;
+  // Many parts: when no key involved is NaN the comparator is a strict weak order, so
+  // inserting the parts one by one equals sorting them (ties: the later part first)
+  // and merging them ahead of equal keys into the sorted rest of the queue.
+  bool merge = m >= 8 && s0 >= n + 2 * m;
+  for (int j = 0; merge && j < m; ++j) {
+    const uint32_t h = q.hdr[s0 - n - 1 - j];
+    const float4 t = q.thr[s0 - n - 1 - j];
+    const float tx = tTopX(h, t), sl = invSlope(h, t);
+    merge = tx == tx && sl == sl;
+  }
+  int rEnd = s0 + n;  // end of the equal-top group at the front of the rest
+  while (merge && rEnd < q.cap && q.thr[rEnd].x == slicePoint) {
+    const float tx = tTopX(q.hdr[rEnd], q.thr[rEnd]), sl = invSlope(q.hdr[rEnd], q.thr[rEnd]);
+    merge = tx == tx && sl == sl;
+    ++rEnd;
+  }
+  if (merge && rEnd < q.cap) merge = q.thr[rEnd].x > slicePoint;
+  // the active block moves down by m (destinations below sources; the parts lie below
+  // the block's new place since m <= n)
+  for (int i = 0; i < n; ++i) {
+    if ((i & (kScanBlock - 1)) == 0 && i + kScanBlock < n) {
+      prefetchL1(&q.thr[s0 + i + kScanBlock]);
+      prefetchL1(&q.hdr[s0 + i + kScanBlock]);
+    }
+    q.hdr[s0 - m + i] = q.hdr[s0 + i];
+    q.thr[s0 - m + i] = q.thr[s0 + i];
+  }
+  q.start = s0 - m;
+  if (merge) {
+    // stable bottom-up merge sort of the parts, stored newest first at [lo, lo + m),
+    // through [lo - m, lo)
+    const int lo = s0 - n - m;
+    int src = lo, dst = lo - m;
+    for (int width = 1; width < m; width *= 2) {
+      for (int a0 = 0; a0 < m; a0 += 2 * width) {
+        const int mid = min(a0 + width, m), hi = min(a0 + 2 * width, m);
+        int a = a0, b = mid, o = a0;
+        while (a < mid && b < hi) {
+          if (isBelow(q.hdr[src + a], q.thr[src + a], q.hdr[src + b], q.thr[src + b])) {
+            q.hdr[dst + o] = q.hdr[src + b];
+            q.thr[dst + o] = q.thr[src + b];
+            ++b;
+          } else {
+            q.hdr[dst + o] = q.hdr[src + a];
+            q.thr[dst + o] = q.thr[src + a];
+            ++a;
+          }
+          ++o;
+        }
+        for (; a < mid; ++a, ++o) {
+          q.hdr[dst + o] = q.hdr[src + a];
+          q.thr[dst + o] = q.thr[src + a];
+        }
+        for (; b < hi; ++b, ++o) {
+          q.hdr[dst + o] = q.hdr[src + b];
+          q.thr[dst + o] = q.thr[src + b];
+        }
+      }
+      const int t = src;
+      src = dst;
+      dst = t;
+    }
+    // merge into the gap ahead of the rest: a rest entry goes first only when the part
+    // is strictly below it (writes never pass the rest's read position)
+    int o = s0 - m + n, r = s0 + n;
+    for (int j = 0; j < m; ++o) {
+      const uint32_t ph = q.hdr[src + j];
+      const float4 pt = q.thr[src + j];
+      if (r < q.cap && isBelow(ph, pt, q.hdr[r], q.thr[r])) {
+        q.hdr[o] = q.hdr[r];
+        q.thr[o] = q.thr[r];
+        ++r;
+      } else {
+        q.hdr[o] = ph;
+        q.thr[o] = pt;
+        ++j;
+      }
+    }
+    return slicePoint;
+  }
+  // insert the parts in order into the queue past the active block
+  int f = s0 + n;
+  for (int j = 0; j < m; ++j) {
+    const uint32_t h = q.hdr[s0 - n - 1 - j];
+    const float4 t = q.thr[s0 - n - 1 - j];
+    f -= 1;
+    int at = f;
+    while (at + 1 < q.cap) {
+      const uint32_t oh = q.hdr[at + 1];
+      const float4 o = q.thr[at + 1];
+      if (!isBelow(h, t, oh, o)) break;
+      q.hdr[at] = oh;
+      q.thr[at] = o;
+      at += 1;
+    }
+    q.hdr[at] = h;
+    q.thr[at] = t;
   }
   return slicePoint;
 }
@@ -733,7 +939,14 @@ template <int SECTIONS>
 __device__ __forceinline__ void verticalAdvance(Queue& q, const ColumnState& c, Parse& p,
                                                 ShapeStack<SECTIONS>& stack) {
   if (p.sEndX != kRight) return;
-  for (int i = 0; i < p.numActive; ++i) stack.pass(q.getH(i));
+  for (int i0 = 0; i0 < p.numActive; i0 += kScanBlock) {
+    uint32_t hb[kScanBlock];
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k) hb[k] = (i0 + k < p.numActive) ? q.getH(i0 + k) : 0u;
+#pragma unroll
+    for (int k = 0; k < kScanBlock; ++k)
+      if (i0 + k < p.numActive) stack.pass(hb[k]);
+  }
   const float nextBreak = cl_min(c.floatHeight, p.pixelY);
   const float activeBottom = q.length() > 0 ? q.get(0).y : FLT_MAX;
   if (activeBottom == p.sEndY) {
@@ -806,6 +1019,9 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   bool colorOk = false;
   bool colorPositional = false;
   int colorStop = 0;
+  WordCache words;
+  words.clear();
+  const bool oneWord = shapeBits <= 64;
   for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
     if (colorPositional) colorOk = false;
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
@@ -820,6 +1036,10 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       // horizontalAdvance
       float nextX = kRight;
       if (p.current < p.numActive) {
+        if ((p.current & (kScanBlock - 1)) == 0 && p.current + kScanBlock < p.numActive) {
+          prefetchL1(&q.thr[q.start + p.current + kScanBlock]);
+          prefetchL1(&q.hdr[q.start + p.current + kScanBlock]);
+        }
         const float4 t = q.get(p.current);
         const uint32_t h = q.getH(p.current);
         const float yMid = p.sStartY + ((p.sEndY - p.sStartY) * 0.5f);
@@ -829,7 +1049,15 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       p.sStartX = p.sEndX;
       p.sEndX = nextX;
       if (!colorOk || stack.hiFlip >= colorStop) {
-        color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, colorPositional, colorStop);
+        const int e = oneWord ? words.find(stack.word(0), py) : -1;
+        if (e >= 0) {
+          color = words.color[e];
+          colorStop = words.stop[e];
+          colorPositional = words.row[e] >= 0;
+        } else {
+          color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, colorPositional, colorStop);
+          if (oneWord) words.put(stack.word(0), py, colorPositional, color, colorStop);
+        }
         colorOk = true;
         stack.clearFlips();
       }
