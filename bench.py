@@ -326,19 +326,29 @@ def run_batch(args):
         return ts
 
     h = stream.cuda_stream
-    for _ in range(args.warmup):
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    for i in range(args.warmup):
+        t0 = time.perf_counter()
         r.render(use_graph=True, stream=h)
-        r.render_each_scene(stream=h)
-    r.sync_status()
+        r.sync_status()
+        log(f"warm-up batch {i}: {time.perf_counter() - t0:.2f} s")
     launches0 = r.launch_count()
     with ClockSampler(0) as clocks:
         bt = timed(lambda: r.render(use_graph=True, stream=h), args.steps)
     r.sync_status()
-    pt = timed(lambda: r.render_each_scene(stream=h), args.steps)
-    r.sync_status()
     launches = r.launch_count() - launches0
+    log(f"batched: {bt} ms")
+    # the plain path: one launch pair per scene, each timed on its own (after one
+    # untimed pass over every scene), summed
+    r.render_each_scene(stream=h)
+    r.sync_status()
+    per_scene = []
+    for i, (first, count) in enumerate(batch.frame_tiles):
+        per_scene.append(timed(lambda: r.render_tiles(first, count, stream=h), 1)[0])
+    r.sync_status()
+    log(f"plain per scene (ms): max {max(per_scene):.1f}, sum {sum(per_scene):.1f}")
     batched_ms = sum(bt) / len(bt)
-    plain_ms = sum(pt) / len(pt)
+    plain_ms = sum(per_scene)
     pixels = batch.out_pixels
     n = len(frames)
     out = r.download()
@@ -365,7 +375,8 @@ def run_batch(args):
                        "l2": "flushed between steps (256 MB write)", "data": "synthetic, seeded"},
             "mpixels_per_s": pixels / (batched_ms / 1000) / 1e6,
             "plain_per_scene": {"ms_per_batch": plain_ms, "frames_per_s": n / (plain_ms / 1000),
-                                "launches_per_batch": 2 * n},
+                                "launches_per_batch": 2 * n, "slowest_scene_ms": max(per_scene),
+                                "timing": "each scene's launch pair timed alone, summed"},
             "batched_over_plain": plain_ms / batched_ms,
             "gpu_launches": int(launches), "clocks": clocks.summary(), "parity_vs_oracle": parity,
             "host_s": {"generate": t_gen, "autotune": t_tune, "serialize": t_ser}}

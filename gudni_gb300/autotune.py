@@ -19,7 +19,7 @@ from . import scene as S
 # (tile size, threads per tile); threads per tile must be >= tile size.  More threads
 # per tile make shorter columns (more parallel work, more threshold generation);
 # smaller tiles give each column fewer shapes.
-CANDIDATES: Tuple[Tuple[int, int], ...] = ((8, 32), (16, 64), (16, 256), (32, 32), (32, 256))
+CANDIDATES: Tuple[Tuple[int, int], ...] = ((8, 32), (16, 64), (32, 256))
 BUCKETS: Tuple[int, ...] = (96, 192, 384, 768, 1 << 30)  # upper bound of max(canvas side)
 
 
@@ -45,7 +45,7 @@ def autotune(flats: Sequence[S.FlatScene], max_shape: int, max_thresholds: int, 
              samples: int = 2, reps: int = 3, candidates=CANDIDATES, device: int = 0,
              log=None) -> Dict[int, Tuple[int, int]]:
     """Return {bucket: (tile, threads_per_tile)}.  Each candidate renders the bucket's
-    sample scenes (its most expensive and, with samples > 1, its median scene by
+    sample scenes (its median and, with samples > 1, its most expensive scene by
     scene_cost) as one batch; the fastest mean over `reps` replays wins.  A candidate
     whose first render is over three times the best so far is not replayed."""
     by_bucket: Dict[int, List[S.FlatScene]] = {}
@@ -56,7 +56,7 @@ def autotune(flats: Sequence[S.FlatScene], max_shape: int, max_thresholds: int, 
     with B.BatchRasterizer(base, device) as r:
         for b, members in sorted(by_bucket.items()):
             ranked = sorted(members, key=scene_cost)
-            picks = [ranked[-1]] + ([ranked[len(ranked) // 2]] if samples > 1 and len(ranked) > 1 else [])
+            picks = [ranked[len(ranked) // 2]] + ([ranked[-1]] if samples > 1 and len(ranked) > 1 else [])
             best = None
             for tile, tpt in candidates:
                 spec = spec_for(tile, tpt, max_shape, max_thresholds, strands_per_tile)

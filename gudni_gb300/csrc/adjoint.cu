@@ -44,6 +44,7 @@ struct EP {
 
 struct LineRec {
   EP a, b;
+  float invDy;  // 1 / (b.y - a.y), or 0 for a horizontal line
 };
 
 // y source: line*2 + end (0 = a, 1 = b), or -1 for a constant
@@ -248,6 +249,7 @@ __device__ __forceinline__ void addLineP(AdjGen& g, const EP& A, const EP& B, ui
       }
       g.lines[id].a = A;
       g.lines[id].b = B;
+      g.lines[id].invDy = (B.y != A.y) ? 1.0f / (B.y - A.y) : 0.0f;
       *g.n_lines = id + 1;
       g.q->push(h, t, make_int4(id, top, bot, 0));
     }
@@ -495,8 +497,8 @@ __device__ __forceinline__ void compositeAdjoint(float4 f, float4 b, float4 dout
 __device__ __forceinline__ bool lineX(const LineRec& L, float y, float dX[4], float& dXdy) {
   const float xa = L.a.x, ya = L.a.y, xb = L.b.x, yb = L.b.y;
   if (yb == ya) return false;
-  const float s = (y - ya) / (yb - ya);
-  const float m = (xb - xa) / (yb - ya);
+  const float s = (y - ya) * L.invDy;
+  const float m = (xb - xa) * L.invDy;
   dX[0] = 1.0f - s;
   dX[1] = m * (s - 1.0f);
   dX[2] = s;
@@ -590,6 +592,11 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   int colorStop = 0, K = 0;
   float chainArea = 0.0f;
   float gI[3] = {0.0f, 0.0f, 0.0f}, I[3] = {0.0f, 0.0f, 0.0f}, A = 1.0f;
+  // Geometry gradients are gathered per band: every section of a band shares its y
+  // sources, and a threshold line is the right edge of one section and the left edge
+  // of the next at the same mid-height, so its two contributions are summed
+  // (pendCoef) and applied once.
+  float gY0 = 0.0f, gY1 = 0.0f, pendCoef = 0.0f;
   auto flushChain = [&]() {
     if (grad && chainArea != 0.0f && K > 0) {
       float4 d = make_float4(gI[0] * chainArea / A, gI[1] * chainArea / A, gI[2] * chainArea / A, 0.0f);
@@ -723,6 +730,11 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
             }
           }
         }
+        if (grad) {
+          addY(s.lineGrad, srcY0, gY0);
+          addY(s.lineGrad, srcY1, gY1);
+          gY0 = gY1 = 0.0f;
+        }
         sy0 = sy1;
         srcY0 = srcY1;
         sy1 = nextBottom;
@@ -768,39 +780,36 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       acc2 += col.z * a;
       area += a;
       if (grad) {
+        // a = (x1 - x0)(y1 - y0): d/dx1 = w, d/dx0 = -w, d/dy1 = h, d/dy0 = -h
         const float dA = (gI[0] * (col.x - I[0]) + gI[1] * (col.y - I[1]) + gI[2] * (col.z - I[2])) / A;
         const float w = sy1 - sy0, hgt = sx1 - sx0;
-        const float dx1 = dA * w, dx0 = -dA * w;
-        float dy1 = dA * hgt, dy0 = -dA * hgt;
-        const float ym = sy0 + (sy1 - sy0) * 0.5f;
-        float dym = 0.0f;
-        float dX[4], dXdy;
-        if (srcX1 >= 0 && lineX(s.lines[srcX1], ym, dX, dXdy)) {
-          float4& g = s.lineGrad[srcX1];
-          g.x += dx1 * dX[0];
-          g.y += dx1 * dX[1];
-          g.z += dx1 * dX[2];
-          g.w += dx1 * dX[3];
-          dym += dx1 * dXdy;
+        gY0 -= dA * hgt;
+        gY1 += dA * hgt;
+        if (srcX0 >= 0) {  // the previous section's right edge: both contributions at once
+          const float coef = pendCoef - dA * w;
+          float dX[4], dXdy;
+          if (lineX(s.lines[srcX0], sy0 + (sy1 - sy0) * 0.5f, dX, dXdy)) {
+            float4& g = s.lineGrad[srcX0];
+            g.x += coef * dX[0];
+            g.y += coef * dX[1];
+            g.z += coef * dX[2];
+            g.w += coef * dX[3];
+            gY0 += 0.5f * coef * dXdy;
+            gY1 += 0.5f * coef * dXdy;
+          }
         }
-        if (srcX0 >= 0 && lineX(s.lines[srcX0], ym, dX, dXdy)) {
-          float4& g = s.lineGrad[srcX0];
-          g.x += dx0 * dX[0];
-          g.y += dx0 * dX[1];
-          g.z += dx0 * dX[2];
-          g.w += dx0 * dX[3];
-          dym += dx0 * dXdy;
-        }
-        dy0 += 0.5f * dym;
-        dy1 += 0.5f * dym;
-        addY(s.lineGrad, srcY0, dy0);
-        addY(s.lineGrad, srcY1, dy1);
+        pendCoef = dA * w;  // for srcX1, applied with the next section
         chainArea += a;  // colour: back through the composite chain at the next flush
       }
       if (current < numActive) stack.pass(q.hdr[q.start + current]);
       current += 1;
     }
     flushChain();  // dL/dI changes with the pixel
+    if (grad) {  // the row's last band
+      addY(s.lineGrad, srcY0, gY0);
+      addY(s.lineGrad, srcY1, gY1);
+      gY0 = gY1 = 0.0f;
+    }
     if (!grad) image[pix] = make_float4(acc0 / area, acc1 / area, acc2 / area, area);
     sx0 = kLeft;
     srcX0 = kConst;
