@@ -73,6 +73,8 @@ WORKLOADS = {
     # the differentiable form (run_adjoint): 1024x1024, 500 random shapes of 16 segments
     "adjoint1024": ("random_1024x1024_shapes500_seg16",
                     "Mpixels/s (fwd+adjoint, 1024x1024 500 shapes, grads vs FP64 reference)"),
+    # batched fitting (run_fit): 64 scenes of 256x256, 128 shapes each, Adam on points and colours
+    "fit64": ("fit_64x256x256_shapes128", "steps/s (batched fwd+adjoint fitting, 64 scenes 256x256)"),
 }
 
 
@@ -247,7 +249,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    if args.workload not in ("page4k", "random512"):
+    if args.workload not in ("page4k", "random512"):  # batch256, adjoint1024, fit64
         print(json.dumps({"impl": "reference", "unavailable": f"workload {args.workload} has no reference "
                           "counterpart (the reference renders one scene per call and has no adjoint)"}))
         return 0
@@ -506,6 +508,77 @@ def run_adjoint(args):
     return 0
 
 
+FIT_SPEC = dict(max_tile_size=32, threads_per_tile=256, max_thresholds=4096, max_shape=255,
+                max_strands_per_tile=1 << 24)
+
+
+def fit_scenes(n=64, side=256, shapes=128, jitter_px=0.0, color_sigma=0.0, seed=100):
+    from gudni_gb300 import scenes as G
+    out = []
+    for i in range(n):
+        f = G.random_shapes(seed=seed + i, width=side, height=side, n_shapes=shapes)
+        if jitter_px or color_sigma:
+            rng = np.random.default_rng(10_000 + seed + i)
+            f.pairs = (f.pairs + rng.normal(0, jitter_px, f.pairs.shape)).astype(np.float32)
+            c = f.substance_color + rng.normal(0, color_sigma, f.substance_color.shape)
+            f.substance_color = np.clip(c, 0.0, 1.0).astype(np.float32)
+        out.append(f)
+    return out
+
+
+def run_fit(args):
+    """Batched fitting: 64 independent 256x256 scenes of 128 shapes fitted by Adam (lr
+    0.5 px on points, 0.01 on colours) to targets rendered from perturbed copies
+    (points N(0, 4 px), colours N(0, 0.1)); each step serializes the scenes, runs every
+    scene's forward and adjoint in one launch and updates on the host."""
+    import torch
+    from gudni_gb300 import adjoint as A
+    from gudni_gb300 import fit as F
+    from gudni_gb300 import lib as L
+    from gudni_gb300 import scene as S
+    from gudni_gb300.raster import Rasterizer
+
+    torch.cuda.set_device(0)
+    spec = L.make_spec(**FIT_SPEC)
+    log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
+    targets = []
+    with Rasterizer(spec) as r:
+        for f in fit_scenes(jitter_px=4.0, color_sigma=0.1):
+            fa = A.FrameAdjoint(r, S.serialize_flat(f, spec))
+            _, img, _, _ = fa.loss_and_gradient(np.zeros((f.canvas_h, f.canvas_w, 4), np.float32))
+            targets.append(img.cpu().numpy())
+    fit = F.BatchFit(fit_scenes(), targets, spec, lr_points=0.5, lr_colors=0.01)
+    pixels = 64 * 256 * 256
+    for _ in range(args.warmup):  # warm-up steps are fitting steps too; they are counted in `steps_total`
+        fit.step()
+    first = None
+    t0 = time.perf_counter()
+    losses = []
+    for k in range(args.steps):
+        loss = fit.step()
+        losses.append(loss)
+        if first is None:
+            first = loss
+        if k % max(1, args.steps // 10) == 0:
+            log(f"step {k}: loss {loss:.4f} per-pixel L2 {loss / (pixels * 3):.6f}")
+    wall = time.perf_counter() - t0
+    final = losses[-1]
+    line = {"metric": WORKLOADS["fit64"][1], "value": args.steps / wall, "unit": "steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["fit64"][0], "scenes": 64, "canvas": [256, 256], "shapes": 128,
+                       **FIT_SPEC, "lr_points_px": 0.5, "lr_colors": 0.01,
+                       "targets": "perturbed copies: points N(0, 4 px), colours N(0, 0.1)",
+                       "data": "synthetic, seeded"},
+            "steps_total": args.warmup + args.steps,
+            "loss": {"first_timed": first, "final": final, "per_pixel_l2_first": first / (pixels * 3),
+                     "per_pixel_l2_final": final / (pixels * 3)},
+            "seconds": {k: v for k, v in fit.timings.items()}}
+    print(json.dumps(line))
+    fit.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -514,6 +587,8 @@ def main():
         return run_batch(args)
     if args.workload == "adjoint1024":
         return run_adjoint(args)
+    if args.workload == "fit64":
+        return run_fit(args)
 
     import torch
 

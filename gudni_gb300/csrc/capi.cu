@@ -254,7 +254,7 @@ int validate_job(gudni_ctx* ctx, const gudni_shape* shapes, size_t n_shapes, con
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "compute_depth must be log2(threads_per_tile)");
   if (n_tiles > 0 && !tiles) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null tiles");
   if (n_shapes > 0 && !shapes) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null shapes");
-  if (n_tiles >= ((size_t)1 << (32 - gudni::kColumnBits)))
+  if (((uint64_t)n_tiles << gudni::chunkLog2(compute_depth)) >= gudni::kMaxUnits)
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles in one launch");
   if (n_shapes > 0xFFFFFFFFull) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many shapes");
   if (host) return validate_tiles_host(ctx, tiles, n_tiles, n_shapes);
@@ -473,7 +473,7 @@ void drop_graph(gudni_ctx* ctx) {
 }
 
 // Adjoint scratch, sized once: one slot per resident thread (capped so the whole
-// stays within ~6 GB), each holding `capacity` thresholds with their provenance and
+// stays within ~16 GB), each holding `capacity` thresholds with their provenance and
 // line records, per-shape-bit index and colour-gradient words, and the composited
 // layers of one section (at most max_shape + 1).
 int ensure_adjoint_scratch(gudni_ctx* ctx) {
@@ -492,7 +492,7 @@ int ensure_adjoint_scratch(gudni_ctx* ctx) {
                           (size_t)ctx->spec.max_shape * (4 + sizeof(float4)) +
                           (size_t)(ctx->spec.max_shape + 1) * (2 * sizeof(float4) + 4);
   size_t slots = (size_t)ctx->sm_count * (size_t)bps * gudni::kAdjointBlock;
-  slots = std::min(slots, ((size_t)6 << 30) / per_slot);
+  slots = std::min(slots, ((size_t)16 << 30) / per_slot);
   slots = std::max<size_t>(gudni::kAdjointBlock, (slots / gudni::kAdjointBlock) * gudni::kAdjointBlock);
   cudaError_t e;
   if ((e = ctx->a_thr.reserve(slots * cap)) != cudaSuccess ||
@@ -721,7 +721,7 @@ int gudni_raster_frame(gudni_ctx* ctx, const gudni_job_desc* jobs, size_t n_jobs
       ctx->h_tile_jobs.push_back((int32_t)j);
     }
   }
-  if (ctx->h_tiles.size() >= ((size_t)1 << (32 - gudni::kColumnBits)))
+  if (((uint64_t)ctx->h_tiles.size() << gudni::chunkLog2(compute_depth)) >= gudni::kMaxUnits)
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles in one frame");
   cudaSetDevice(ctx->device);
   int rc;
@@ -775,7 +775,7 @@ int gudni_batch_upload(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   drop_graph(ctx);
   if ((n_tiles && (!tiles || !tile_scene)) || (n_scenes && !scenes) || (n_shapes && !shapes))
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "null batch array");
-  if (n_tiles >= ((size_t)1 << (32 - gudni::kColumnBits))) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles");
+  if ((uint64_t)n_tiles * 32 >= gudni::kMaxUnits) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many tiles");
   int rc = validate_tiles_host(ctx, tiles, n_tiles, n_shapes);
   if (rc) return rc;
   int max_tpt = 1;

@@ -89,7 +89,8 @@ extern "C" int gudni_raster_job_noalloc(const gudni_spec* spec, const void* geom
   if (!aligned(geometry, 16) || !aligned(substances, 16) || !aligned(picture_uses, 4) || !aligned(radials, 16) ||
       !aligned(shapes, 8) || !aligned(tiles, 4) || !aligned(out, 4) || !aligned(pictures, 4))
     return fail(GUDNI_ERR_BAD_INPUT, "misaligned device pointer");
-  if (n_tiles >= ((size_t)1 << (32 - gudni::kColumnBits)) || n_shapes > 0xFFFFFFFFull)
+  if (compute_depth < 0 || compute_depth > gudni::kMaxLog2Tpt ||
+      ((uint64_t)n_tiles << gudni::chunkLog2(compute_depth)) >= gudni::kMaxUnits || n_shapes > 0xFFFFFFFFull)
     return fail(GUDNI_ERR_BAD_INPUT, "too many tiles or shapes");
 
   cudaStream_t s = (cudaStream_t)stream;

@@ -16,7 +16,7 @@
 //   queue of `capacity` entries and the shape-index table of its column).
 //
 // raster_list_kernel -- the full-capacity pass.  Columns that overflowed the fast
-//   pass's small working capacity were appended to a list; this kernel, launched
+//   pass's small working capacity were appended to a list (work unit and lane); this kernel, launched
 //   right after on the same stream, reads the list's length on the device and re-runs
 //   them with the spec's max_thresholds.  The result does not depend on the capacity,
 //   only on whether it suffices, and no host round trip separates the two launches
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a
         if (a.overflow_items) {
           const uint32_t n = atomicAdd(a.overflow_count, 1u);
           if (n < a.overflow_cap) {
-            a.overflow_items[n] = ((uint32_t)tile << kColumnBits) | (uint32_t)column;
+            a.overflow_items[n] = (k << kLaneBits) | (uint32_t)lane;
           } else {
             status |= kStatusOverflow;
           }
@@ -115,8 +115,9 @@ __global__ void __launch_bounds__(kRasterBlock) raster_list_kernel(TileLaunch a)
   const uint32_t n_items = min(*a.list_count, a.list_cap);
   for (uint32_t w = slot; w < n_items; w += nslots) {
     const uint32_t item = a.list[w];
-    const int tile = (int)(item >> kColumnBits);
-    const int column = (int)(item & ((1u << kColumnBits) - 1u));
+    int tile, chunk;
+    unitOf(a.units, a.chunk_log2, item >> kLaneBits, tile, chunk);
+    const int column = chunk * 32 + (int)(item & ((1u << kLaneBits) - 1u));
     bool ok;
     const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
     if (!ok) continue;

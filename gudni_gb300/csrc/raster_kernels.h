@@ -8,7 +8,8 @@
 namespace gudni {
 
 constexpr int kRasterBlock = 128;
-constexpr int kColumnBits = 11;   // overflow-list items are (tile << 11) | column
+constexpr int kLaneBits = 5;      // overflow-list items are (work unit << 5) | lane
+constexpr uint64_t kMaxUnits = 1ull << 27;  // work units per launch (items fit 32 bits)
 constexpr int kMaxLog2Tpt = 10;   // up to 1024 threads per tile
 constexpr int kChunkBits = 5;     // work units are (tile << 5) | chunk of 32 columns
 

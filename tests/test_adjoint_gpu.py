@@ -119,3 +119,24 @@ def test_batch_adjoint_matches_frames():
             sg, ss = r.frame_slices(i)
             check_vec(gg[sg], g_geo, f"batch frame {i} geometry")
             check_vec(gs[ss], g_sub, f"batch frame {i} substances")
+
+
+def test_batch_fit_reduces_loss():
+    """A few Adam steps of the batched fitting loop bring every scene closer to its
+    target (targets rendered from perturbed copies of the same scenes)."""
+    from gudni_gb300 import fit as Fm
+    spec = L.make_spec(16, 32, 4096, 127, 8, max_strands_per_tile=1 << 24)
+    make = lambda i: G.random_shapes(seed=60 + i, width=64, height=64, n_shapes=12)  # noqa: E731
+    targets = []
+    for i in range(4):
+        t = make(i)
+        t = jitter(t, 2.0, 70 + i)
+        targets.append(O.render_float(S.serialize_flat(t, spec)))
+    fit = Fm.BatchFit([make(i) for i in range(4)], targets, spec, lr_points=0.3, lr_colors=0.01)
+    try:
+        first = fit.step()
+        for _ in range(40):
+            last = fit.step()
+    finally:
+        fit.close()
+    assert last < 0.8 * first, (first, last)
