@@ -17,7 +17,17 @@ The L2 (126 MB) is flushed between timed steps by writing a 256 MB buffer.
 
 `--impl reference` times the reference's own kernels (Kernels.cl compiled for the
 CPU, oracle/_ref) -- or, where that translation unit is not present, the oracle's
-restatement -- on all host cores, one frame per step.
+restatement -- on all host cores, one frame per step.  The reference has no radial
+gradient substance, so its arm renders the page with every gradient baked into an
+RGBA8 picture (scene.bake_radials, the reference's PictureFunction route); the line
+reports that image's parity with the oracle's rendering of the page itself.
+
+Other workloads (--workload): page1080 (a quarter page, the profiled size),
+random512 (512x512, 64 random shapes), batch256 (the batched form: 256 scenes in one
+persistent launch, CUDA graph, autotuned tile shapes, against one launch pair per
+scene), adjoint1024 (forward vs fwd+adjoint on 1024x1024 with 500 shapes, gradients
+checked against the FP64 reference and central differences), fit64 (batched
+fitting of 64 scenes by Adam, steps/s).
 
 Multi-GPU: frames are independent, so N ranks render N replicas (weak scaling).
 """
@@ -65,6 +75,9 @@ WORKLOADS = {
     # the headline plain workload
     "page4k": ("page_3840x2160_glyphs5000_shapes2000",
                "Mpixels/s (plain single-frame raster, 3840x2160 page, <=1 LSB RGBA8)"),
+    # a quarter of the page (1920x1080, 1250 glyphs, 500 shapes): the size profiled in full
+    "page1080": ("page_1920x1080_glyphs1250_shapes500",
+                 "Mpixels/s (plain single-frame raster, 1920x1080 page, <=1 LSB RGBA8)"),
     # the small CPU-runnable plain workload: 512x512, 64 random shapes of 8-32 segments
     "random512": ("random_512x512_shapes64",
                   "Mpixels/s (plain single-frame raster, 512x512 64 shapes, <=1 LSB RGBA8)"),
@@ -87,7 +100,12 @@ def make_frame(workload: str = "page4k", baked: bool = False, tile: int = 32, tp
 
     spec = L.make_spec(max_tile_size=tile, threads_per_tile=tpt, max_thresholds=4096, max_shape=127,
                        stack_sections=8)
-    flat = G.glyph_page(seed=1) if workload == "page4k" else G.random_shapes(seed=0)
+    if workload == "page4k":
+        flat = G.glyph_page(seed=1)
+    elif workload == "page1080":
+        flat = G.glyph_page(seed=1, width=1920, height=1080, n_glyphs=1250, n_shapes=500)
+    else:
+        flat = G.random_shapes(seed=0)
     if baked:
         flat = S.bake_radials(flat)
     return S.serialize_flat(flat, spec)
@@ -249,7 +267,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    if args.workload not in ("page4k", "random512"):  # batch256, adjoint1024, fit64
+    if args.workload not in ("page4k", "page1080", "random512"):  # batch256, adjoint1024, fit64
         print(json.dumps({"impl": "reference", "unavailable": f"workload {args.workload} has no reference "
                           "counterpart (the reference renders one scene per call and has no adjoint)"}))
         return 0
