@@ -119,6 +119,8 @@ struct gudni_ctx {
   DevBuf<gudni_tile_info> b_tiles;
   DevBuf<int32_t> b_tile_scene;
   DevBuf<uint32_t> b_order;           // work units, cost-descending
+  DevBuf<uint32_t> f_units;           // a frame's cost-ordered work units (device-built)
+  DevBuf<uint32_t> f_order_words;     // their bucket counts and cursors
   DevBuf<gudni::SceneInfo> b_scenes;
   DevBuf<uint32_t> b_out;
   cudaGraph_t graph = nullptr;
@@ -309,10 +311,21 @@ int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInf
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
   if (n_tiles == 0) return GUDNI_OK;
+  cudaError_t e;
+  if (!units && n_tiles >= 64) {
+    // no unit list given: schedule the tiles most expensive first, ordered on the device
+    n_units = n_tiles << chunk_log2;
+    if ((e = ctx->f_units.reserve(n_units)) != cudaSuccess || (e = ctx->f_order_words.reserve(128)) != cudaSuccess)
+      return cuda_fail(ctx, e, "tile order scratch");
+    if ((e = gudni::launch_tile_order(in.tiles, (uint32_t)n_tiles, in.shapes, in.n_shapes, chunk_log2,
+                                      ctx->f_order_words.ptr, ctx->f_units.ptr, stream)) != cudaSuccess)
+      return cuda_fail(ctx, e, "tile order");
+    ctx->launches += 3;
+    units = ctx->f_units.ptr;
+  }
   if (!units) n_units = n_tiles << chunk_log2;
   const size_t max_items = n_tiles * (size_t)max_tpt;
   const bool need_fallback = ctx->working_capacity < ctx->spec.max_thresholds;
-  cudaError_t e;
   if (need_fallback) {
     if ((e = ctx->overflow_items.reserve(max_items)) != cudaSuccess) return cuda_fail(ctx, e, "overflow list");
     if ((rc = ensure_fallback_pool(ctx))) return rc;
@@ -517,8 +530,19 @@ int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::
   int rc = ensure_adjoint_scratch(ctx);
   if (rc) return rc;
   if (n_tiles == 0) return GUDNI_OK;
+  cudaError_t e;
+  if (!units && n_tiles >= 64) {  // most expensive tiles first, as for the raster pass
+    n_units = n_tiles << chunk_log2;
+    if ((e = ctx->f_units.reserve(n_units)) != cudaSuccess || (e = ctx->f_order_words.reserve(128)) != cudaSuccess)
+      return cuda_fail(ctx, e, "tile order scratch");
+    if ((e = gudni::launch_tile_order(in.tiles, (uint32_t)n_tiles, in.shapes, in.n_shapes, chunk_log2,
+                                      ctx->f_order_words.ptr, ctx->f_units.ptr, stream)) != cudaSuccess)
+      return cuda_fail(ctx, e, "tile order");
+    ctx->launches += 3;
+    units = ctx->f_units.ptr;
+  }
   if (!units) n_units = n_tiles << chunk_log2;
-  cudaError_t e = cudaMemsetAsync(ctx->words.ptr, 0, 2 * sizeof(uint32_t), stream);
+  e = cudaMemsetAsync(ctx->words.ptr, 0, 2 * sizeof(uint32_t), stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "memset");
   gudni::AdjointLaunch a;
   std::memset(&a, 0, sizeof(a));
@@ -619,7 +643,7 @@ void gudni_destroy(gudni_ctx* ctx) {
   ctx->strand_table.release(); ctx->strand_y.release(); ctx->strand_first.release();
   ctx->tile_jobs.release(); ctx->out.release();
   ctx->b_shapes.release(); ctx->b_tiles.release(); ctx->b_tile_scene.release(); ctx->b_order.release();
-  ctx->b_scenes.release(); ctx->b_out.release();
+  ctx->b_scenes.release(); ctx->b_out.release(); ctx->f_units.release(); ctx->f_order_words.release();
   ctx->thr.release(); ctx->hdr.release(); ctx->idx.release(); ctx->big_thr.release(); ctx->big_hdr.release();
   ctx->big_idx.release(); ctx->overflow_items.release(); ctx->words.release(); ctx->status.release();
   ctx->counters.release();

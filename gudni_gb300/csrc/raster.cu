@@ -26,6 +26,8 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "raster_device.cuh"
 #include "raster_kernels.h"
 
@@ -62,7 +64,7 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
 }
 
 template <int SECTIONS>
-__global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a) {
+__global__ void __launch_bounds__(kRasterBlock, 4) raster_tiles_kernel(TileLaunch a) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
@@ -125,6 +127,61 @@ __global__ void __launch_bounds__(kRasterBlock) raster_list_kernel(TileLaunch a)
     if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) status |= kStatusOverflow;
   }
   if (status) atomicOr(a.status, status);
+}
+
+// ------------------------------------------------------------------ tile order
+// A frame's tiles differ in cost by orders of magnitude (a tile crossed by a large
+// shape against an empty one), and the persistent grid pulls units in list order, so
+// the expensive tiles should start first.  Three small kernels build a cost-descending
+// unit list on the device: a histogram of log2(cost) over the tiles, a prefix over the
+// 32 buckets in descending order, and a scatter of every tile's units to its bucket's
+// next slots (order within a bucket is arbitrary; the output does not depend on it).
+// Cost: the strands of the tile's shapes plus its shape count, plus one.
+
+__device__ __forceinline__ int tileBucket(const gudni_tile_info& ti, const gudni_shape* shapes, uint32_t n_shapes) {
+  uint64_t cost = 1;
+  if ((uint64_t)ti.shapes.start + ti.shapes.length <= n_shapes) {
+    for (uint32_t i = 0; i < ti.shapes.length; ++i) cost += 1 + shapes[ti.shapes.start + i].num_strands;
+  }
+  return 63 - __clzll((long long)cost);  // 0..63
+}
+
+__global__ void tile_cost_hist_kernel(const gudni_tile_info* tiles, uint32_t n_tiles, const gudni_shape* shapes,
+                                      uint32_t n_shapes, uint32_t* hist) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x)
+    atomicAdd(&hist[tileBucket(tiles[t], shapes, n_shapes)], 1u);
+}
+
+__global__ void tile_bucket_prefix_kernel(const uint32_t* hist, uint32_t* cursor) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    uint32_t acc = 0;
+    for (int b = 63; b >= 0; --b) {  // most expensive bucket first
+      cursor[b] = acc;
+      acc += hist[b];
+    }
+  }
+}
+
+__global__ void tile_order_scatter_kernel(const gudni_tile_info* tiles, uint32_t n_tiles, const gudni_shape* shapes,
+                                          uint32_t n_shapes, int chunk_log2, uint32_t* cursor, uint32_t* units) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_tiles; t += gridDim.x * blockDim.x) {
+    const uint32_t pos = atomicAdd(&cursor[tileBucket(tiles[t], shapes, n_shapes)], 1u);
+    for (uint32_t c = 0; c < (1u << chunk_log2); ++c)
+      units[((size_t)pos << chunk_log2) + c] = (t << kChunkBits) | c;
+  }
+}
+
+cudaError_t launch_tile_order(const gudni_tile_info* tiles, uint32_t n_tiles, const gudni_shape* shapes,
+                              uint32_t n_shapes, int chunk_log2, uint32_t* words128, uint32_t* units,
+                              cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(words128, 0, 128 * sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  const int grid = (int)std::min<uint32_t>((n_tiles + 255) / 256, 1024u);
+  tile_cost_hist_kernel<<<grid, 256, 0, stream>>>(tiles, n_tiles, shapes, n_shapes, words128);
+  tile_bucket_prefix_kernel<<<1, 32, 0, stream>>>(words128, words128 + 64);
+  tile_order_scatter_kernel<<<grid, 256, 0, stream>>>(tiles, n_tiles, shapes, n_shapes, chunk_log2, words128 + 64,
+                                                       units);
+  return cudaGetLastError();
 }
 
 int sections_for(int max_shape) {

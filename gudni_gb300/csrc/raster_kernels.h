@@ -101,6 +101,11 @@ __device__ __forceinline__ RasterInputs sceneInputs(const RasterInputs& base, co
 
 int sections_for(int max_shape);
 cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream);
+// Cost-descending work units of a frame's tiles (3 launches); words128: 128 words of
+// scratch (bucket counts and cursors), units: n_tiles << chunk_log2 entries.
+cudaError_t launch_tile_order(const gudni_tile_info* tiles, uint32_t n_tiles, const gudni_shape* shapes,
+                              uint32_t n_shapes, int chunk_log2, uint32_t* words128, uint32_t* units,
+                              cudaStream_t stream);
 cudaError_t raster_occupancy(int sections, int* blocks_per_sm);
 
 }  // namespace gudni
