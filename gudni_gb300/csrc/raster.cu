@@ -64,7 +64,7 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
 }
 
 template <int SECTIONS>
-__global__ void __launch_bounds__(kRasterBlock, 4) raster_tiles_kernel(TileLaunch a) {
+__global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;

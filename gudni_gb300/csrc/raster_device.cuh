@@ -174,15 +174,6 @@ struct Queue {
   }
 };
 
-// Queue scans stream through a column's slab, which for dense columns is far larger
-// than the cache share of one thread: loads are issued eight at a time, and the
-// section loop prefetches ahead of its cursor, so that a scan waits on one memory
-// round trip per eight entries instead of per entry.
-constexpr int kScanBlock = 8;
-__device__ __forceinline__ void prefetchL1(const void* p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
 // The shape stack (ShapeState's shapeBits, K:270-292): one bit per shape of the
 // column, 64 per word.  `nz` marks the non-zero words, so findTop skips empty words
 // with one bit scan instead of a word-by-word walk (the reference walks the words;
@@ -761,32 +752,19 @@ __device__ __forceinline__ float splitNext(Queue& q, Parse& p) {
   float slicePoint = FLT_MAX;
   const float top = q.get(0).x;
   int n = 1;
-  bool found = false;
-  for (int n0 = 1; n0 < len && !found; n0 += kScanBlock) {
-    float tb[kScanBlock];
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k) tb[k] = (n0 + k < len) ? q.get(n0 + k).x : 0.0f;
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k) {
-      if (!found && n0 + k < len) {
-        if (tb[k] > top) {
-          slicePoint = tb[k];
-          found = true;
-        } else {
-          n = n0 + k + 1;
-        }
-      }
+  while (n < len) {
+    float t = q.get(n).x;
+    if (t > top) {
+      slicePoint = t;
+      break;
     }
+    n += 1;
   }
   p.numActive = n;
   float sp = slicePoint;
-  for (int i0 = 0; i0 < n; i0 += kScanBlock) {
-    float bb[kScanBlock];
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k) bb[k] = (i0 + k < n) ? q.get(i0 + k).y : 0.0f;
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k)
-      if (i0 + k < n && top < bb[k]) sp = cl_min(sp, bb[k]);
+  for (int i = 0; i < n; ++i) {
+    float bottom = q.get(i).y;
+    if (top < bottom) sp = cl_min(sp, bottom);
   }
   slicePoint = cl_min(slicePoint, sp);
   bool batched = q.start >= 2 * n;
@@ -813,10 +791,6 @@ __device__ __forceinline__ float splitNext(Queue& q, Parse& p) {
   const int s0 = q.start;
   int m = 0;
   for (int cursor = 0; cursor < n; ++cursor) {
-    if ((cursor & (kScanBlock - 1)) == 0 && cursor + kScanBlock < n) {
-      prefetchL1(&q.thr[s0 + cursor + kScanBlock]);
-      prefetchL1(&q.hdr[s0 + cursor + kScanBlock]);
-    }
     uint32_t ch = q.hdr[s0 + cursor];
     float4 cur = q.thr[s0 + cursor];
     if (cur.x < slicePoint && slicePoint < cur.y) {
@@ -853,10 +827,6 @@ __device__ __forceinline__ float splitNext(Queue& q, Parse& p) {
   // the active block moves down by m (destinations below sources; the parts lie below
   // the block's new place since m <= n)
   for (int i = 0; i < n; ++i) {
-    if ((i & (kScanBlock - 1)) == 0 && i + kScanBlock < n) {
-      prefetchL1(&q.thr[s0 + i + kScanBlock]);
-      prefetchL1(&q.hdr[s0 + i + kScanBlock]);
-    }
     q.hdr[s0 - m + i] = q.hdr[s0 + i];
     q.thr[s0 - m + i] = q.thr[s0 + i];
   }
@@ -939,14 +909,7 @@ template <int SECTIONS>
 __device__ __forceinline__ void verticalAdvance(Queue& q, const ColumnState& c, Parse& p,
                                                 ShapeStack<SECTIONS>& stack) {
   if (p.sEndX != kRight) return;
-  for (int i0 = 0; i0 < p.numActive; i0 += kScanBlock) {
-    uint32_t hb[kScanBlock];
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k) hb[k] = (i0 + k < p.numActive) ? q.getH(i0 + k) : 0u;
-#pragma unroll
-    for (int k = 0; k < kScanBlock; ++k)
-      if (i0 + k < p.numActive) stack.pass(hb[k]);
-  }
+  for (int i = 0; i < p.numActive; ++i) stack.pass(q.getH(i));
   const float nextBreak = cl_min(c.floatHeight, p.pixelY);
   const float activeBottom = q.length() > 0 ? q.get(0).y : FLT_MAX;
   if (activeBottom == p.sEndY) {
@@ -1036,10 +999,6 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       // horizontalAdvance
       float nextX = kRight;
       if (p.current < p.numActive) {
-        if ((p.current & (kScanBlock - 1)) == 0 && p.current + kScanBlock < p.numActive) {
-          prefetchL1(&q.thr[q.start + p.current + kScanBlock]);
-          prefetchL1(&q.hdr[q.start + p.current + kScanBlock]);
-        }
         const float4 t = q.get(p.current);
         const uint32_t h = q.getH(p.current);
         const float yMid = p.sStartY + ((p.sEndY - p.sStartY) * 0.5f);
