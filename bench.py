@@ -750,8 +750,10 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "algorithmic_bytes_per_launch": b_alg,
                 "peak_source": f"{peak_src} (hbm_gbs burst)",
-                "kernel": "raster_columns_kernel (one fused launch per frame)",
-                "note": "the scan is divergent scalar FP32/INT work; SM issue utilisation, not HBM, bounds it"}
+                "kernel": "raster_tiles_kernel (the fast pass: 99.8 % of a frame's device time; the frame's "
+                          "three tile-order kernels and the full-capacity pass are inside the timed step)",
+                "note": "the scan is divergent scalar FP32/INT work in serial per-column chains; SM issue and "
+                        "the longest columns, not HBM, bound it"}
     if prof:
         roofline["profile"] = {k: prof[k] for k in prof if k != "dram_bytes_per_launch"}
 
