@@ -4,7 +4,8 @@
 // to every float of the geometry pile and every solid substance colour.
 //
 // Each column runs twice, start to finish, in one thread:
-//   pass 1  the forward scan, writing I(p) and the pixel's section area sum A(p);
+//   pass 1  the raster kernel's own generate / order / render, writing I(p) and the
+//           pixel's section area sum A(p) instead of bytes;
 //   pass 2  the thresholds are generated again (recomputed, not stored), now with
 //           provenance -- every threshold remembers the line it lies on, whose two end
 //           points are either strand points of the pile or intercepts of a de
@@ -825,7 +826,28 @@ __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti,
                               float4* image, const float4* target, float* gGeo, float* gSub, int& status) {
   const ColumnState c = initColumn(in, ti, column, in.job_index);
   if (!c.active) return false;
-  for (int pass = 0; pass < 2; ++pass) {
+  {
+    // pass 1: the raster kernel's own generate / order / render, writing the float
+    // image (I rgb, section-area sum) instead of bytes
+    Queue q{s.thr, s.hdr, s.cap, s.cap, false};
+    ShapeStack<SECTIONS> stack;
+    stack.clear();
+    const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, s.idx, status);
+    if (q.overflow) return true;
+    sortQueue(q);
+    if (SECTIONS > 1 && bits <= 64) {
+      ShapeStack<1> one;
+      one.clear();
+      one.w[0] = stack.word(0);
+      one.nz = one.w[0] ? 1u : 0u;
+      renderColumn<1>(in, c, q, one, s.idx, status, (int)bits, image);
+    } else {
+      renderColumn<SECTIONS>(in, c, q, stack, s.idx, status, (int)bits, image);
+    }
+    if (q.overflow) return true;
+  }
+  // pass 2: the thresholds again, now with provenance, and the gradients
+  for (int pass = 1; pass < 2; ++pass) {
     AdjQueue q{s.thr, s.hdr, s.prov, s.cap, s.cap, false};
     ShapeStack<SECTIONS> stack;
     stack.clear();

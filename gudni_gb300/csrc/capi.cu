@@ -548,6 +548,8 @@ int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::
   std::memset(&a, 0, sizeof(a));
   a.in = in;
   a.in.counters = nullptr;
+  a.in.stochastic = 0.0f;  // the loss is defined on the deterministic render
+  a.in.random_field = nullptr;
   a.scenes = scenes;
   a.tile_scene = tile_scene;
   a.n_scenes = (uint32_t)n_scenes;

@@ -953,10 +953,12 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 
 // renderThresholdArray K:1978-2028 (calculatePixel K:1881-1916, horizontalAdvance
 // K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
+// `image` (optional): instead of the BGRA word, write each pixel's colour before the
+// byte conversion and its section-area sum as a float4 (the adjoint's forward pass).
 template <int SECTIONS>
 __device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
                                              ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
-                                             int shapeBits) {
+                                             int shapeBits, float4* image = nullptr) {
   Parse p;
   p.current = 0;
   p.numActive = 0;
@@ -971,7 +973,7 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   }
   const int px = c.deltaX;
   int py = c.deltaY;
-  uint32_t* outp = in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
+  uint32_t* outp = image ? nullptr : in.out + (size_t)c.deltaY * (size_t)in.bitmap_w + (size_t)c.deltaX;
   int64_t sections = 0;
   int64_t texels = 0;
   // Section-colour memo, exact: determineColor reads the stack bits from the top
@@ -1035,8 +1037,12 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       ++sections;
     }
     const float r = acc0 / acc4, g = acc1 / acc4, b = acc2 / acc4;
-    *outp = toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
-    outp += in.bitmap_w;
+    if (image) {
+      image[(size_t)py * (size_t)in.bitmap_w + (size_t)px] = make_float4(r, g, b, acc4);
+    } else {
+      *outp = toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
+      outp += in.bitmap_w;
+    }
     p.sStartX = kLeft;
     p.sStartY = p.pixelY;
     py += 1;
