@@ -514,13 +514,25 @@ __device__ __forceinline__ void addY(float4* lg, int32_t src, float g) {
   p[(src & 1) ? 3 : 1] += g;
 }
 
-// Carry a line end point's (gx, gy) to pile floats.
-__device__ __forceinline__ void chainEP(const EP& e, float gx, float gy, const float* pile, float2 d, float* gGeo) {
+// A line end point's (gx, gy) carried to pile floats: up to seven (float index, value)
+// pairs -- a strand point's x and y, or an intercept's x source and the x and y of the
+// three points of its sub-curve.  Unused pairs have index -1.
+constexpr int kEpTargets = 7;
+
+__device__ __forceinline__ void epTargets(const EP& e, float gx, float gy, const float* pile, float2 d,
+                                          int32_t* idx, float* val) {
+#pragma unroll
+  for (int k = 0; k < kEpTargets; ++k) {
+    idx[k] = -1;
+    val[k] = 0.0f;
+  }
   if (gx == 0.0f && gy == 0.0f) return;
   if (e.kind == 0) {
     if (e.pt < 0) return;  // a stand-in end point (never on a kept line)
-    atomicAdd(&gGeo[e.pt], gx);
-    atomicAdd(&gGeo[e.pt + 1], gy);
+    idx[0] = e.pt;
+    val[0] = gx;
+    idx[1] = e.pt + 1;
+    val[1] = gy;
     return;
   }
   const float u0 = 1.0f - e.t0, u1 = 1.0f - e.t1;
@@ -550,12 +562,28 @@ __device__ __forceinline__ void chainEP(const EP& e, float gx, float gy, const f
     dydy1 = u;
     dydxp = m;
   }
-  if (e.pt >= 0) atomicAdd(&gGeo[e.pt], gx + gy * dydxp);
+  if (e.pt >= 0) {
+    idx[0] = e.pt;
+    val[0] = gx + gy * dydxp;
+  }
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    atomicAdd(&gGeo[q[i]], gy * (dydx0 * w0[i] + dydx1 * w1[i]));
-    atomicAdd(&gGeo[q[i] + 1], gy * (dydy0 * w0[i] + dydy1 * w1[i]));
+    idx[1 + 2 * i] = q[i];
+    val[1 + 2 * i] = gy * (dydx0 * w0[i] + dydx1 * w1[i]);
+    idx[2 + 2 * i] = q[i] + 1;
+    val[2 + 2 * i] = gy * (dydy0 * w0[i] + dydy1 * w1[i]);
   }
+}
+
+// Add v to base[idx] for every lane of the (converged, full) warp, one atomic per
+// distinct index: neighbouring columns carry gradient to the same curve points, and
+// aggregating first removes most of the contention on them.  idx < 0: nothing.
+__device__ __forceinline__ void warpAdd(float* base, int32_t idx, float v) {
+  const unsigned peers = __match_any_sync(0xffffffffu, idx);
+  if (idx < 0) return;
+  float sum = 0.0f;
+  for (unsigned p = peers; p != 0u; p &= p - 1u) sum += __shfl_sync(peers, v, __ffs((int)p) - 1);
+  if ((int)(threadIdx.x & 31u) == __ffs((int)peers) - 1 && sum != 0.0f) atomicAdd(&base[idx], sum);
 }
 
 struct AdjSlot {
@@ -821,9 +849,14 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
 }
 
 // one column: float image, then gradients
+// The column's lines and their gradients stay in the slot (nLines, nBits, delta out);
+// the kernel carries them to the pile and the substances for the whole warp at once.
 template <int SECTIONS>
 __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti, int column, const AdjSlot& s,
-                              float4* image, const float4* target, float* gGeo, float* gSub, int& status) {
+                              float4* image, const float4* target, int& nLines, int& nBits, float2& delta,
+                              int& status) {
+  nLines = 0;
+  nBits = 0;
   const ColumnState c = initColumn(in, ti, column, in.job_index);
   if (!c.active) return false;
   {
@@ -870,27 +903,50 @@ __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti,
       scanP<SECTIONS>(in, c, q, s, stack, (int)bits, image, target, pass == 1, status);
     }
     if (q.overflow) return true;
-    if (pass == 1) {
-      const float2 d = make_float2((float)c.deltaX, (float)c.deltaY);
-      const float* pile = reinterpret_cast<const float*>(in.geometry);
-      for (int i = 0; i < n_lines; ++i) {
-        const float4 lg = s.lineGrad[i];
-        chainEP(s.lines[i].a, lg.x, lg.y, pile, d, gGeo);
-        chainEP(s.lines[i].b, lg.z, lg.w, pile, d, gGeo);
-      }
-      for (uint32_t b = 0; b < bits; ++b) {
-        const float4 bg = s.bitGrad[b];
-        if (bg.x == 0.0f && bg.y == 0.0f && bg.z == 0.0f && bg.w == 0.0f) continue;
-        const uint64_t sid = in.shapes[s.idx[b]].tag & GUDNI_TAG_ID_MASK;
-        if (sid >= in.n_substances) continue;
-        atomicAdd(&gSub[4 * sid + 0], bg.x);
-        atomicAdd(&gSub[4 * sid + 1], bg.y);
-        atomicAdd(&gSub[4 * sid + 2], bg.z);
-        atomicAdd(&gSub[4 * sid + 3], bg.w);
-      }
-    }
+    nLines = n_lines;
+    nBits = (int)bits;
+    delta = make_float2((float)c.deltaX, (float)c.deltaY);
   }
   return false;
+}
+
+// Carry every lane's line and colour gradients to the pile and substance gradients;
+// called by the whole warp together.
+__device__ void warpChain(const RasterInputs& in, const AdjSlot& s, int nLines, int nBits, float2 delta,
+                          float* gGeo, float* gSub) {
+  const float* pile = reinterpret_cast<const float*>(in.geometry);
+  const int maxLines = (int)__reduce_max_sync(0xffffffffu, (unsigned)nLines);
+  for (int i = 0; i < maxLines; ++i) {
+    int32_t idx[2 * kEpTargets];
+    float val[2 * kEpTargets];
+    if (i < nLines) {
+      const float4 lg = s.lineGrad[i];
+      epTargets(s.lines[i].a, lg.x, lg.y, pile, delta, idx, val);
+      epTargets(s.lines[i].b, lg.z, lg.w, pile, delta, idx + kEpTargets, val + kEpTargets);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 2 * kEpTargets; ++k) {
+        idx[k] = -1;
+        val[k] = 0.0f;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * kEpTargets; ++k) warpAdd(gGeo, idx[k], val[k]);
+  }
+  const int maxBits = (int)__reduce_max_sync(0xffffffffu, (unsigned)nBits);
+  for (int b = 0; b < maxBits; ++b) {
+    int32_t sub = -1;
+    float4 bg = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (b < nBits) {
+      bg = s.bitGrad[b];
+      const uint64_t sid = in.shapes[s.idx[b]].tag & GUDNI_TAG_ID_MASK;
+      if ((bg.x != 0.0f || bg.y != 0.0f || bg.z != 0.0f || bg.w != 0.0f) && sid < in.n_substances) sub = (int32_t)sid;
+    }
+    warpAdd(gSub, sub < 0 ? -1 : 4 * sub + 0, bg.x);
+    warpAdd(gSub, sub < 0 ? -1 : 4 * sub + 1, bg.y);
+    warpAdd(gSub, sub < 0 ? -1 : 4 * sub + 2, bg.z);
+    warpAdd(gSub, sub < 0 ? -1 : 4 * sub + 3, bg.w);
+  }
 }
 
 }  // namespace
@@ -933,11 +989,14 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
     const size_t base = a.scenes ? (size_t)a.scenes[a.tile_scene[tile]].out_offset : 0;
     const int tpt = 1 << in.log2_tpt;
     const int column = chunk * 32 + lane;
+    int nLines = 0, nBits = 0;
+    float2 delta = make_float2(0.0f, 0.0f);
     if (column < tpt) {
-      if (adjointColumn<SECTIONS>(in, ti, column, s, a.image + base, a.target + base, a.grad_geometry,
-                                  a.grad_substances, status))
+      if (adjointColumn<SECTIONS>(in, ti, column, s, a.image + base, a.target + base, nLines, nBits, delta,
+                                  status))
         status |= kStatusOverflow;
     }
+    warpChain(in, s, nLines, nBits, delta, a.grad_geometry, a.grad_substances);  // all 32 lanes
   }
   if (status) atomicOr(a.status, status);
 }
