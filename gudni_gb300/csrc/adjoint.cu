@@ -94,6 +94,73 @@ struct AdjQueue {
     hdr[to] = hdr[from];
     prov[to] = prov[from];
   }
+  // sliceActive of the first n (active) entries at sp: the part above stays in place,
+  // the part below (when kept) is inserted as insertThreshold would; the same batched
+  // form as the forward scan's splitNext (parts collected below the queue, the active
+  // block moved once, the parts walked in past it) when every active top is below sp
+  // and the slab has room.  y sources: the split point's for the new bottom / top.
+  __device__ __forceinline__ void splitActive(int n, float sp, int32_t spSrc) {
+    bool batched = start >= 2 * n;
+    for (int i = 0; batched && i < n; ++i) batched = thr[start + i].x < sp;
+    const int s0 = start;
+    int m = 0;
+    for (int cur = 0; cur < n; ++cur) {
+      const int at = batched ? s0 + cur : start + cur;
+      const uint32_t ch = hdr[at];
+      const float4 e = thr[at];
+      const int4 pv = prov[at];
+      if (e.x < sp && sp < e.y) {
+        const float splitX = intersectX(ch, e, sp);
+        float4 lo, hi;
+        uint32_t lh, hh;
+        if (hPositive(ch)) {
+          lo = make_float4(sp, e.y, splitX, e.w);
+          hi = make_float4(e.x, sp, e.z, splitX);
+          lh = ch & kUnpersist;
+          hh = ch;
+        } else {
+          lo = make_float4(sp, e.y, e.z, splitX);
+          hi = make_float4(e.x, sp, splitX, e.w);
+          lh = ch;
+          hh = ch & kUnpersist;
+        }
+        hdr[at] = hh;
+        thr[at] = hi;
+        prov[at] = make_int4(pv.x, pv.y, spSrc, 0);
+        if (tKeep(lh, lo)) {
+          const int4 lp = make_int4(pv.x, spSrc, pv.z, 0);
+          if (batched) {
+            hdr[s0 - n - 1 - m] = lh;
+            thr[s0 - n - 1 - m] = lo;
+            prov[s0 - n - 1 - m] = lp;
+            ++m;
+          } else {
+            insert(lh, lo, lp);
+            if (overflow) return;
+          }
+        }
+      }
+    }
+    if (!batched || m == 0) return;
+    for (int i = 0; i < n; ++i) move(s0 - m + i, s0 + i);
+    start = s0 - m;
+    int f = s0 + n;
+    for (int j = 0; j < m; ++j) {
+      const int src = s0 - n - 1 - j;
+      const uint32_t h = hdr[src];
+      const float4 t = thr[src];
+      const int4 pv = prov[src];
+      f -= 1;
+      int at = f;
+      while (at + 1 < cap && isBelow(h, t, hdr[at + 1], thr[at + 1])) {
+        move(at, at + 1);
+        at += 1;
+      }
+      hdr[at] = h;
+      thr[at] = t;
+      prov[at] = pv;
+    }
+  }
   // stable sort (the order the forward pass's sort produces): bottom-up merge sort
   // through the free slab space below the queue when it has room, else insertion sort
   __device__ __forceinline__ void sort() {
@@ -718,34 +785,8 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
               sp = sp2;
               spSrc = sp2Src;
             }
-            for (int cur = 0; cur < n; ++cur) {
-              const uint32_t ch = q.hdr[q.start + cur];
-              const float4 e = q.thr[q.start + cur];
-              const int4 pv = q.prov[q.start + cur];
-              if (e.x < sp && sp < e.y) {
-                const float splitX = intersectX(ch, e, sp);
-                float4 lo, hi;
-                uint32_t lh, hh;
-                if (hPositive(ch)) {
-                  lo = make_float4(sp, e.y, splitX, e.w);
-                  hi = make_float4(e.x, sp, e.z, splitX);
-                  lh = ch & kUnpersist;
-                  hh = ch;
-                } else {
-                  lo = make_float4(sp, e.y, e.z, splitX);
-                  hi = make_float4(e.x, sp, splitX, e.w);
-                  lh = ch;
-                  hh = ch & kUnpersist;
-                }
-                q.hdr[q.start + cur] = hh;
-                q.thr[q.start + cur] = hi;
-                q.prov[q.start + cur] = make_int4(pv.x, pv.y, spSrc, 0);
-                if (tKeep(lh, lo)) {
-                  q.insert(lh, lo, make_int4(pv.x, spSrc, pv.z, 0));
-                  if (q.overflow) return;
-                }
-              }
-            }
+            q.splitActive(n, sp, spSrc);
+            if (q.overflow) return;
             const bool brk = sp < nextBreak;
             nextBottom = brk ? sp : nextBreak;
             nextSrc = brk ? spSrc : kConst;
