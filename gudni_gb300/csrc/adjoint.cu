@@ -668,8 +668,9 @@ struct AdjSlot {
   int layerCap;
 };
 
-// The scan of K:1744-2028.  grad == false: write I(p), A(p) to `image`.  grad ==
-// true: read them back and accumulate gradients.
+// The scan of K:1744-2028 with provenance.  grad == true (the kernel's second pass):
+// read I(p), A(p) back from `image` and accumulate gradients; grad == false writes
+// them instead (the kernel's first pass uses the raster scan for that).
 template <int SECTIONS>
 __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState& c, AdjQueue& q, const AdjSlot& s,
                                       ShapeStack<SECTIONS>& stack, int bits, float4* image, const float4* target,
@@ -921,33 +922,29 @@ __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti,
     if (q.overflow) return true;
   }
   // pass 2: the thresholds again, now with provenance, and the gradients
-  for (int pass = 1; pass < 2; ++pass) {
-    AdjQueue q{s.thr, s.hdr, s.prov, s.cap, s.cap, false};
-    ShapeStack<SECTIONS> stack;
-    stack.clear();
-    int n_lines = 0;
-    AdjGen g{&q, s.lines, &n_lines, s.cap, &c};
-    const uint32_t bits = generateP<SECTIONS>(in, c, g, stack, s.idx, status);
-    if (q.overflow) return true;
-    q.sort();
-    if (pass == 1) {
-      for (int i = 0; i < n_lines; ++i) s.lineGrad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      for (uint32_t b = 0; b < bits; ++b) s.bitGrad[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    }
-    if (SECTIONS > 1 && bits <= 64) {  // as the forward scan: a one-word stack
-      ShapeStack<1> one;
-      one.clear();
-      one.w[0] = stack.word(0);
-      one.nz = one.w[0] ? 1u : 0u;
-      scanP<1>(in, c, q, s, one, (int)bits, image, target, pass == 1, status);
-    } else {
-      scanP<SECTIONS>(in, c, q, s, stack, (int)bits, image, target, pass == 1, status);
-    }
-    if (q.overflow) return true;
-    nLines = n_lines;
-    nBits = (int)bits;
-    delta = make_float2((float)c.deltaX, (float)c.deltaY);
+  AdjQueue q{s.thr, s.hdr, s.prov, s.cap, s.cap, false};
+  ShapeStack<SECTIONS> stack;
+  stack.clear();
+  int n_lines = 0;
+  AdjGen g{&q, s.lines, &n_lines, s.cap, &c};
+  const uint32_t bits = generateP<SECTIONS>(in, c, g, stack, s.idx, status);
+  if (q.overflow) return true;
+  q.sort();
+  for (int i = 0; i < n_lines; ++i) s.lineGrad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (uint32_t b = 0; b < bits; ++b) s.bitGrad[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (SECTIONS > 1 && bits <= 64) {  // as the forward scan: a one-word stack
+    ShapeStack<1> one;
+    one.clear();
+    one.w[0] = stack.word(0);
+    one.nz = one.w[0] ? 1u : 0u;
+    scanP<1>(in, c, q, s, one, (int)bits, image, target, true, status);
+  } else {
+    scanP<SECTIONS>(in, c, q, s, stack, (int)bits, image, target, true, status);
   }
+  if (q.overflow) return true;
+  nLines = n_lines;
+  nBits = (int)bits;
+  delta = make_float2((float)c.deltaX, (float)c.deltaY);
   return false;
 }
 
