@@ -17,9 +17,10 @@ from . import lib as L
 from . import scene as S
 
 # (tile size, threads per tile); threads per tile must be >= tile size.  More threads
-# per tile make shorter columns (more parallel work, more threshold generation);
-# smaller tiles give each column fewer shapes.
-CANDIDATES: Tuple[Tuple[int, int], ...] = ((8, 32), (16, 64), (32, 256))
+# per tile make shorter columns (more parallel work, more threshold generation; an
+# 8-pixel tile with 64 threads has one-pixel columns); smaller tiles give each column
+# fewer shapes.
+CANDIDATES: Tuple[Tuple[int, int], ...] = ((8, 32), (8, 64), (16, 64), (32, 256))
 BUCKETS: Tuple[int, ...] = (96, 192, 384, 768, 1 << 30)  # upper bound of max(canvas side)
 
 

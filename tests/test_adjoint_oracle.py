@@ -133,3 +133,17 @@ def test_pair_gradient_sums_knob_splits():
     # only point floats move (headers and sizes are equal bit patterns)
     lhs = float(np.dot(g, np.nan_to_num(d)))
     assert abs(lhs - gp[p, c] * e) <= 1e-4 * max(1.0, abs(lhs))
+
+
+def test_adam_step_matches_the_textbook_update():
+    """fit.Adam: bias-corrected first and second moments (Kingma & Ba, Algorithm 1)."""
+    from gudni_gb300.fit import Adam
+    opt = Adam(lr=0.1)
+    x = np.array([1.0, -2.0])
+    g1, g2 = np.array([0.5, -1.0]), np.array([0.25, 2.0])
+    x1 = opt.step(x, g1)
+    np.testing.assert_allclose(x1, x - 0.1 * np.sign(g1), rtol=1e-6)  # first step: lr * g / |g|
+    m = 0.9 * 0.1 * g1 + 0.1 * g2
+    v = 0.999 * 0.001 * g1 ** 2 + 0.001 * g2 ** 2
+    mh, vh = m / (1 - 0.9 ** 2), v / (1 - 0.999 ** 2)
+    np.testing.assert_allclose(opt.step(x1, g2), x1 - 0.1 * mh / (np.sqrt(vh) + 1e-8), rtol=1e-9)
