@@ -48,7 +48,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 UNIT = "Mpixels/s"
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "raster_columns_{}.json")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "raster_tiles_{}.json")
 
 
 def parse():
