@@ -618,12 +618,10 @@ def main():
 
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from gudni_gb300 import replicas as R
+
+    rank, world, local = R.ranks()
+    R.init(world, "nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
@@ -665,9 +663,7 @@ def main():
     r.sync_status()
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        R.barrier(world)
 
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -685,14 +681,9 @@ def main():
     launches = r.launch_count() - launches0
     r.sync_status()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = R.max_over_ranks(sum(step_ms) / len(step_ms), world, dev)
     pixels = frame.canvas_w * frame.canvas_h
-    value = world * pixels / (ms / 1000) / 1e6
+    value = R.job_rate(pixels, world, ms / 1000) / 1e6
 
     # end to end through the frame-level C ABI with pinned host buffers
     def pinned(a):
@@ -726,12 +717,7 @@ def main():
         t0 = time.perf_counter()
         r.raster_frame(hframe, out=out_np)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_times) / len(e2e_times)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = R.max_over_ranks(sum(e2e_times) / len(e2e_times), world, dev)
     h2d = (frame.geometry.nbytes + frame.substances.nbytes + frame.pictures.nbytes + frame.picture_uses.nbytes +
            frame.radials.nbytes + frame.random_field.nbytes + shapes.nbytes + tiles.nbytes + tile_jobs.nbytes)
     e2e = {"value": world * pixels / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -82,3 +82,15 @@ def test_batch_per_scene_launches_match_oracle(monkeypatch):
         imgs = batch.images(r.download())
     for f, img in zip(frames, imgs):
         assert np.array_equal(img, O.render_frame(f))
+
+
+def test_autotune_buckets_and_tuned_specs():
+    """Scenes fall into canvas-size buckets by their longer side; serialize_tuned gives
+    every scene its bucket's (tile, threads per tile)."""
+    from gudni_gb300 import autotune as A
+    assert [A.bucket_of(w, h) for w, h in ((64, 64), (96, 40), (97, 10), (300, 500), (1024, 64))] == [0, 0, 1, 3, 4]
+    flats = [G.random_shapes(seed=i, width=w, height=h, n_shapes=4) for i, (w, h) in enumerate(((64, 80), (200, 150)))]
+    frames = A.serialize_tuned(flats, {0: (8, 64), 2: (16, 64)}, 127, 4096, 1 << 24)
+    assert (frames[0].spec.max_tile_size, frames[0].spec.threads_per_tile) == (8, 64)
+    assert (frames[1].spec.max_tile_size, frames[1].spec.threads_per_tile) == (16, 64)
+    assert A.scene_cost(flats[1]) == 200 * 150 * 4
