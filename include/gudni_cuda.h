@@ -252,7 +252,9 @@ int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
  * (geometry_bytes/4 floats) and `grad_substances` (4 floats per substance) are ADDED
  * to.  Thresholds are recomputed in the backward pass, not stored.  A column that
  * needs more than the adjoint's working capacity (min(max_thresholds, 1024), or
- * GUDNI_ADJOINT_CAPACITY) raises GUDNI_ERR_THRESHOLD_OVERFLOW. */
+ * GUDNI_ADJOINT_CAPACITY) raises GUDNI_ERR_THRESHOLD_OVERFLOW.  The stochastic area
+ * jitter (STOCHASTIC_FACTOR) is off in the adjoint: the loss is defined on the
+ * deterministic render. */
 int gudni_adjoint_tiles_device(gudni_ctx* ctx,
                                const gudni_shape* shapes, size_t n_shapes,
                                const gudni_tile_info* tiles, const int32_t* tile_jobs, size_t n_tiles,
