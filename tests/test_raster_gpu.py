@@ -142,3 +142,38 @@ def test_device_pointer_path():
         torch.cuda.synchronize()
     got = out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
     assert np.array_equal(got, want)
+
+
+def _poly(points, color):
+    o = S.segments_to_outline([S.straight(x, y) for x, y in points])
+    return S.solid(color, S.shape([o]))
+
+
+def test_shapes_far_above_and_below_the_columns():
+    """Shapes whose strands lie wholly above or below most columns (the generation's
+    y culling and its enclosure-only path): a tall canvas-spanning diamond and a
+    rectangle reaching far past the canvas, over and under smaller shapes."""
+    items = [
+        _poly([(-50, -4000), (130, 60), (-50, 4000), (-60, 60)], (0.9, 0.2, 0.1, 0.7)),
+        _poly([(20, -9000), (100, -9000), (100, 9000), (20, 9000)], (0.1, 0.6, 0.3, 0.6)),
+        _poly([(10, 10), (40, 12), (30, 50)], (0.2, 0.2, 0.9, 1.0)),
+        _poly([(60, 90), (110, 70), (90, 110)], (0.8, 0.8, 0.1, 0.5)),
+    ]
+    scene = S.Scene((1, 1, 1, 1), S.overlap(items))
+    for tile, tpt in ((32, 32), (16, 64), (8, 32)):
+        frame = S.serialize(scene, 128, 120, L.make_spec(tile, tpt, 4096, 127, 8))
+        assert_parity(render(frame), O.render_frame(frame))
+
+
+def test_non_finite_control_points_match_the_oracle():
+    """NaN and +inf coordinates reach the kernels' comparisons (the culling and the
+    batched insertion fall back to the literal path there); the image must still
+    match the oracle's.  (A -inf x makes the reference's unbounded de Casteljau loop,
+    Kernels.cl:1233-1258, run forever; the kernels stop after 96 halvings and report
+    GUDNI_ERR_ITER_LIMIT, so there is no image to compare.)"""
+    flat = G.random_shapes(seed=77, width=96, height=80, n_shapes=10)
+    flat.pairs = flat.pairs.copy()
+    flat.pairs[3, 1] = np.nan
+    flat.pairs[17, 2] = np.inf
+    frame = S.serialize_flat(flat, L.make_spec(16, 32, 4096, 127, 8))
+    assert_parity(render(frame), O.render_frame(frame))
