@@ -57,8 +57,19 @@ def defines(max_shape: int, sections: int, stochastic: float) -> list[str]:
     ]
 
 
-def library_name(max_shape: int, sections: int) -> str:
-    return os.path.join(OUT_DIR, f"libgudni_ref_m{max_shape}_s{sections}.so")
+def variant(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
+    """File-name tag of one compile-time configuration (MAXSHAPE, SHAPESTACKSECTIONS,
+    STOCHASTIC_FACTOR)."""
+    tag = f"m{max_shape}_s{sections}"
+    return tag if stochastic == 0.0 else f"{tag}_st{stochastic!r}"
+
+
+def library_name(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
+    return os.path.join(OUT_DIR, f"libgudni_ref_{variant(max_shape, sections, stochastic)}.so")
+
+
+def source_name(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
+    return os.path.join(OUT_DIR, f"ref_kernels_{variant(max_shape, sections, stochastic)}.cpp")
 
 
 def generate(reference: str, max_shape: int, sections: int, stochastic: float = 0.0) -> str:
@@ -71,23 +82,24 @@ def generate(reference: str, max_shape: int, sections: int, stochastic: float = 
     body = VECTOR_LITERAL.sub(lambda m: f"ocl_make<{m.group(1)}>(", body)
     text = "\n".join(head) + "\n" + body + '\n#include "ref_driver.inc"\n'
     os.makedirs(OUT_DIR, exist_ok=True)
-    out = os.path.join(OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp")
+    out = source_name(max_shape, sections, stochastic)
     with open(out, "w") as f:
         f.write(text)
     return out
 
 
 def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: int = 8,
-          force: bool = False) -> str | None:
-    """Build the reference kernels for one (MAXSHAPE, SHAPESTACKSECTIONS) pair.
-    Returns the library path, or None when the reference checkout is absent."""
-    lib = library_name(max_shape, sections)
-    cpp = os.path.join(OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp")
+          force: bool = False, stochastic: float = 0.0) -> str | None:
+    """Build the reference kernels for one (MAXSHAPE, SHAPESTACKSECTIONS,
+    STOCHASTIC_FACTOR) configuration.  Returns the library path, or None when neither
+    the reference checkout nor a translation unit generated from it is present."""
+    lib = library_name(max_shape, sections, stochastic)
+    cpp = source_name(max_shape, sections, stochastic)
     deps = [os.path.join(HERE, "ref_driver.inc"), os.path.join(HERE, "ref_shim.h")]
     if os.path.isfile(lib) and not force and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in deps):
         return lib
     if os.path.isfile(os.path.join(reference, KERNELS_REL)):
-        cpp = generate(reference, max_shape, sections)
+        cpp = generate(reference, max_shape, sections, stochastic)
     elif not os.path.isfile(cpp):
         # neither the reference checkout nor a translation unit generated from it
         return None

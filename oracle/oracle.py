@@ -94,18 +94,18 @@ def render_frame(frame, n_threads: int = 0, max_thresholds: Optional[int] = None
     return out
 
 
-def ref_available(max_shape: int = 127, sections: int = 8) -> bool:
+def ref_available(max_shape: int = 127, sections: int = 8, stochastic: float = 0.0) -> bool:
     from . import build_ref
-    return (os.path.isfile(build_ref.library_name(max_shape, sections))
-            or os.path.isfile(os.path.join(build_ref.OUT_DIR, f"ref_kernels_m{max_shape}_s{sections}.cpp"))
+    return (os.path.isfile(build_ref.library_name(max_shape, sections, stochastic))
+            or os.path.isfile(build_ref.source_name(max_shape, sections, stochastic))
             or os.path.isfile(os.path.join(build_ref.DEFAULT_REFERENCE, build_ref.KERNELS_REL)))
 
 
-def _load_ref(max_shape: int, sections: int):
-    key = (max_shape, sections)
+def _load_ref(max_shape: int, sections: int, stochastic: float = 0.0):
+    key = (max_shape, sections, stochastic)
     if key not in _ref_libs:
         from . import build_ref
-        path = build_ref.build(max_shape=max_shape, sections=sections)
+        path = build_ref.build(max_shape=max_shape, sections=sections, stochastic=stochastic)
         if path is None or not os.path.isfile(path):
             raise FileNotFoundError("reference kernels not built (no reference checkout)")
         lib = C.CDLL(path)
@@ -121,7 +121,7 @@ def _load_ref(max_shape: int, sections: int):
 def ref_render_frame(frame, max_thresholds: int, n_threads: int = 0) -> np.ndarray:
     """Rasterize with the reference's own Kernels.cl (compiled for the CPU)."""
     spec = frame.spec
-    lib = _load_ref(spec.max_shape, spec.stack_sections)
+    lib = _load_ref(spec.max_shape, spec.stack_sections, float(np.float32(spec.stochastic_factor)))
     out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
     bg = np.ascontiguousarray(frame.background, dtype=np.float32)
     for ji, job in enumerate(frame.jobs):
