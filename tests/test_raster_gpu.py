@@ -177,3 +177,16 @@ def test_non_finite_control_points_match_the_oracle():
     flat.pairs[17, 2] = np.inf
     frame = S.serialize_flat(flat, L.make_spec(16, 32, 4096, 127, 8))
     assert_parity(render(frame), O.render_frame(frame))
+
+
+@pytest.mark.parametrize("tile,tpt", [(32, 32), (8, 64)])
+def test_dense_canvas_wide_shapes(tile, tpt):
+    """220 canvas-wide shapes on 160x120 (the batched mix's generator at its dense
+    end): hundreds of thresholds and shape bits per column, so the multi-word stack,
+    the batched and merged insertion of split parts and the opaque-cut memo all run."""
+    flat = G.random_shapes(seed=91, width=160, height=120, n_shapes=220)
+    frame = S.serialize_flat(flat, L.make_spec(tile, tpt, 4096, 255, 4, max_strands_per_tile=1 << 24))
+    got = render(frame)
+    want = O.render_frame(frame)
+    assert_parity(got, want)
+    assert np.array_equal(got, want)
