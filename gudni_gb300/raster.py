@@ -99,7 +99,10 @@ class Rasterizer:
 
     def raster_tiles_device(self, frame, shapes_ptr: int, n_shapes: int, tiles_ptr: int, tile_jobs_ptr: int,
                             n_tiles: int, out_ptr: int, stream: int = 0, frame_number: int = 0) -> None:
-        """Enqueue a whole frame whose concatenated piles are device-resident."""
+        """Enqueue a whole frame whose concatenated piles are device-resident
+        (scene.concatenated_piles layout).  `stream`: a CUDA stream handle; 0 means the
+        context's own non-blocking stream (lib.current_stream_handle() gives torch's
+        current stream, the legacy default stream included)."""
         bg = np.ascontiguousarray(frame.background, np.float32)
         self._check(self.lib.gudni_raster_tiles_device(
             self.ctx, shapes_ptr, n_shapes, tiles_ptr, tile_jobs_ptr or None, n_tiles, frame.canvas_w,
@@ -118,7 +121,8 @@ class Rasterizer:
 
     def raster_job_device(self, frame, job_index: int, shapes_ptr: int, tiles_ptr: int, out_ptr: int,
                           stream: int = 0, frame_number: int = 0) -> None:
-        """Enqueue one job with device-resident shapes/tiles/out (torch data_ptr()s)."""
+        """Enqueue one job with device-resident shapes/tiles/out (torch data_ptr()s) on
+        `stream` (0: the context's own stream; see raster_tiles_device)."""
         job = frame.jobs[job_index]
         bg = np.ascontiguousarray(frame.background, np.float32)
         self._check(self.lib.gudni_raster_job_device(
