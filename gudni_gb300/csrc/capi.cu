@@ -25,6 +25,7 @@
 #include "adjoint_kernels.h"
 #include "gudni_cuda.h"
 #include "raster_kernels.h"
+#include "strand_table.h"
 
 using gudni::TileLaunch;
 
@@ -424,49 +425,12 @@ int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_
   return GUDNI_OK;
 }
 
-// Walk the geometry pile strand by strand from its first byte (the pile is the
-// strands of every shape back to back: Raster/Serialize.hs:76-84, Enclosure.hs:76-80)
-// and record each strand's offset, size and the left/right x its range test reads.
-// The walk stops at the first malformed header; shapes starting past that point keep
-// the kernel's checked per-strand path.
+// The strand table of the uploaded pile (strand_table.h), uploaded beside it.
 int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes) {
+  static_assert(gudni::kNoStrandIndex == gudni::kNoStrand, "one marker for units without a strand");
   ctx->n_strands = 0;
   ctx->n_units = bytes / 16;
-  ctx->h_strand_table.clear();
-  ctx->h_strand_y.clear();
-  ctx->h_strand_first.assign(ctx->n_units, gudni::kNoStrand);
-  size_t off = 0;
-  while (off + 32 <= bytes) {
-    uint16_t size;
-    std::memcpy(&size, geo + off, 2);
-    if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > bytes) break;
-    if (ctx->h_strand_table.size() >= 0xFFFFFFF0ull || off / 8 > 0xFFFFFFFFull) break;
-    uint32_t lx, rx;
-    std::memcpy(&rx, geo + off + 8, 4);
-    std::memcpy(&lx, geo + off + 16, 4);
-    if (off % 16 == 0) ctx->h_strand_first[off / 16] = (uint32_t)ctx->h_strand_table.size();
-    ctx->h_strand_table.push_back(make_uint4((uint32_t)(off / 8), size, lx, rx));
-    // y range of every point of the strand (right end, left end and its control,
-    // then each tree node's point and control); NaN disables culling for the strand
-    float lo = INFINITY, hi = -INFINITY;
-    bool nan = false;
-    auto take = [&](size_t at) {
-      float y;
-      std::memcpy(&y, geo + off + at, 4);
-      if (y != y) nan = true;
-      lo = std::min(lo, y);
-      hi = std::max(hi, y);
-    };
-    take(12);
-    take(20);
-    take(28);
-    for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
-      take(node + 4);
-      take(node + 12);
-    }
-    ctx->h_strand_y.push_back(nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi));
-    off += (size_t)size * 8;
-  }
+  gudni::build_strand_table(geo, bytes, ctx->h_strand_table, ctx->h_strand_y, ctx->h_strand_first);
   int rc;
   if ((rc = upload(ctx, ctx->strand_table, ctx->h_strand_table.data(), ctx->h_strand_table.size(), "strand table")))
     return rc;

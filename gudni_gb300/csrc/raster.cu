@@ -33,36 +33,6 @@
 
 namespace gudni {
 
-// One column, start to finish.  Returns true when the queue overflowed `cap`.
-template <int SECTIONS>
-__device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_tile_info& ti, int column,
-                                          float4* thr, uint32_t* hdr, int cap, uint32_t* idx, int& status) {
-  const ColumnState c = initColumn(in, ti, column, in.job_index);
-  if (!c.active) return false;
-  Queue q{thr, hdr, cap, cap, false};
-  ShapeStack<SECTIONS> stack;
-  stack.clear();
-  const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, idx, status);
-  if (q.overflow) return true;
-  sortQueue(q);
-  if (in.counters) {
-    atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[2]), (unsigned long long)q.length());
-    atomicMax(reinterpret_cast<unsigned long long*>(&in.counters[3]), (unsigned long long)bits);
-  }
-  if (SECTIONS > 1 && bits <= 64) {
-    // every shape bit of the column sits in the first stack word: scan with a
-    // one-word stack (flips and findTop on a single register)
-    ShapeStack<1> one;
-    one.clear();
-    one.w[0] = stack.word(0);
-    one.nz = one.w[0] ? 1u : 0u;
-    renderColumn<1>(in, c, q, one, idx, status, (int)bits);
-  } else {
-    renderColumn<SECTIONS>(in, c, q, stack, idx, status, (int)bits);
-  }
-  return q.overflow;
-}
-
 template <int SECTIONS>
 __global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a) {
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;

@@ -1,0 +1,63 @@
+// The strand table of a geometry pile (host code; shared by the C ABI and tests).
+//
+// The pile is the strands of every shape back to back (Raster/Serialize.hs:76-84,
+// Enclosure.hs:76-80).  One walk from its first byte records, per strand, its offset
+// (8-byte units), size, the left and right x its range test reads (checkInRange,
+// Kernels.cl:1360-1363) and the y range of all its points, and, per 16-byte unit of
+// the pile, the index of the strand starting there.  The walk stops at the first
+// malformed header; shapes starting past that point keep the kernel's checked
+// per-strand path.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace gudni {
+
+constexpr uint32_t kNoStrandIndex = 0xFFFFFFFFu;  // no strand starts at this unit
+
+inline void build_strand_table(const uint8_t* geo, size_t bytes, std::vector<uint4>& table, std::vector<float2>& ys,
+                               std::vector<uint32_t>& first) {
+  table.clear();
+  ys.clear();
+  first.assign(bytes / 16, kNoStrandIndex);
+  size_t off = 0;
+  while (off + 32 <= bytes) {
+    uint16_t size;
+    std::memcpy(&size, geo + off, 2);
+    if (size < 4 || (size & 1u) != 0 || off + (size_t)size * 8 > bytes) break;
+    if (table.size() >= 0xFFFFFFF0ull || off / 8 > 0xFFFFFFFFull) break;
+    uint32_t lx, rx;
+    std::memcpy(&rx, geo + off + 8, 4);
+    std::memcpy(&lx, geo + off + 16, 4);
+    if (off % 16 == 0) first[off / 16] = (uint32_t)table.size();
+    table.push_back(make_uint4((uint32_t)(off / 8), size, lx, rx));
+    // y range of every point of the strand (right end, left end and its control,
+    // then each tree node's point and control); NaN disables culling for the strand
+    float lo = INFINITY, hi = -INFINITY;
+    bool nan = false;
+    auto take = [&](size_t at) {
+      float y;
+      std::memcpy(&y, geo + off + at, 4);
+      if (y != y) nan = true;
+      lo = std::min(lo, y);
+      hi = std::max(hi, y);
+    };
+    take(12);
+    take(20);
+    take(28);
+    for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
+      take(node + 4);
+      take(node + 12);
+    }
+    ys.push_back(nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi));
+    off += (size_t)size * 8;
+  }
+}
+
+}  // namespace gudni

@@ -1,0 +1,29 @@
+"""Build recipe of the host-compiled column machine (test infrastructure)."""
+import ctypes as C
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+SRC = os.path.join(HERE, "host_column.cpp")
+OUT = os.path.join(HERE, "_build", "libhost_column.so")
+DEPS = [SRC] + [os.path.join(ROOT, "gudni_gb300", "csrc", f) for f in ("raster_device.cuh", "strand_table.h")] + [
+    os.path.join(ROOT, "include", "gudni_cuda.h")]
+CUDA_INCLUDE = "/usr/local/cuda/include"
+
+
+def build() -> str:
+    if not os.path.isfile(OUT) or max(os.path.getmtime(d) for d in DEPS) > os.path.getmtime(OUT):
+        os.makedirs(os.path.dirname(OUT), exist_ok=True)
+        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fPIC", "-shared",
+                        "-w", "-I", CUDA_INCLUDE, "-I", os.path.join(ROOT, "include"), SRC, "-o", OUT], check=True)
+    return OUT
+
+
+def load():
+    lib = C.CDLL(build())
+    vp, sz, i = C.c_void_p, C.c_size_t, C.c_int
+    lib.host_column_raster_job.restype = C.c_int
+    lib.host_column_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
+                                           i, vp, C.POINTER(C.c_int)]
+    return lib

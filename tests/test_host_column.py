@@ -1,0 +1,80 @@
+"""The product's device column machine, compiled for the host CPU
+(tests/host_column), against the oracle: the exact-arithmetic transformations of the
+CUDA path (strand-table range test and y culling, batched and merged insertion of
+split parts, opaque-cut colour memo, one-word and multi-word stacks) checked without a
+GPU, on sparse, dense and degenerate scenes."""
+import ctypes as C
+import os
+import shutil
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from gudni_gb300 import lib as L  # noqa: E402
+from gudni_gb300 import scene as S  # noqa: E402
+from gudni_gb300 import scenes as G  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+pytestmark = pytest.mark.skipif(shutil.which("g++") is None or not os.path.isdir("/usr/local/cuda/include"),
+                                reason="needs g++ and the CUDA headers")
+
+
+def host_render(frame) -> np.ndarray:
+    from host_column.build import load
+    lib = load()
+    out = np.zeros((frame.canvas_h, frame.canvas_w), np.uint32)
+    bg = np.ascontiguousarray(frame.background, np.float32)
+    p = L.ptr
+    for ji, job in enumerate(frame.jobs):
+        ov = C.c_int(0)
+        st = lib.host_column_raster_job(p(frame.geometry), frame.geometry.size, p(frame.substances),
+                                        len(frame.substances), p(frame.pictures), frame.pictures.size,
+                                        p(frame.picture_uses), len(frame.picture_uses), p(frame.radials),
+                                        len(frame.radials), p(job.shapes), len(job.shapes), p(job.tiles),
+                                        len(job.tiles), frame.compute_depth, frame.canvas_w, frame.canvas_h, ji,
+                                        bg.ctypes.data, frame.spec.max_thresholds, frame.spec.max_shape,
+                                        out.ctypes.data, C.byref(ov))
+        assert st == 0 and ov.value == 0, (st, ov.value)
+    return out
+
+
+def check(frame):
+    got, want = host_render(frame), O.render_frame(frame)
+    assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+
+
+@pytest.mark.parametrize("tile,tpt", [(32, 32), (16, 64), (8, 32)])
+def test_random_scene(tile, tpt):
+    check(S.serialize_flat(G.random_shapes(seed=5, width=160, height=120, n_shapes=40),
+                           L.make_spec(tile, tpt, 4096, 127, 8)))
+
+
+@pytest.mark.parametrize("tile,tpt", [(32, 32), (8, 64)])
+def test_dense_canvas_wide_shapes(tile, tpt):
+    """Hundreds of thresholds and shape bits per column: multi-word stack, batched and
+    merged insertion of split parts."""
+    flat = G.random_shapes(seed=91, width=160, height=120, n_shapes=220)
+    check(S.serialize_flat(flat, L.make_spec(tile, tpt, 4096, 255, 4, max_strands_per_tile=1 << 24)))
+
+
+def test_very_dense_small_canvas():
+    """The batched mix's densest corner: a small canvas crossed by many shapes."""
+    flat = G.random_shapes(seed=9, width=48, height=40, n_shapes=300, seg_lo=8, seg_hi=32)
+    check(S.serialize_flat(flat, L.make_spec(8, 64, 8192, 511, 8, max_strands_per_tile=1 << 24)))
+
+
+def test_glyph_page_all_substances():
+    flat = G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25)
+    check(S.serialize_flat(flat, L.make_spec(32, 32, 4096, 511, 8)))
+
+
+def test_non_finite_points():
+    flat = G.random_shapes(seed=77, width=96, height=80, n_shapes=10)
+    flat.pairs = flat.pairs.copy()
+    flat.pairs[3, 1] = np.nan
+    flat.pairs[17, 2] = np.inf
+    check(S.serialize_flat(flat, L.make_spec(16, 32, 4096, 127, 8)))
