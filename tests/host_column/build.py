@@ -7,7 +7,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 SRC = os.path.join(HERE, "host_column.cpp")
 OUT = os.path.join(HERE, "_build", "libhost_column.so")
-DEPS = [SRC] + [os.path.join(ROOT, "gudni_gb300", "csrc", f) for f in ("raster_device.cuh", "strand_table.h")] + [
+DEPS = [SRC] + [os.path.join(ROOT, "gudni_gb300", "csrc", f) for f in ("raster_device.cuh", "adjoint_device.cuh", "strand_table.h")] + [
     os.path.join(ROOT, "include", "gudni_cuda.h")]
 CUDA_INCLUDE = "/usr/local/cuda/include"
 
@@ -26,4 +26,7 @@ def load():
     lib.host_column_raster_job.restype = C.c_int
     lib.host_column_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
                                            i, vp, C.POINTER(C.c_int)]
+    lib.host_column_adjoint_job.restype = C.c_int
+    lib.host_column_adjoint_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
+                                            i, vp, vp, vp, vp, C.POINTER(C.c_int)]
     return lib

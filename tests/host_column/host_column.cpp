@@ -43,6 +43,7 @@ static inline unsigned long long atomicMax(unsigned long long* p, unsigned long 
 }
 
 #include "../../gudni_gb300/csrc/raster_device.cuh"
+#include "../../gudni_gb300/csrc/adjoint_device.cuh"
 #include "../../gudni_gb300/csrc/strand_table.h"
 
 namespace {
@@ -64,6 +65,139 @@ int run_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_t
 }
 
 }  // namespace
+
+struct HostTables {
+  std::vector<uint4> table;
+  std::vector<float2> ys;
+  std::vector<uint32_t> first;
+};
+
+static gudni::RasterInputs host_inputs(HostTables& t, const uint8_t* geometry, size_t geometry_bytes,
+                                       const float* substances, size_t n_substances, const uint8_t* pictures,
+                                       size_t picture_bytes, const gudni_picture_use* uses, size_t n_uses,
+                                       const gudni_radial* radials, size_t n_radials, const gudni_shape* shapes,
+                                       size_t n_shapes, const gudni_tile_info* tiles, int n_tiles, int compute_depth,
+                                       int bitmap_w, int bitmap_h, int job_index, const float* background,
+                                       int max_shape, uint32_t* out) {
+  gudni::build_strand_table(geometry, geometry_bytes, t.table, t.ys, t.first);
+  gudni::RasterInputs in;
+  std::memset(&in, 0, sizeof(in));
+  in.geometry = geometry;
+  in.geometry_bytes = geometry_bytes;
+  in.substances = reinterpret_cast<const float4*>(substances);
+  in.n_substances = (uint32_t)n_substances;
+  in.pictures = pictures;
+  in.picture_bytes = picture_bytes;
+  in.uses = uses;
+  in.n_uses = (uint32_t)n_uses;
+  in.radials = radials;
+  in.n_radials = (uint32_t)n_radials;
+  in.shapes = shapes;
+  in.n_shapes = (uint32_t)n_shapes;
+  in.tiles = tiles;
+  in.n_tiles = n_tiles;
+  in.log2_tpt = compute_depth;
+  in.bitmap_w = bitmap_w;
+  in.bitmap_h = bitmap_h;
+  in.job_index = job_index;
+  in.background = make_float4(background[0], background[1], background[2], background[3]);
+  in.max_shape = max_shape;
+  in.out = out;
+  in.strand_table = t.table.empty() ? nullptr : t.table.data();
+  in.strand_y = t.ys.empty() ? nullptr : t.ys.data();
+  in.n_strands = (uint32_t)t.table.size();
+  in.strand_first = t.first.data();
+  in.n_units = (uint32_t)t.first.size();
+  return in;
+}
+
+static int stack_words(int max_shape) {
+  int sections = 1;  // stack words for max_shape, a power of two (as the CUDA launch picks them)
+  while (64 * sections < max_shape + 1) sections *= 2;
+  return sections;
+}
+
+template <int SECTIONS>
+static int adjoint_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_tiles, int tpt, int cap,
+                       float4* image, const float4* target, float* gGeo, float* gSub, int* overflow) {
+  const int layerCap = in.max_shape + 1;
+  std::vector<float4> thr((size_t)cap), lineGrad((size_t)cap), bitGrad((size_t)in.max_shape + 1);
+  std::vector<uint32_t> hdr((size_t)cap), idx((size_t)in.max_shape + 1);
+  std::vector<int4> prov((size_t)cap);
+  std::vector<gudni::LineRec> lines((size_t)cap);
+  std::vector<float4> layers(2 * (size_t)layerCap);
+  std::vector<int32_t> layerBits((size_t)layerCap);
+  gudni::AdjSlot s;
+  s.thr = thr.data();
+  s.hdr = hdr.data();
+  s.prov = prov.data();
+  s.lines = lines.data();
+  s.lineGrad = lineGrad.data();
+  s.idx = idx.data();
+  s.bitGrad = bitGrad.data();
+  s.layer = layers.data();
+  s.front = layers.data() + layerCap;
+  s.layerBit = layerBits.data();
+  s.cap = cap;
+  s.layerCap = layerCap;
+  const float* pile = reinterpret_cast<const float*>(in.geometry);
+  int status = 0;
+  for (int t = 0; t < n_tiles; ++t) {
+    for (int column = 0; column < tpt; ++column) {
+      int nLines = 0, nBits = 0;
+      float2 delta = make_float2(0.0f, 0.0f);
+      if (gudni::adjointColumn<SECTIONS>(in, tiles[t], column, s, image, target, nLines, nBits, delta, status))
+        *overflow = 1;
+      // the kernel's warp gathering, one lane at a time
+      for (int i = 0; i < nLines; ++i) {
+        int32_t ix[2 * gudni::kEpTargets];
+        float v[2 * gudni::kEpTargets];
+        gudni::epTargets(lines[i].a, lineGrad[i].x, lineGrad[i].y, pile, delta, ix, v);
+        gudni::epTargets(lines[i].b, lineGrad[i].z, lineGrad[i].w, pile, delta, ix + gudni::kEpTargets,
+                         v + gudni::kEpTargets);
+        for (int k = 0; k < 2 * gudni::kEpTargets; ++k)
+          if (ix[k] >= 0) gGeo[ix[k]] += v[k];
+      }
+      for (int b = 0; b < nBits; ++b) {
+        const uint64_t sid = in.shapes[idx[b]].tag & GUDNI_TAG_ID_MASK;
+        if (sid >= in.n_substances) continue;
+        gSub[4 * sid + 0] += bitGrad[b].x;
+        gSub[4 * sid + 1] += bitGrad[b].y;
+        gSub[4 * sid + 2] += bitGrad[b].z;
+        gSub[4 * sid + 3] += bitGrad[b].w;
+      }
+    }
+  }
+  return status;
+}
+
+// One job's adjoint, as gudni_adjoint_tiles_device computes it, on the host: image
+// (W*H float4: I rgb, section-area sum), gradients ADDED to gGeo / gSub.
+extern "C" int host_column_adjoint_job(const uint8_t* geometry, size_t geometry_bytes, const float* substances,
+                                       size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                                       const gudni_picture_use* uses, size_t n_uses, const gudni_radial* radials,
+                                       size_t n_radials, const gudni_shape* shapes, size_t n_shapes,
+                                       const gudni_tile_info* tiles, int n_tiles, int compute_depth, int bitmap_w,
+                                       int bitmap_h, int job_index, const float* background, int capacity,
+                                       int max_shape, const float* target, float* image, float* grad_geometry,
+                                       float* grad_substances, int* overflow) {
+  HostTables t;
+  gudni::RasterInputs in = host_inputs(t, geometry, geometry_bytes, substances, n_substances, pictures,
+                                       picture_bytes, uses, n_uses, radials, n_radials, shapes, n_shapes, tiles,
+                                       n_tiles, compute_depth, bitmap_w, bitmap_h, job_index, background, max_shape,
+                                       nullptr);
+  *overflow = 0;
+  const int tpt = 1 << compute_depth;
+  float4* img = reinterpret_cast<float4*>(image);
+  const float4* tg = reinterpret_cast<const float4*>(target);
+  switch (stack_words(max_shape)) {
+    case 1: return adjoint_all<1>(in, tiles, n_tiles, tpt, capacity, img, tg, grad_geometry, grad_substances, overflow);
+    case 2: return adjoint_all<2>(in, tiles, n_tiles, tpt, capacity, img, tg, grad_geometry, grad_substances, overflow);
+    case 4: return adjoint_all<4>(in, tiles, n_tiles, tpt, capacity, img, tg, grad_geometry, grad_substances, overflow);
+    case 8: return adjoint_all<8>(in, tiles, n_tiles, tpt, capacity, img, tg, grad_geometry, grad_substances, overflow);
+    default: return -1;
+  }
+}
 
 // One job, as gudni_raster_job does it, on the host.  Returns the kernel status bits
 // (0 when clean); *overflow is set when a column needed more than max_thresholds.

@@ -78,3 +78,58 @@ def test_non_finite_points():
     flat.pairs[3, 1] = np.nan
     flat.pairs[17, 2] = np.inf
     check(S.serialize_flat(flat, L.make_spec(16, 32, 4096, 127, 8)))
+
+
+def host_adjoint(frame, target, capacity=1024):
+    from host_column.build import load
+    lib = load()
+    img = np.zeros((frame.canvas_h, frame.canvas_w, 4), np.float32)
+    gg = np.zeros(frame.geometry.size // 4, np.float32)
+    gs = np.zeros((len(frame.substances), 4), np.float32)
+    tgt = np.ascontiguousarray(target, np.float32)
+    bg = np.ascontiguousarray(frame.background, np.float32)
+    p = L.ptr
+    for ji, job in enumerate(frame.jobs):
+        ov = C.c_int(0)
+        st = lib.host_column_adjoint_job(p(frame.geometry), frame.geometry.size, p(frame.substances),
+                                         len(frame.substances), p(frame.pictures), frame.pictures.size,
+                                         p(frame.picture_uses), len(frame.picture_uses), p(frame.radials),
+                                         len(frame.radials), p(job.shapes), len(job.shapes), p(job.tiles),
+                                         len(job.tiles), frame.compute_depth, frame.canvas_w, frame.canvas_h, ji,
+                                         bg.ctypes.data, capacity, frame.spec.max_shape, tgt.ctypes.data,
+                                         img.ctypes.data, gg.ctypes.data, gs.ctypes.data, C.byref(ov))
+        assert st == 0 and ov.value == 0, (st, ov.value)
+    return img, gg, gs
+
+
+def _rel(got, want):
+    got, want = np.asarray(got, np.float64).ravel(), np.asarray(want, np.float64).ravel()
+    big = np.abs(want) > 0.01 * np.abs(want).max()
+    return (float(np.linalg.norm(got - want) / np.linalg.norm(want)),
+            float(np.max(np.abs(got[big] - want[big]) / np.abs(want[big]))))
+
+
+@pytest.mark.parametrize("name", ["random", "dense", "glyphs"])
+def test_adjoint_column_code_matches_fp64_reference(name):
+    """The adjoint's per-column device code (adjoint_device.cuh) on the host: float image
+    equal to the FP64 reference's forward, gradients within 1e-3 of it."""
+    rng = np.random.default_rng(1)
+    if name == "random":
+        make = lambda: G.random_shapes(seed=9, width=160, height=120, n_shapes=24)  # noqa: E731
+        spec = L.make_spec(32, 32, 4096, 127, 8)
+    elif name == "dense":
+        make = lambda: G.random_shapes(seed=91, width=96, height=80, n_shapes=120)  # noqa: E731
+        spec = L.make_spec(16, 64, 4096, 255, 4, max_strands_per_tile=1 << 24)
+    else:
+        make = lambda: G.glyph_page(seed=3, width=256, height=192, n_glyphs=60, n_shapes=30)  # noqa: E731
+        spec = L.make_spec(32, 32, 4096, 127, 8)
+    frame = S.serialize_flat(make(), spec)
+    t = make()
+    t.pairs = (t.pairs + rng.normal(0, 2.0, t.pairs.shape)).astype(np.float32)
+    target = O.render_float(S.serialize_flat(t, spec))
+    _, g_geo, g_sub, img_ref = O.loss_and_gradient(frame, target)
+    img, gg, gs = host_adjoint(frame, target)
+    np.testing.assert_allclose(img, img_ref, rtol=1e-6, atol=1e-6)
+    for got, want, what in ((gg, g_geo, "geometry"), (gs, g_sub, "substances")):
+        norm, worst = _rel(got, want)
+        assert norm <= 1e-3 and worst <= 1e-3, (what, norm, worst)
