@@ -430,7 +430,9 @@ int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes) {
   static_assert(gudni::kNoStrandIndex == gudni::kNoStrand, "one marker for units without a strand");
   ctx->n_strands = 0;
   ctx->n_units = bytes / 16;
-  gudni::build_strand_table(geo, bytes, ctx->h_strand_table, ctx->h_strand_y, ctx->h_strand_first);
+  const unsigned cores = std::thread::hardware_concurrency();
+  gudni::build_strand_table(geo, bytes, ctx->h_strand_table, ctx->h_strand_y, ctx->h_strand_first,
+                            std::min(16u, cores ? cores : 1u));
   int rc;
   if ((rc = upload(ctx, ctx->strand_table, ctx->h_strand_table.data(), ctx->h_strand_table.size(), "strand table")))
     return rc;

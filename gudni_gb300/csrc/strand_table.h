@@ -15,14 +15,40 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace gudni {
 
 constexpr uint32_t kNoStrandIndex = 0xFFFFFFFFu;  // no strand starts at this unit
 
+// y range of every point of one strand (right end, left end and its control, then
+// each tree node's point and control); NaN disables culling for the strand.
+inline float2 strand_y_range(const uint8_t* strand, uint32_t size) {
+  float lo = INFINITY, hi = -INFINITY;
+  bool nan = false;
+  auto take = [&](size_t at) {
+    float y;
+    std::memcpy(&y, strand + at, 4);
+    if (y != y) nan = true;
+    lo = std::min(lo, y);
+    hi = std::max(hi, y);
+  };
+  take(12);
+  take(20);
+  take(28);
+  for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
+    take(node + 4);
+    take(node + 12);
+  }
+  return nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+}
+
+// `threads` > 1: the y ranges (independent per strand, most of the time of a large
+// pile) are computed on that many host threads after the sequential walk; the table is
+// the same.
 inline void build_strand_table(const uint8_t* geo, size_t bytes, std::vector<uint4>& table, std::vector<float2>& ys,
-                               std::vector<uint32_t>& first) {
+                               std::vector<uint32_t>& first, unsigned threads = 1) {
   table.clear();
   ys.clear();
   first.assign(bytes / 16, kNoStrandIndex);
@@ -37,27 +63,22 @@ inline void build_strand_table(const uint8_t* geo, size_t bytes, std::vector<uin
     std::memcpy(&lx, geo + off + 16, 4);
     if (off % 16 == 0) first[off / 16] = (uint32_t)table.size();
     table.push_back(make_uint4((uint32_t)(off / 8), size, lx, rx));
-    // y range of every point of the strand (right end, left end and its control,
-    // then each tree node's point and control); NaN disables culling for the strand
-    float lo = INFINITY, hi = -INFINITY;
-    bool nan = false;
-    auto take = [&](size_t at) {
-      float y;
-      std::memcpy(&y, geo + off + at, 4);
-      if (y != y) nan = true;
-      lo = std::min(lo, y);
-      hi = std::max(hi, y);
-    };
-    take(12);
-    take(20);
-    take(28);
-    for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
-      take(node + 4);
-      take(node + 12);
-    }
-    ys.push_back(nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi));
     off += (size_t)size * 8;
   }
+  ys.resize(table.size());
+  auto range = [&](size_t a, size_t b) {
+    for (size_t i = a; i < b; ++i) ys[i] = strand_y_range(geo + (size_t)table[i].x * 8, table[i].y);
+  };
+  const size_t n = table.size();
+  threads = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, n / 16384));
+  if (threads <= 1) {
+    range(0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < threads; ++t) pool.emplace_back(range, n * t / threads, n * (t + 1) / threads);
+  range(0, n / threads);
+  for (auto& th : pool) th.join();
 }
 
 }  // namespace gudni

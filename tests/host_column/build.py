@@ -16,7 +16,7 @@ def build() -> str:
     if not os.path.isfile(OUT) or max(os.path.getmtime(d) for d in DEPS) > os.path.getmtime(OUT):
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
         subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fPIC", "-shared",
-                        "-w", "-I", CUDA_INCLUDE, "-I", os.path.join(ROOT, "include"), SRC, "-o", OUT], check=True)
+                        "-w", "-pthread", "-I", CUDA_INCLUDE, "-I", os.path.join(ROOT, "include"), SRC, "-o", OUT], check=True)
     return OUT
 
 
@@ -29,4 +29,6 @@ def load():
     lib.host_column_adjoint_job.restype = C.c_int
     lib.host_column_adjoint_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
                                             i, vp, vp, vp, vp, C.POINTER(C.c_int)]
+    lib.host_strand_table.restype = sz
+    lib.host_strand_table.argtypes = [vp, sz, C.c_uint, vp, vp, vp, sz]
     return lib

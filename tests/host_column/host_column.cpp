@@ -258,3 +258,18 @@ extern "C" int host_column_raster_job(const uint8_t* geometry, size_t geometry_b
     default: return -1;
   }
 }
+
+// The strand table of a pile built with `threads` host threads, copied out (at most
+// `cap` strands); returns the strand count.
+extern "C" size_t host_strand_table(const uint8_t* geometry, size_t bytes, unsigned threads, uint4* table_out,
+                                    float2* ys_out, uint32_t* first_out, size_t cap) {
+  std::vector<uint4> table;
+  std::vector<float2> ys;
+  std::vector<uint32_t> first;
+  gudni::build_strand_table(geometry, bytes, table, ys, first, threads);
+  const size_t n = std::min(cap, table.size());
+  std::memcpy(table_out, table.data(), n * sizeof(uint4));
+  std::memcpy(ys_out, ys.data(), n * sizeof(float2));
+  std::memcpy(first_out, first.data(), first.size() * sizeof(uint32_t));
+  return table.size();
+}

@@ -133,3 +133,23 @@ def test_adjoint_column_code_matches_fp64_reference(name):
     for got, want, what in ((gg, g_geo, "geometry"), (gs, g_sub, "substances")):
         norm, worst = _rel(got, want)
         assert norm <= 1e-3 and worst <= 1e-3, (what, norm, worst)
+
+
+def test_strand_table_threads_give_the_same_table():
+    """The C ABI builds the strand table's y ranges on several host threads; the table
+    is the one-thread table, entry for entry."""
+    from host_column.build import load
+    lib = load()
+    flat = G.glyph_page(seed=2, width=960, height=540, n_glyphs=600, n_shapes=200)
+    geo = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 127, 8)).geometry
+    outs = []
+    for threads in (1, 4, 16):
+        cap = geo.size // 16
+        table = np.zeros((cap, 4), np.uint32)
+        ys = np.zeros((cap, 2), np.float32)
+        first = np.zeros(geo.size // 16, np.uint32)
+        n = lib.host_strand_table(geo.ctypes.data, geo.size, threads, table.ctypes.data, ys.ctypes.data,
+                                  first.ctypes.data, cap)
+        assert n >= 2 * 16384  # large enough for the threads to split it
+        outs.append((table[:n].tobytes(), ys[:n].tobytes(), first.tobytes()))
+    assert outs[0] == outs[1] == outs[2]
