@@ -48,3 +48,25 @@ def test_invalid_spec_rejected():
     spec.threads_per_tile = 48  # not a power of two
     assert not lib.gudni_create(C.byref(spec), 0)
     assert "threads_per_tile" in lib.gudni_last_error(None).decode() or "device" in lib.gudni_last_error(None).decode()
+
+
+def test_headers_compile_as_c_and_link(tmp_path):
+    """The ABI is plain C: a C99 translation unit that includes both headers and takes
+    the address of every declared entry point compiles with gcc and links against the
+    two libraries (nothing is run)."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    cuda_lib, host_lib = B.build_cuda(), B.build_host()
+    names = declared("gudni_cuda.h") + declared("gudni_serialize.h")
+    src = tmp_path / "abi.c"
+    src.write_text("#include <stdio.h>\n#include \"gudni_cuda.h\"\n#include \"gudni_serialize.h\"\n"
+                   "int main(void) {\n  const void* fns[] = {\n" +
+                   "".join(f"    (const void*)&{n},\n" for n in names) +
+                   "  };\n  printf(\"%d\\n\", (int)(sizeof fns / sizeof fns[0]));\n  return 0;\n}\n")
+    exe = tmp_path / "abi"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe), cuda_lib, host_lib, "-Wl,-rpath," + os.path.dirname(cuda_lib)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
