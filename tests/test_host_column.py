@@ -23,9 +23,10 @@ pytestmark = pytest.mark.skipif(shutil.which("g++") is None or not os.path.isdir
                                 reason="needs g++ and the CUDA headers")
 
 
-def host_render(frame) -> np.ndarray:
+def host_render(frame, capacity=None) -> np.ndarray:
     from host_column.build import load
     lib = load()
+    capacity = capacity or frame.spec.max_thresholds
     out = np.zeros((frame.canvas_h, frame.canvas_w), np.uint32)
     bg = np.ascontiguousarray(frame.background, np.float32)
     p = L.ptr
@@ -36,7 +37,7 @@ def host_render(frame) -> np.ndarray:
                                         p(frame.picture_uses), len(frame.picture_uses), p(frame.radials),
                                         len(frame.radials), p(job.shapes), len(job.shapes), p(job.tiles),
                                         len(job.tiles), frame.compute_depth, frame.canvas_w, frame.canvas_h, ji,
-                                        bg.ctypes.data, frame.spec.max_thresholds, frame.spec.max_shape,
+                                        bg.ctypes.data, capacity, frame.spec.max_shape,
                                         out.ctypes.data, C.byref(ov))
         assert st == 0 and ov.value == 0, (st, ov.value)
     return out
@@ -153,3 +154,15 @@ def test_strand_table_threads_give_the_same_table():
         assert n >= 2 * 16384  # large enough for the threads to split it
         outs.append((table[:n].tobytes(), ys[:n].tobytes(), first.tobytes()))
     assert outs[0] == outs[1] == outs[2]
+
+
+@pytest.mark.parametrize("extra", [1, 3])
+def test_nearly_full_queues(extra):
+    """Slabs only just large enough for the longest column: the merge sort and the
+    batched insertion lack free space below the queue and take their literal paths;
+    the image must not change."""
+    flat = G.random_shapes(seed=301, width=96, height=80, n_shapes=150)
+    frame = S.serialize_flat(flat, L.make_spec(8, 64, 8192, 255, 4, max_strands_per_tile=1 << 24))
+    st = {}
+    want = O.render_frame(frame, stats=st)
+    assert np.array_equal(host_render(frame, st["max_queue"] + extra), want)
