@@ -24,8 +24,8 @@ def load():
     lib = C.CDLL(build())
     vp, sz, i = C.c_void_p, C.c_size_t, C.c_int
     lib.host_column_raster_job.restype = C.c_int
-    lib.host_column_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
-                                           i, vp, C.POINTER(C.c_int)]
+    lib.host_column_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, vp,
+                                           C.c_float, i, i, vp, C.POINTER(C.c_int)]
     lib.host_column_adjoint_job.restype = C.c_int
     lib.host_column_adjoint_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
                                             i, vp, vp, vp, vp, C.POINTER(C.c_int)]

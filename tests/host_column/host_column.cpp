@@ -206,7 +206,8 @@ extern "C" int host_column_raster_job(const uint8_t* geometry, size_t geometry_b
                                       const gudni_picture_use* uses, size_t n_uses, const gudni_radial* radials,
                                       size_t n_radials, const gudni_shape* shapes, size_t n_shapes,
                                       const gudni_tile_info* tiles, int n_tiles, int compute_depth, int bitmap_w,
-                                      int bitmap_h, int job_index, const float* background, int max_thresholds,
+                                      int bitmap_h, int job_index, const float* background,
+                                      const float* random_field, float stochastic, int max_thresholds,
                                       int max_shape, uint32_t* out, int* overflow) {
   std::vector<uint4> table;
   std::vector<float2> ys;
@@ -224,8 +225,8 @@ extern "C" int host_column_raster_job(const uint8_t* geometry, size_t geometry_b
   in.n_uses = (uint32_t)n_uses;
   in.radials = radials;
   in.n_radials = (uint32_t)n_radials;
-  in.random_field = nullptr;
-  in.stochastic = 0.0f;
+  in.random_field = random_field;
+  in.stochastic = stochastic;
   in.shapes = shapes;
   in.n_shapes = (uint32_t)n_shapes;
   in.tiles = tiles;

@@ -37,7 +37,8 @@ def host_render(frame, capacity=None) -> np.ndarray:
                                         p(frame.picture_uses), len(frame.picture_uses), p(frame.radials),
                                         len(frame.radials), p(job.shapes), len(job.shapes), p(job.tiles),
                                         len(job.tiles), frame.compute_depth, frame.canvas_w, frame.canvas_h, ji,
-                                        bg.ctypes.data, capacity, frame.spec.max_shape,
+                                        bg.ctypes.data, p(frame.random_field), frame.spec.stochastic_factor,
+                                        capacity, frame.spec.max_shape,
                                         out.ctypes.data, C.byref(ov))
         assert st == 0 and ov.value == 0, (st, ov.value)
     return out
@@ -71,6 +72,20 @@ def test_very_dense_small_canvas():
 def test_glyph_page_all_substances():
     flat = G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25)
     check(S.serialize_flat(flat, L.make_spec(32, 32, 4096, 511, 8)))
+
+
+@pytest.mark.parametrize("factor", [0.25, 0.37])
+def test_stochastic_jitter(factor):
+    """A non-zero STOCHASTIC_FACTOR: the area jitter reads the random field from the
+    same per-column cursor, advanced once per section (K:1597-1613)."""
+    spec = L.make_spec(32, 32, 4096, 127, 8, stochastic_factor=factor)
+    frame = S.serialize_flat(G.glyph_page(seed=8, width=200, height=150, n_glyphs=50, n_shapes=12), spec)
+    assert np.any(frame.random_field != 0)
+    plain = O.render_frame(S.serialize_flat(G.glyph_page(seed=8, width=200, height=150, n_glyphs=50, n_shapes=12),
+                                            L.make_spec(32, 32, 4096, 127, 8)))
+    got, want = host_render(frame), O.render_frame(frame)
+    assert not np.array_equal(want, plain)  # the jitter changes the image
+    assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
 
 
 def test_non_finite_points():

@@ -91,6 +91,27 @@ def test_oracle_matches_reference_kernels_glyphs():
     assert np.array_equal(a, b), f"{(a != b).sum()} pixels differ"
 
 
+@pytest.mark.parametrize("factor,exact", [(0.25, True), (0.37, False)])
+def test_oracle_matches_reference_kernels_stochastic(factor, exact):
+    """STOCHASTIC_FACTOR != 0.  The reference pastes the factor as a decimal literal,
+    so its jitter term is a double product; the oracle's is float.  A power-of-two
+    factor scales exactly in both, so the images agree bit for bit; any other factor
+    may round one way or the other now and then, inside the parity bar."""
+    if not O.ref_available(127, 8, factor):
+        pytest.skip("reference checkout not present")
+    spec = L.make_spec(32, 32, 4096, 127, 8, stochastic_factor=factor)
+    frame = S.serialize_flat(G.glyph_page(seed=8, width=200, height=150, n_glyphs=50, n_shapes=12, radial_frac=0.0),
+                             spec)
+    st = {}
+    a = O.render_frame(frame, stats=st)
+    b = O.ref_render_frame(frame, max_thresholds=st["max_queue"] + 8)
+    if exact:
+        assert np.array_equal(a, b), f"{(a != b).sum()} pixels differ"
+    else:
+        from conftest import assert_parity
+        assert_parity(a, b, max_lsb=1, min_exact=0.999)
+
+
 def test_oracle_reports_overflow():
     """A column that needs more thresholds than max_thresholds is reported, not
     silently corrupted (the reference writes past its slab there)."""
