@@ -140,6 +140,7 @@ struct gudni_ctx {
   DevBuf<int> status;
   DevBuf<int64_t> counters;
   bool counters_on = false;
+  int dense_min = 0;  // gudni_set_dense_columns (0: per-lane scan only)
 
   // adjoint scratch: slots x capacity thresholds, provenance and line records
   int adj_grid = 0;
@@ -348,6 +349,7 @@ int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInf
   a.overflow_items = need_fallback ? ctx->overflow_items.ptr : nullptr;
   a.overflow_cap = (uint32_t)std::min<size_t>(max_items, 0xFFFFFFFFull);
   a.overflow_count = ctx->words.ptr;
+  a.dense_min = ctx->dense_min;
   a.status = ctx->status.ptr;
   const size_t warps_per_block = gudni::kRasterBlock / 32;
   const int grid = (int)std::min<size_t>((n_units + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
@@ -936,6 +938,14 @@ int gudni_enable_counters(gudni_ctx* ctx, int enable) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
   ctx->counters_on = enable != 0;
+  return GUDNI_OK;
+}
+
+int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (min_thresholds < 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "min_thresholds must be >= 0");
+  if (min_thresholds != ctx->dense_min) drop_graph(ctx);  // a captured launch holds the old setting
+  ctx->dense_min = min_thresholds;
   return GUDNI_OK;
 }
 

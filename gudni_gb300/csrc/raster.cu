@@ -15,6 +15,12 @@
 //   output, background and threads per tile.  Every thread owns a scratch slot (a
 //   queue of `capacity` entries and the shape-index table of its column).
 //
+// raster_tiles_warp_kernel -- the fast pass with warp-cooperative dense columns
+//   (warp_column.cuh): the same units, but a unit's columns whose queues hold at least
+//   `dense_min` thresholds are scanned by the whole warp, one after another, instead
+//   of each by its own lane.  Chosen by gudni_set_dense_columns; the output is the
+//   same bit for bit.
+//
 // raster_list_kernel -- the full-capacity pass.  Columns that overflowed the fast
 //   pass's small working capacity were appended to a list (work unit and lane); this kernel, launched
 //   right after on the same stream, reads the list's length on the device and re-runs
@@ -30,6 +36,7 @@
 
 #include "raster_device.cuh"
 #include "raster_kernels.h"
+#include "warp_column.cuh"
 
 namespace gudni {
 
@@ -70,6 +77,52 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a
         } else {
           status |= kStatusOverflow;
         }
+      }
+    }
+  }
+  if (status) atomicOr(a.status, status);
+}
+
+template <int SECTIONS>
+__global__ void __launch_bounds__(kRasterBlock) raster_tiles_warp_kernel(TileLaunch a) {
+  __shared__ float4 sProd[kRasterBlock];
+  __shared__ uint32_t sBit[kRasterBlock];
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const WarpScratch ws{sProd + (threadIdx.x & ~31u), sBit + (threadIdx.x & ~31u)};
+  float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
+  uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
+  uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
+  int status = 0;
+  for (;;) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(a.next_tile, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= a.n_units) break;
+    int tile, chunk;
+    unitOf(a.units, a.chunk_log2, k, tile, chunk);
+    bool ok;
+    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
+    if (!ok) continue;
+    const gudni_tile_info ti = in.tiles[tile];
+    if (!tileOk(ti, in.n_shapes) || in.log2_tpt < 0 || in.log2_tpt > kMaxLog2Tpt) {
+      status |= kStatusBadInput;
+      continue;
+    }
+    const int tpt = 1 << in.log2_tpt;
+    const int column = chunk * 32 + lane;
+    const int flags = runUnitWarp<SECTIONS>(in, ti, column, column < tpt, thr, hdr, a.scratch.capacity, idx, status,
+                                            lane, a.dense_min, ws);
+    if (flags & kUnitOverflow) {
+      if (a.overflow_items) {
+        const uint32_t n = atomicAdd(a.overflow_count, 1u);
+        if (n < a.overflow_cap) {
+          a.overflow_items[n] = (k << kLaneBits) | (uint32_t)lane;
+        } else {
+          status |= kStatusOverflow;
+        }
+      } else {
+        status |= kStatusOverflow;
       }
     }
   }
@@ -165,6 +218,8 @@ template <int S>
 static cudaError_t launch_s(const TileLaunch& a, bool list, int grid, cudaStream_t stream) {
   if (list) {
     raster_list_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+  } else if (a.dense_min > 0) {
+    raster_tiles_warp_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
   } else {
     raster_tiles_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
   }

@@ -44,6 +44,8 @@ struct TileLaunch {
   uint32_t* overflow_items;     // where columns that overflow `capacity` go
   uint32_t overflow_cap;
   uint32_t* overflow_count;
+  int dense_min;                // > 0: columns with at least this many thresholds are
+                                // scanned by the whole warp (raster_tiles_warp_kernel)
   // full-capacity pass
   const uint32_t* list;         // overflowed columns
   const uint32_t* list_count;   // their number (device)

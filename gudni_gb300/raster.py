@@ -111,6 +111,12 @@ class Rasterizer:
     def enable_counters(self, on: bool = True) -> None:
         self._check(self.lib.gudni_enable_counters(self.ctx, 1 if on else 0))
 
+    def set_dense_columns(self, min_thresholds: int) -> None:
+        """Scan columns whose queues hold at least `min_thresholds` thresholds with the
+        whole warp (gudni_set_dense_columns); 0 keeps every column on its own lane.
+        The image does not change."""
+        self._check(self.lib.gudni_set_dense_columns(self.ctx, int(min_thresholds)))
+
     def read_counters(self) -> dict:
         c = (C.c_int64 * 4)()
         self._check(self.lib.gudni_read_counters(self.ctx, c))

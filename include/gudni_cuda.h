@@ -239,6 +239,14 @@ int gudni_batch_download(gudni_ctx* ctx, uint32_t* out);
 int gudni_enable_counters(gudni_ctx* ctx, int enable);
 int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
 
+/* Warp-cooperative dense columns for the next launches of this context: a column
+ * whose sorted queue holds at least `min_thresholds` thresholds is scanned by all 32
+ * lanes of its warp together (sections dealt to the lanes, pixel sums taken in section
+ * order), instead of by its own lane.  The output is the same bit for bit; the choice
+ * is one of speed.  0 (the default) keeps every column on its own lane.  No
+ * counterpart in the reference.  Not yet timed on a GPU. */
+int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds);
+
 /* ------------------------------------------------------------------ adjoint */
 
 /* Gradients of the per-pixel L2 loss L = sum_p sum_{c in RGB} (I_c(p) - T_c(p))^2,

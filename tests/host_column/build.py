@@ -7,7 +7,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 SRC = os.path.join(HERE, "host_column.cpp")
 OUT = os.path.join(HERE, "_build", "libhost_column.so")
-DEPS = [SRC] + [os.path.join(ROOT, "gudni_gb300", "csrc", f) for f in ("raster_device.cuh", "adjoint_device.cuh", "strand_table.h")] + [
+DEPS = [SRC, os.path.join(HERE, "warp_emu.h")] + [
+    os.path.join(ROOT, "gudni_gb300", "csrc", f)
+    for f in ("raster_device.cuh", "adjoint_device.cuh", "strand_table.h", "warp_column.cuh")] + [
     os.path.join(ROOT, "include", "gudni_cuda.h")]
 CUDA_INCLUDE = "/usr/local/cuda/include"
 
@@ -29,6 +31,10 @@ def load():
     lib.host_column_adjoint_job.restype = C.c_int
     lib.host_column_adjoint_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
                                             i, vp, vp, vp, vp, C.POINTER(C.c_int)]
+    lib.host_column_raster_job_warp.restype = C.c_int
+    lib.host_column_raster_job_warp.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i,
+                                                vp, vp, C.c_float, i, i, i, i, C.c_uint64, vp,
+                                                C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.host_strand_table.restype = sz
     lib.host_strand_table.argtypes = [vp, sz, C.c_uint, vp, vp, vp, sz]
     return lib

@@ -42,9 +42,31 @@ static inline unsigned long long atomicMax(unsigned long long* p, unsigned long 
   return o;
 }
 
+#include "warp_emu.h"
+
+// warp collectives on the emulated warp
+static inline void __syncwarp(unsigned = 0xffffffffu) { warp_emu::collective(warp_emu::kSync, 0u, 0); }
+static inline unsigned __shfl_sync(unsigned, unsigned v, int src) {
+  return warp_emu::collective(warp_emu::kShfl, v, src);
+}
+static inline int __shfl_sync(unsigned, int v, int src) {
+  return (int)warp_emu::collective(warp_emu::kShfl, (unsigned)v, src);
+}
+static inline float __shfl_sync(unsigned, float v, int src) {
+  return __uint_as_float(warp_emu::collective(warp_emu::kShfl, __float_as_uint(v), src));
+}
+static inline float __shfl_up_sync(unsigned, float v, unsigned delta) {
+  return __uint_as_float(warp_emu::collective(warp_emu::kShflUp, __float_as_uint(v), (int)delta));
+}
+static inline unsigned __ballot_sync(unsigned, int pred) {
+  return warp_emu::collective(warp_emu::kBallot, pred ? 1u : 0u, 0);
+}
+static inline int __ffs(int x) { return __builtin_ffs(x); }
+
 #include "../../gudni_gb300/csrc/raster_device.cuh"
 #include "../../gudni_gb300/csrc/adjoint_device.cuh"
 #include "../../gudni_gb300/csrc/strand_table.h"
+#include "../../gudni_gb300/csrc/warp_column.cuh"
 
 namespace {
 
@@ -59,6 +81,49 @@ int run_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_t
     for (int column = 0; column < tpt; ++column) {
       if (gudni::runColumn<SECTIONS>(in, tiles[t], column, thr.data(), hdr.data(), cap, idx.data(), status))
         *overflow = 1;
+    }
+  }
+  return status;
+}
+
+// The warp-cooperative form: every work unit (32 columns of a tile) on an emulated
+// warp, the lanes resuming in a seeded random order at each collective; columns that
+// overflow the working capacity `cap` are re-run by the per-lane path with
+// `full_cap`, as the full-capacity pass does.
+template <int SECTIONS>
+int run_all_warp(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_tiles, int tpt, int cap,
+                 int full_cap, int dense_min, uint64_t seed, int* overflow, int* by_warp) {
+  const size_t idxStride = (size_t)in.max_shape + 1;
+  std::vector<float4> thr(32 * (size_t)cap), big((size_t)full_cap);
+  std::vector<uint32_t> hdr(32 * (size_t)cap), bigH((size_t)full_cap);
+  std::vector<uint32_t> idx(32 * idxStride);
+  float4 prod[32];
+  uint32_t bits[32];
+  const gudni::WarpScratch ws{prod, bits};
+  int status = 0;
+  for (int t = 0; t < n_tiles; ++t) {
+    for (int chunk = 0; chunk * 32 < tpt; ++chunk) {
+      int flags[32] = {0};
+      int laneStatus[32] = {0};
+      const std::function<void(int)> body = [&](int lane) {
+        const int column = chunk * 32 + lane;
+        int st = 0;
+        flags[lane] = gudni::runUnitWarp<SECTIONS>(in, tiles[t], column, column < tpt,
+                                                   thr.data() + (size_t)lane * cap, hdr.data() + (size_t)lane * cap,
+                                                   cap, idx.data() + (size_t)lane * idxStride, st, lane, dense_min,
+                                                   ws);
+        laneStatus[lane] = st;
+      };
+      if (!warp_emu::run(body, seed * 1000003ull + (uint64_t)t * 64u + (uint64_t)chunk)) return -100;
+      for (int lane = 0; lane < 32; ++lane) {
+        status |= laneStatus[lane];
+        if (flags[lane] & gudni::kUnitByWarp) *by_warp += 1;
+        if (flags[lane] & gudni::kUnitOverflow) {
+          if (gudni::runColumn<SECTIONS>(in, tiles[t], chunk * 32 + lane, big.data(), bigH.data(), full_cap,
+                                         idx.data(), status))
+            *overflow = 1;
+        }
+      }
     }
   }
   return status;
@@ -273,4 +338,37 @@ extern "C" size_t host_strand_table(const uint8_t* geometry, size_t bytes, unsig
   std::memcpy(ys_out, ys.data(), n * sizeof(float2));
   std::memcpy(first_out, first.data(), first.size() * sizeof(uint32_t));
   return table.size();
+}
+
+// One job by the warp-cooperative form (see run_all_warp).  Returns the status bits;
+// *by_warp receives the number of columns the whole warp scanned, *overflow is set
+// when a column needed more than full_cap.
+extern "C" int host_column_raster_job_warp(const uint8_t* geometry, size_t geometry_bytes, const float* substances,
+                                           size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                                           const gudni_picture_use* uses, size_t n_uses, const gudni_radial* radials,
+                                           size_t n_radials, const gudni_shape* shapes, size_t n_shapes,
+                                           const gudni_tile_info* tiles, int n_tiles, int compute_depth,
+                                           int bitmap_w, int bitmap_h, int job_index, const float* background,
+                                           const float* random_field, float stochastic, int cap, int full_cap,
+                                           int max_shape, int dense_min, uint64_t seed, uint32_t* out,
+                                           int* overflow, int* by_warp) {
+  HostTables t;
+  gudni::RasterInputs in = host_inputs(t, geometry, geometry_bytes, substances, n_substances, pictures,
+                                       picture_bytes, uses, n_uses, radials, n_radials, shapes, n_shapes, tiles,
+                                       n_tiles, compute_depth, bitmap_w, bitmap_h, job_index, background, max_shape,
+                                       out);
+  in.random_field = random_field;
+  in.stochastic = stochastic;
+  *overflow = 0;
+  *by_warp = 0;
+  const int tpt = 1 << compute_depth;
+  switch (stack_words(max_shape)) {
+    case 1: return run_all_warp<1>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    case 2: return run_all_warp<2>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    case 4: return run_all_warp<4>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    case 8: return run_all_warp<8>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    case 16: return run_all_warp<16>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    case 32: return run_all_warp<32>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
+    default: return -1;
+  }
 }

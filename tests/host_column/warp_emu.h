@@ -1,0 +1,116 @@
+// TEST INFRASTRUCTURE -- not part of the product and never loaded by it.
+//
+// A 32-lane warp on one host thread, for running the product's warp-cooperative
+// device code on the CPU.  Each lane is a fiber (ucontext) running the same function;
+// a lane runs until its next warp collective (__syncwarp, a shuffle, a ballot), which
+// is a barrier: when every lane has arrived the collective's results are formed and
+// the lanes resume, each round in a fresh seeded random order.  Memory written by
+// one lane between two collectives is therefore seen by the others in an order that
+// changes from round to round, so device code that reads another lane's writes
+// without a barrier in between gives results that depend on the seed.
+//
+// Requires every lane to call the same collectives in the same order (full-mask,
+// convergent use, which is how the device code uses them); run() reports a mismatch.
+
+#pragma once
+
+#include <ucontext.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <functional>
+#include <random>
+#include <vector>
+
+namespace warp_emu {
+
+enum Kind { kSync = 1, kShfl = 2, kShflUp = 3, kBallot = 4 };
+
+struct Warp {
+  ucontext_t sched;
+  ucontext_t ctx[32];
+  std::vector<char> stack[32];
+  bool finished[32];
+  int kind[32];
+  uint32_t value[32];
+  int arg[32];
+  uint32_t result[32];
+  const std::function<void(int)>* body;
+  int lane;
+};
+
+inline thread_local Warp* g_warp = nullptr;
+
+inline void trampoline() {
+  Warp* w = g_warp;
+  const int lane = w->lane;
+  (*w->body)(lane);
+  w->finished[lane] = true;  // returning resumes uc_link, the scheduler
+}
+
+inline uint32_t collective(int kind, uint32_t v, int arg) {
+  Warp* w = g_warp;
+  const int lane = w->lane;
+  w->kind[lane] = kind;
+  w->value[lane] = v;
+  w->arg[lane] = arg;
+  swapcontext(&w->ctx[lane], &w->sched);
+  return w->result[lane];
+}
+
+// Runs body(lane) for lanes 0..31.  Returns false when the lanes' collectives did not
+// match (different kinds at one barrier, or some lanes finished while others wait).
+inline bool run(const std::function<void(int)>& body, uint64_t seed) {
+  Warp w;
+  Warp* saved = g_warp;
+  g_warp = &w;
+  w.body = &body;
+  for (int l = 0; l < 32; ++l) {
+    w.stack[l].resize(1 << 18);
+    getcontext(&w.ctx[l]);
+    w.ctx[l].uc_stack.ss_sp = w.stack[l].data();
+    w.ctx[l].uc_stack.ss_size = w.stack[l].size();
+    w.ctx[l].uc_link = &w.sched;
+    makecontext(&w.ctx[l], trampoline, 0);
+    w.finished[l] = false;
+  }
+  std::mt19937_64 rng(seed);
+  int order[32];
+  for (int l = 0; l < 32; ++l) order[l] = l;
+  bool ok = true;
+  for (;;) {
+    std::shuffle(order, order + 32, rng);
+    for (int i = 0; i < 32; ++i) {
+      const int l = order[i];
+      if (w.finished[l]) continue;
+      w.lane = l;
+      swapcontext(&w.sched, &w.ctx[l]);
+    }
+    int done = 0;
+    for (int l = 0; l < 32; ++l) done += w.finished[l] ? 1 : 0;
+    if (done == 32) break;
+    if (done != 0) {
+      ok = false;
+      break;
+    }
+    const int kind = w.kind[0];
+    for (int l = 1; l < 32; ++l)
+      if (w.kind[l] != kind) ok = false;
+    if (!ok) break;
+    uint32_t ballot = 0;
+    for (int l = 0; l < 32; ++l)
+      if (w.value[l]) ballot |= 1u << l;
+    for (int l = 0; l < 32; ++l) {
+      switch (kind) {
+        case kShfl: w.result[l] = w.value[w.arg[l] & 31]; break;
+        case kShflUp: w.result[l] = l - w.arg[l] >= 0 ? w.value[l - w.arg[l]] : w.value[l]; break;
+        case kBallot: w.result[l] = ballot; break;
+        default: w.result[l] = 0; break;
+      }
+    }
+  }
+  g_warp = saved;
+  return ok;
+}
+
+}  // namespace warp_emu

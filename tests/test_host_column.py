@@ -2,7 +2,8 @@
 (tests/host_column), against the oracle: the exact-arithmetic transformations of the
 CUDA path (strand-table range test and y culling, batched and merged insertion of
 split parts, opaque-cut colour memo, one-word and multi-word stacks) checked without a
-GPU, on sparse, dense and degenerate scenes."""
+GPU, on sparse, dense and degenerate scenes; and the warp-cooperative scan of dense
+columns (warp_column.cuh) on an emulated 32-lane warp (tests/host_column/warp_emu.h)."""
 import ctypes as C
 import os
 import shutil
@@ -181,3 +182,81 @@ def test_nearly_full_queues(extra):
     st = {}
     want = O.render_frame(frame, stats=st)
     assert np.array_equal(host_render(frame, st["max_queue"] + extra), want)
+
+
+# ------------------------------------------------------------------ warp-cooperative scan
+def host_render_warp(frame, dense_min=0, seed=1, capacity=None):
+    """The warp-cooperative fast pass (warp_column.cuh) on an emulated warp; columns
+    that overflow `capacity` are re-run at max_thresholds by the per-lane path, as the
+    full-capacity pass does.  Returns the image and the number of columns the whole
+    warp scanned."""
+    from host_column.build import load
+    lib = load()
+    cap = capacity or frame.spec.max_thresholds
+    out = np.zeros((frame.canvas_h, frame.canvas_w), np.uint32)
+    bg = np.ascontiguousarray(frame.background, np.float32)
+    p = L.ptr
+    by_warp = 0
+    for ji, job in enumerate(frame.jobs):
+        ov, bw = C.c_int(0), C.c_int(0)
+        st = lib.host_column_raster_job_warp(p(frame.geometry), frame.geometry.size, p(frame.substances),
+                                             len(frame.substances), p(frame.pictures), frame.pictures.size,
+                                             p(frame.picture_uses), len(frame.picture_uses), p(frame.radials),
+                                             len(frame.radials), p(job.shapes), len(job.shapes), p(job.tiles),
+                                             len(job.tiles), frame.compute_depth, frame.canvas_w, frame.canvas_h,
+                                             ji, bg.ctypes.data, p(frame.random_field),
+                                             frame.spec.stochastic_factor, cap, frame.spec.max_thresholds,
+                                             frame.spec.max_shape, dense_min, seed, out.ctypes.data, C.byref(ov),
+                                             C.byref(bw))
+        assert st == 0 and ov.value == 0, (st, ov.value)
+        by_warp += bw.value
+    return out, by_warp
+
+
+def check_warp(frame, min_by_warp, **kw):
+    got, by_warp = host_render_warp(frame, **kw)
+    want = O.render_frame(frame)
+    assert by_warp >= min_by_warp
+    assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_warp_scan_random_scene(seed):
+    """Every column scanned by the whole warp; the lanes resume in a different order
+    at each barrier (seeded), so a read of another lane's write without a barrier
+    between would change pixels."""
+    frame = S.serialize_flat(G.random_shapes(seed=5, width=64, height=48, n_shapes=12),
+                             L.make_spec(32, 32, 4096, 127, 8))
+    check_warp(frame, 128, dense_min=0, seed=seed)
+
+
+def test_warp_scan_dense_multiword_stack():
+    """Canvas-wide shapes: bands of dozens of sections (several chunks of 32), a
+    multi-word stack, batched and merged insertion of split parts on lane 0."""
+    frame = S.serialize_flat(G.random_shapes(seed=91, width=40, height=30, n_shapes=120),
+                             L.make_spec(8, 64, 4096, 255, 4, max_strands_per_tile=1 << 24))
+    check_warp(frame, 1000, dense_min=0, seed=3)
+
+
+def test_warp_scan_all_substances_and_jitter():
+    """Pictures and gradients (colours that depend on the pixel row) and a non-zero
+    stochastic factor (one random-field step per section)."""
+    frame = S.serialize_flat(G.glyph_page(seed=4, width=160, height=96, n_glyphs=40, n_shapes=10),
+                             L.make_spec(32, 32, 4096, 511, 8))
+    check_warp(frame, 400, dense_min=0, seed=4)
+    frame = S.serialize_flat(G.glyph_page(seed=8, width=100, height=64, n_glyphs=30, n_shapes=8),
+                             L.make_spec(32, 32, 4096, 127, 8, stochastic_factor=0.37))
+    check_warp(frame, 150, dense_min=0, seed=5)
+
+
+def test_warp_scan_capacity_and_mixed_columns():
+    """A working capacity below the longest queue (those columns go to the
+    full-capacity pass), and a threshold that leaves short queues on their lanes."""
+    frame = S.serialize_flat(G.random_shapes(seed=301, width=40, height=32, n_shapes=80),
+                             L.make_spec(8, 64, 8192, 255, 4, max_strands_per_tile=1 << 24))
+    st = {}
+    O.render_frame(frame, stats=st)
+    check_warp(frame, 1000, dense_min=0, seed=7, capacity=st["max_queue"] // 2)
+    got, by_warp = host_render_warp(frame, dense_min=st["max_queue"] // 2, seed=8)
+    assert 0 < by_warp < 1280
+    assert np.array_equal(got, O.render_frame(frame))
