@@ -87,9 +87,11 @@ template <int SECTIONS>
 __global__ void __launch_bounds__(kRasterBlock) raster_tiles_warp_kernel(TileLaunch a) {
   __shared__ float4 sProd[kRasterBlock];
   __shared__ uint32_t sBit[kRasterBlock];
+  __shared__ uint32_t sFlips[kRasterBlock / 32 * kWarpFlipWords];
   const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const WarpScratch ws{sProd + (threadIdx.x & ~31u), sBit + (threadIdx.x & ~31u)};
+  const WarpScratch ws{sProd + (threadIdx.x & ~31u), sBit + (threadIdx.x & ~31u),
+                       sFlips + (threadIdx.x >> 5) * kWarpFlipWords};
   float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
   uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
   uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;

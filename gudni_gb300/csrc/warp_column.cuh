@@ -30,13 +30,31 @@
 
 #include "raster_device.cuh"
 
+// Path counters for the host tests (empty in the CUDA build): which way splitNextWarp
+// went, and how the parts were sorted.
+#ifndef GUDNI_WARP_TRACE
+#define GUDNI_WARP_TRACE(event)
+#endif
+
 namespace gudni {
+
+enum WarpTraceEvent {
+  kTraceSplitWarp = 0,   // splitNextWarp across the lanes
+  kTraceSplitLane0 = 1,  // splitNextWarp on lane 0
+  kTraceSortRounds = 2,  // parts sorted by transposition rounds
+  kTraceSortLane0 = 3,   // parts sorted on lane 0
+  kTraceTies = 4,        // parts with equal keys reordered
+  kTraceEvents = 5
+};
 
 // Per-warp scratch in shared memory: one entry per lane.
 struct WarpScratch {
-  float4* prod;   // a chunk's section products (r, g, b, area)
-  uint32_t* bit;  // a chunk's threshold shape bits
+  float4* prod;     // a chunk's section products (r, g, b, area)
+  uint32_t* bit;    // a chunk's threshold shape bits
+  uint32_t* flips;  // a set of shape-bit flips (kWarpFlipWords words)
 };
+
+constexpr int kWarpFlipWords = 64;  // 2 per stack word, up to 32 stack words
 
 __device__ __forceinline__ uint64_t shflWord(uint64_t v, int src) {
   const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
@@ -44,47 +62,383 @@ __device__ __forceinline__ uint64_t shflWord(uint64_t v, int src) {
   return ((uint64_t)hi << 32) | (uint64_t)lo;
 }
 
-// verticalAdvance K:1744-1824 by the whole warp, at a band's end (p.sEndX == kRight).
-// Every lane runs the same steps on its copy of the stack; only splitNext writes the
-// queue, on lane 0.
+// ---- shape-bit flips by the whole warp
+//
+// A set of flips is an XOR, so its order does not matter: the lanes mark their share
+// of the flips in a per-warp bitset (2 words per stack word), then every lane folds the
+// set into its copy of the stack.  `hiFlip` (the colour memo's test) takes the highest
+// bit the set changes: a bit flipped twice is unchanged, and the memo depends only on
+// the bits themselves.
+
+__device__ __forceinline__ void flipClear(uint32_t* d, int words, int lane) {
+  for (int w = lane; w < words; w += 32) d[w] = 0u;
+  __syncwarp();
+}
+
+__device__ __forceinline__ void flipMark(uint32_t* d, uint32_t bit) {
+  atomicXor(&d[bit >> 5], 1u << (bit & 31u));
+}
+
 template <int SECTIONS>
-__device__ __forceinline__ void verticalAdvanceWarp(Queue& q, const ColumnState& c, Parse& p,
-                                                    ShapeStack<SECTIONS>& stack, int lane) {
-  for (int i = 0; i < p.numActive; ++i) stack.pass(q.getH(i));
-  const float nextBreak = cl_min(c.floatHeight, p.pixelY);
-  const float activeBottom = q.length() > 0 ? q.get(0).y : FLT_MAX;
-  if (activeBottom == p.sEndY) {
-    while (p.numActive > 0) {
-      stack.passBottom(q.getH(0));
-      q.pop();
-      p.numActive -= 1;
+__device__ __forceinline__ void flipApply(const uint32_t* d, ShapeStack<SECTIONS>& s) {
+  __syncwarp();
+#pragma unroll
+  for (int w = 0; w < SECTIONS; ++w) {
+    const uint64_t m = ((uint64_t)d[2 * w + 1] << 32) | (uint64_t)d[2 * w];
+    if (m) {
+      s.w[w] ^= m;
+      s.nz = s.w[w] ? (s.nz | (1u << w)) : (s.nz & ~(1u << w));
+      s.hiFlip = max(s.hiFlip, w * 64 + 63 - __clzll((long long)m));
     }
   }
+  __syncwarp();  // every lane has read the set before it is cleared again
+}
+
+// ---- splitNext by the whole warp
+
+// splitNext on lane 0 (the per-lane code, raster_device.cuh), the other lanes taking
+// its queue state.  Nothing may have changed the queue since the last barrier.
+__device__ __forceinline__ float splitNextLane0(Queue& q, Parse& p, int lane) {
+  if (lane == 0) GUDNI_WARP_TRACE(kTraceSplitLane0);
+  __syncwarp();  // every lane is done reading the queue
+  float slice = 0.0f;
+  if (lane == 0) slice = splitNext(q, p);
+  __syncwarp();  // lane 0's writes are visible
+  slice = __shfl_sync(0xffffffffu, slice, 0);
+  q.start = __shfl_sync(0xffffffffu, q.start, 0);
+  q.overflow = __shfl_sync(0xffffffffu, q.overflow ? 1 : 0, 0) != 0;
+  p.numActive = __shfl_sync(0xffffffffu, p.numActive, 0);
+  return slice;
+}
+
+// The parts [lo, lo + m), in the order they were split off, into the order the per-lane
+// code gives them: ascending (an entry goes after another only when it is strictly
+// below it, thresholdIsBelow K:1079-1094), equal keys latest first.  A stable sort
+// first -- odd-even transposition rounds across the lanes until a round swaps
+// nothing, which the few line crossings inside one band keep short, or after
+// `kSortRounds` rounds an insertion sort on lane 0 (a stable sort's result is unique)
+// -- then each run of equal keys is reversed.
+constexpr int kSortRounds = 16;
+
+__device__ __forceinline__ bool sameKey(uint32_t ha, float4 ta, uint32_t hb, float4 tb) {
+  return !isBelow(ha, ta, hb, tb) && !isBelow(hb, tb, ha, ta);
+}
+
+__device__ __forceinline__ void sortPartsWarp(Queue& q, int lo, int m, int lane) {
+  bool sorted = false;
+  for (int round = 0; round < kSortRounds && !sorted; ++round) {
+    bool swapped = false;
+    for (int phase = 0; phase < 2; ++phase) {
+      for (int a = 2 * lane + phase; a + 1 < m; a += 64) {
+        const uint32_t ha = q.hdr[lo + a], hb = q.hdr[lo + a + 1];
+        const float4 ta = q.thr[lo + a], tb = q.thr[lo + a + 1];
+        if (isBelow(ha, ta, hb, tb)) {
+          q.hdr[lo + a] = hb;
+          q.thr[lo + a] = tb;
+          q.hdr[lo + a + 1] = ha;
+          q.thr[lo + a + 1] = ta;
+          swapped = true;
+        }
+      }
+      __syncwarp();
+    }
+    sorted = __ballot_sync(0xffffffffu, swapped) == 0u;
+  }
+  if (lane == 0) {
+    if (sorted) {
+      GUDNI_WARP_TRACE(kTraceSortRounds);
+    } else {
+      GUDNI_WARP_TRACE(kTraceSortLane0);
+      for (int i = lo + 1; i < lo + m; ++i) {
+        const float4 t = q.thr[i];
+        const uint32_t h = q.hdr[i];
+        int j = i - 1;
+        while (j >= lo && isBelow(q.hdr[j], q.thr[j], h, t)) {
+          q.thr[j + 1] = q.thr[j];
+          q.hdr[j + 1] = q.hdr[j];
+          --j;
+        }
+        q.thr[j + 1] = t;
+        q.hdr[j + 1] = h;
+      }
+    }
+  }
+  __syncwarp();
+  // equal keys: latest first
+  bool tie = false;
+  for (int a = lane; a + 1 < m; a += 32) tie = tie || sameKey(q.hdr[lo + a], q.thr[lo + a], q.hdr[lo + a + 1], q.thr[lo + a + 1]);
+  if (__ballot_sync(0xffffffffu, tie) != 0u) {
+    if (lane == 0) {
+      GUDNI_WARP_TRACE(kTraceTies);
+      int a = 0;
+      while (a < m) {
+        int z = a + 1;
+        while (z < m && sameKey(q.hdr[lo + z - 1], q.thr[lo + z - 1], q.hdr[lo + z], q.thr[lo + z])) ++z;
+        for (int i = a, j = z - 1; i < j; ++i, --j) {
+          const uint32_t h = q.hdr[lo + i];
+          const float4 t = q.thr[lo + i];
+          q.hdr[lo + i] = q.hdr[lo + j];
+          q.thr[lo + i] = q.thr[lo + j];
+          q.hdr[lo + j] = h;
+          q.thr[lo + j] = t;
+        }
+        a = z;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// splitNext K:1069-1077 by the whole warp.  The band's end, the split of the active
+// entries and the placing of their kept lower parts run across the lanes, producing
+// the per-lane splitNext's queue entry for entry: the parts are sorted and merged
+// with the entries of equal top after the active block (the per-lane merge path; with
+// no NaN key involved it equals inserting the parts one by one).  Any case outside
+// that (the literal path, a NaN key, more than 32 equal-top entries) runs the
+// per-lane splitNext on lane 0 before anything is written.  Every lane returns the
+// slice point with q.start and p.numActive updated.
+__device__ __forceinline__ float splitNextWarp(Queue& q, Parse& p, int lane) {
+  const unsigned full = 0xffffffffu;
+  const int len = q.length();
+  const int s0 = q.start;
+  const float top = q.get(0).x;
+  // the active block ends at the first entry whose top is above `top`
+  int n = len;
+  float slicePoint = FLT_MAX;
+  for (int b = 1; b < len; b += 32) {
+    const int i = b + lane;
+    const float t = i < len ? q.get(i).x : 0.0f;
+    const uint32_t above = __ballot_sync(full, i < len && t > top);
+    if (above) {
+      const int f = __ffs((int)above) - 1;
+      n = b + f;
+      slicePoint = __shfl_sync(full, t, f);
+      break;
+    }
+  }
+  // the nearest active bottom below `top`: cl_min keeps the earlier of equal values,
+  // so the smallest (value, index), the next top (index -1) first
+  float best = FLT_MAX;
+  int bestAt = 0x7fffffff;
+  for (int i = lane; i < n; i += 32) {
+    const float bottom = q.get(i).y;
+    if (top < bottom && bottom < best) {
+      best = bottom;
+      bestAt = i;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const float ob = __shfl_xor_sync(full, best, off);
+    const int oa = __shfl_xor_sync(full, bestAt, off);
+    if (ob < best || (ob == best && oa < bestAt)) {
+      best = ob;
+      bestAt = oa;
+    }
+  }
+  slicePoint = best < slicePoint ? best : slicePoint;
+  // the per-lane code's batched case: room below the queue, every active top above
+  // the slice point
+  bool batched = s0 >= 2 * n;
+  for (int b = 0; batched && b < n; b += 32) {
+    const int i = b + lane;
+    batched = __ballot_sync(full, i < n && !(q.get(i).x < slicePoint)) == 0u;
+  }
+  if (!batched) return splitNextLane0(q, p, lane);
+  // read only: how many lower parts are kept, and whether a sort key is NaN
+  int m = 0;
+  bool nan = false;
+  for (int b = 0; b < n; b += 32) {
+    const int i = b + lane;
+    bool keep = false, bad = false;
+    if (i < n) {
+      uint32_t ch = q.getH(i);
+      float4 cur = q.get(i);
+      if (cur.x < slicePoint && slicePoint < cur.y) {
+        uint32_t sh;
+        float4 split;
+        splitAt(ch, cur, slicePoint, sh, split);
+        keep = tKeep(sh, split);
+        const float tx = tTopX(sh, split), sl = invSlope(sh, split);
+        bad = keep && !(tx == tx && sl == sl);
+      }
+    }
+    m += __popc(__ballot_sync(full, keep));
+    nan = nan || __ballot_sync(full, bad) != 0u;
+  }
+  // the entries of top == slicePoint right after the active block, and the one after
+  int g = 0;
+  bool mergeable = !nan;
+  for (int b = 0; m > 0 && mergeable; b += 32) {
+    const int r = s0 + n + b + lane;
+    bool eq = false, bad = false;
+    if (r < q.cap) {
+      const float4 t = q.thr[r];
+      eq = t.x == slicePoint;
+      if (eq) {
+        const uint32_t h = q.hdr[r];
+        const float tx = tTopX(h, t), sl = invSlope(h, t);
+        bad = !(tx == tx && sl == sl);
+      }
+    }
+    const uint32_t noteq = ~__ballot_sync(full, eq);
+    const int run = noteq ? __ffs((int)noteq) - 1 : 32;
+    mergeable = __ballot_sync(full, lane < run && bad) == 0u;
+    g += run;
+    if (g > 32) mergeable = false;
+    if (run < 32) {
+      const int rEnd = s0 + n + g;
+      if (mergeable && rEnd < q.cap) mergeable = q.thr[rEnd].x > slicePoint;
+      break;
+    }
+  }
+  if (m > 0 && !mergeable) return splitNextLane0(q, p, lane);
+  if (lane == 0) GUDNI_WARP_TRACE(kTraceSplitWarp);
+  p.numActive = n;
+  __syncwarp();  // every lane is done reading before the queue changes
+  // split in place; kept part j (in cursor order) to s0 - n - m + j
+  int j0 = 0;
+  for (int b = 0; b < n; b += 32) {
+    const int i = b + lane;
+    bool keep = false;
+    uint32_t sh = 0u;
+    float4 split = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < n) {
+      uint32_t ch = q.hdr[s0 + i];
+      float4 cur = q.thr[s0 + i];
+      if (cur.x < slicePoint && slicePoint < cur.y) {
+        splitAt(ch, cur, slicePoint, sh, split);
+        q.hdr[s0 + i] = ch;
+        q.thr[s0 + i] = cur;
+        keep = tKeep(sh, split);
+      }
+    }
+    const uint32_t kept = __ballot_sync(full, keep);
+    if (keep) {
+      const int j = j0 + __popc(kept & ((1u << lane) - 1u));
+      q.hdr[s0 - n - m + j] = sh;
+      q.thr[s0 - n - m + j] = split;
+    }
+    j0 += __popc(kept);
+  }
+  __syncwarp();
+  if (m == 0) return slicePoint;
+  // the active block moves down by m (each chunk read before it is written; a chunk's
+  // destinations lie below the next chunk's sources)
+  for (int b = 0; b < n; b += 32) {
+    const int i = b + lane;
+    uint32_t h = 0u;
+    float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < n) {
+      h = q.hdr[s0 + i];
+      t = q.thr[s0 + i];
+    }
+    __syncwarp();
+    if (i < n) {
+      q.hdr[s0 - m + i] = h;
+      q.thr[s0 - m + i] = t;
+    }
+  }
+  q.start = s0 - m;
+  // the parts, in cursor order at [lo, lo + m), into the per-lane order
+  const int lo = s0 - n - m;
+  sortPartsWarp(q, lo, m, lane);
+  // merge with the g equal-top entries: an entry goes ahead of a part only when the
+  // part is strictly below it.  Entry r is preceded by the parts not below it (a
+  // prefix of the sorted parts); part k by the entries whose prefix ends at or
+  // before k.
+  const int out = s0 - m + n;
+  uint32_t eh = 0u;
+  float4 et = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int ahead = 0;
+  if (lane < g) {
+    eh = q.hdr[s0 + n + lane];
+    et = q.thr[s0 + n + lane];
+    int a = 0, z = m;  // first part strictly below the entry
+    while (a < z) {
+      const int mid = (a + z) >> 1;
+      if (isBelow(q.hdr[lo + mid], q.thr[lo + mid], eh, et)) {
+        z = mid;
+      } else {
+        a = mid + 1;
+      }
+    }
+    ahead = a;
+  }
+  __syncwarp();  // the entries are read before the parts may land on their places
+  if (lane < g) {
+    q.hdr[out + lane + ahead] = eh;
+    q.thr[out + lane + ahead] = et;
+  }
+  for (int b = 0; b < m; b += 32) {
+    const int k = b + lane;
+    int before = 0;
+    for (int r = 0; r < g; ++r) before += __shfl_sync(full, ahead, r) <= k ? 1 : 0;
+    if (k < m) {
+      q.hdr[out + k + before] = q.hdr[lo + k];
+      q.thr[out + k + before] = q.thr[lo + k];
+    }
+  }
+  __syncwarp();
+  return slicePoint;
+}
+
+// verticalAdvance K:1744-1824 by the whole warp, at a band's end (p.sEndX == kRight).
+// The stack flips of each step are applied as one set; the queue changes only in
+// splitNextWarp.
+template <int SECTIONS>
+__device__ __forceinline__ void verticalAdvanceWarp(Queue& q, const ColumnState& c, Parse& p,
+                                                    ShapeStack<SECTIONS>& stack, int lane, uint32_t* flips) {
+  const int n0 = p.numActive;
+  const float activeBottom = q.length() > 0 ? q.get(0).y : FLT_MAX;
+  const bool dropAll = activeBottom == p.sEndY;
+  if (n0 > 0) {
+    // every active threshold is passed; when the band ended at their bottom they are
+    // dropped, the persistent bottoms passed again (two flips of one bit cancel)
+    flipClear(flips, 2 * SECTIONS, lane);
+    for (int i = lane; i < n0; i += 32) {
+      const uint32_t h = q.getH(i);
+      if (!(dropAll && hPersistBottom(h))) flipMark(flips, h & kShapeBitMask);
+    }
+    flipApply<SECTIONS>(flips, stack);
+    if (dropAll) {
+      q.start += n0;
+      p.numActive = 0;
+    }
+  }
+  const float nextBreak = cl_min(c.floatHeight, p.pixelY);
   float nextBottom;
   if (p.numActive > 0) {
     nextBottom = cl_min(activeBottom, nextBreak);
   } else {
-    const float nextTop = p.numActive < q.length() ? q.get(p.numActive).x : FLT_MAX;
+    const float nextTop = q.length() > 0 ? q.get(0).x : FLT_MAX;
     if (nextTop > p.sEndY) {
       nextBottom = cl_min(nextBreak, nextTop);
     } else {
-      __syncwarp();  // every lane is done reading the queue
-      float slice = 0.0f;
-      if (lane == 0) slice = splitNext(q, p);
-      __syncwarp();  // lane 0's writes are visible
-      slice = __shfl_sync(0xffffffffu, slice, 0);
-      q.start = __shfl_sync(0xffffffffu, q.start, 0);
-      q.overflow = __shfl_sync(0xffffffffu, q.overflow ? 1 : 0, 0) != 0;
-      p.numActive = __shfl_sync(0xffffffffu, p.numActive, 0);
-      nextBottom = cl_min(nextBreak, slice);
-      while (p.numActive > 0 && q.get(0).x == q.get(0).y) {
-        stack.passTop(q.getH(0));
-        q.pop();
-        p.numActive -= 1;
+      nextBottom = cl_min(nextBreak, splitNextWarp(q, p, lane));
+      // leading zero-height entries are dropped (their persistent tops passed), then
+      // the persistent tops of the active entries below the column top are passed
+      int lead = p.numActive;
+      for (int b = 0; b < p.numActive; b += 32) {
+        const int i = b + lane;
+        bool flat = true;
+        if (i < p.numActive) {
+          const float4 t = q.get(i);
+          flat = t.x == t.y;
+        }
+        const uint32_t notFlat = __ballot_sync(0xffffffffu, !flat);
+        if (notFlat) {
+          lead = b + __ffs((int)notFlat) - 1;
+          break;
+        }
       }
-      for (int i = 0; i < p.numActive; ++i) {
-        if (q.get(i).x > 0.0f) stack.passTop(q.getH(i));
+      flipClear(flips, 2 * SECTIONS, lane);
+      for (int i = lane; i < p.numActive; i += 32) {
+        const uint32_t h = q.getH(i);
+        if (hPersistTop(h) && (i < lead || q.get(i).x > 0.0f)) flipMark(flips, h & kShapeBitMask);
       }
+      flipApply<SECTIONS>(flips, stack);
+      q.start += lead;
+      p.numActive -= lead;
     }
   }
   p.sStartY = p.sEndY;
@@ -126,7 +480,7 @@ __device__ __forceinline__ void renderColumnWarp(const RasterInputs& in, const C
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
     int guard = 0;
     while ((p.sEndX < kRight) || (p.sEndY < p.pixelY)) {
-      verticalAdvanceWarp<SECTIONS>(q, c, p, stack, lane);
+      verticalAdvanceWarp<SECTIONS>(q, c, p, stack, lane, ws.flips);
       if (q.overflow) return;
       const int n = p.numActive;  // the band has n + 1 sections
       if (n + 1 > kSectionCap - guard) {

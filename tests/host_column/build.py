@@ -35,6 +35,8 @@ def load():
     lib.host_column_raster_job_warp.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i,
                                                 vp, vp, C.c_float, i, i, i, i, C.c_uint64, vp,
                                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.host_warp_trace.restype = None
+    lib.host_warp_trace.argtypes = [C.POINTER(C.c_longlong)]
     lib.host_strand_table.restype = sz
     lib.host_strand_table.argtypes = [vp, sz, C.c_uint, vp, vp, vp, sz]
     return lib

@@ -44,6 +44,10 @@ static inline unsigned long long atomicMax(unsigned long long* p, unsigned long 
 
 #include "warp_emu.h"
 
+// how often each path of the warp-cooperative band step ran (GUDNI_WARP_TRACE)
+static long long g_warp_trace[8];
+#define GUDNI_WARP_TRACE(event) (g_warp_trace[(event)] += 1)
+
 // warp collectives on the emulated warp
 static inline void __syncwarp(unsigned = 0xffffffffu) { warp_emu::collective(warp_emu::kSync, 0u, 0); }
 static inline unsigned __shfl_sync(unsigned, unsigned v, int src) {
@@ -61,7 +65,20 @@ static inline float __shfl_up_sync(unsigned, float v, unsigned delta) {
 static inline unsigned __ballot_sync(unsigned, int pred) {
   return warp_emu::collective(warp_emu::kBallot, pred ? 1u : 0u, 0);
 }
+static inline float __shfl_xor_sync(unsigned, float v, int mask) {
+  return __uint_as_float(warp_emu::collective(warp_emu::kShflXor, __float_as_uint(v), mask));
+}
+static inline int __shfl_xor_sync(unsigned, int v, int mask) {
+  return (int)warp_emu::collective(warp_emu::kShflXor, (unsigned)v, mask);
+}
 static inline int __ffs(int x) { return __builtin_ffs(x); }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
+// shared-memory atomics: lanes run one at a time between collectives
+static inline unsigned atomicXor(unsigned* p, unsigned v) {
+  const unsigned o = *p;
+  *p = o ^ v;
+  return o;
+}
 
 #include "../../gudni_gb300/csrc/raster_device.cuh"
 #include "../../gudni_gb300/csrc/adjoint_device.cuh"
@@ -99,7 +116,8 @@ int run_all_warp(const gudni::RasterInputs& in, const gudni_tile_info* tiles, in
   std::vector<uint32_t> idx(32 * idxStride);
   float4 prod[32];
   uint32_t bits[32];
-  const gudni::WarpScratch ws{prod, bits};
+  uint32_t flips[gudni::kWarpFlipWords];
+  const gudni::WarpScratch ws{prod, bits, flips};
   int status = 0;
   for (int t = 0; t < n_tiles; ++t) {
     for (int chunk = 0; chunk * 32 < tpt; ++chunk) {
@@ -370,5 +388,14 @@ extern "C" int host_column_raster_job_warp(const uint8_t* geometry, size_t geome
     case 16: return run_all_warp<16>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
     case 32: return run_all_warp<32>(in, tiles, n_tiles, tpt, cap, full_cap, dense_min, seed, overflow, by_warp);
     default: return -1;
+  }
+}
+
+// Path counts of the warp-cooperative band step since the last call, by
+// gudni::WarpTraceEvent (GUDNI_WARP_TRACE).
+extern "C" void host_warp_trace(long long out[gudni::kTraceEvents]) {
+  for (int i = 0; i < gudni::kTraceEvents; ++i) {
+    out[i] = g_warp_trace[i];
+    g_warp_trace[i] = 0;
   }
 }

@@ -24,12 +24,15 @@
 
 namespace warp_emu {
 
-enum Kind { kSync = 1, kShfl = 2, kShflUp = 3, kBallot = 4 };
+enum Kind { kSync = 1, kShfl = 2, kShflUp = 3, kBallot = 4, kShflXor = 5 };
 
 struct Warp {
   ucontext_t sched;
   ucontext_t ctx[32];
   std::vector<char> stack[32];
+  void* schedJmp[5];    // __builtin_setjmp buffers: switching lanes this way keeps the
+  void* laneJmp[32][5];  // signal mask alone (swapcontext makes a system call each time)
+  bool started[32];
   bool finished[32];
   int kind[32];
   uint32_t value[32];
@@ -41,11 +44,29 @@ struct Warp {
 
 inline thread_local Warp* g_warp = nullptr;
 
+// (a function may not both __builtin_setjmp and __builtin_longjmp: each jump has its own)
+__attribute__((noinline)) inline void jumpScheduler(Warp* w) { __builtin_longjmp(w->schedJmp, 1); }
+
+__attribute__((noinline)) inline void jumpLane(Warp* w, int lane) {
+  if (w->started[lane]) __builtin_longjmp(w->laneJmp[lane], 1);
+  w->started[lane] = true;
+  setcontext(&w->ctx[lane]);  // first entry onto the fiber's own stack
+}
+
+__attribute__((noinline)) inline void toScheduler(Warp* w, int lane) {
+  if (__builtin_setjmp(w->laneJmp[lane]) == 0) jumpScheduler(w);
+}
+
+__attribute__((noinline)) inline void toLane(Warp* w, int lane) {
+  if (__builtin_setjmp(w->schedJmp) == 0) jumpLane(w, lane);
+}
+
 inline void trampoline() {
   Warp* w = g_warp;
   const int lane = w->lane;
   (*w->body)(lane);
-  w->finished[lane] = true;  // returning resumes uc_link, the scheduler
+  w->finished[lane] = true;
+  jumpScheduler(w);
 }
 
 inline uint32_t collective(int kind, uint32_t v, int arg) {
@@ -54,7 +75,7 @@ inline uint32_t collective(int kind, uint32_t v, int arg) {
   w->kind[lane] = kind;
   w->value[lane] = v;
   w->arg[lane] = arg;
-  swapcontext(&w->ctx[lane], &w->sched);
+  toScheduler(w, lane);
   return w->result[lane];
 }
 
@@ -72,6 +93,7 @@ inline bool run(const std::function<void(int)>& body, uint64_t seed) {
     w.ctx[l].uc_stack.ss_size = w.stack[l].size();
     w.ctx[l].uc_link = &w.sched;
     makecontext(&w.ctx[l], trampoline, 0);
+    w.started[l] = false;
     w.finished[l] = false;
   }
   std::mt19937_64 rng(seed);
@@ -84,7 +106,7 @@ inline bool run(const std::function<void(int)>& body, uint64_t seed) {
       const int l = order[i];
       if (w.finished[l]) continue;
       w.lane = l;
-      swapcontext(&w.sched, &w.ctx[l]);
+      toLane(&w, l);
     }
     int done = 0;
     for (int l = 0; l < 32; ++l) done += w.finished[l] ? 1 : 0;
@@ -105,6 +127,7 @@ inline bool run(const std::function<void(int)>& body, uint64_t seed) {
         case kShfl: w.result[l] = w.value[w.arg[l] & 31]; break;
         case kShflUp: w.result[l] = l - w.arg[l] >= 0 ? w.value[l - w.arg[l]] : w.value[l]; break;
         case kBallot: w.result[l] = ballot; break;
+        case kShflXor: w.result[l] = w.value[(l ^ w.arg[l]) & 31]; break;
         default: w.result[l] = 0; break;
       }
     }

@@ -5,6 +5,7 @@ split parts, opaque-cut colour memo, one-word and multi-word stacks) checked wit
 GPU, on sparse, dense and degenerate scenes; and the warp-cooperative scan of dense
 columns (warp_column.cuh) on an emulated 32-lane warp (tests/host_column/warp_emu.h)."""
 import ctypes as C
+import dataclasses
 import os
 import shutil
 import sys
@@ -213,11 +214,24 @@ def host_render_warp(frame, dense_min=0, seed=1, capacity=None):
     return out, by_warp
 
 
+def warp_trace():
+    """Counts of the warp band step's paths since the last call: split across the
+    lanes, split on lane 0, parts sorted by rounds, parts sorted on lane 0, equal
+    keys reordered."""
+    from host_column.build import load
+    t = (C.c_longlong * 5)()
+    load().host_warp_trace(t)
+    return {"split_warp": t[0], "split_lane0": t[1], "sort_rounds": t[2], "sort_lane0": t[3], "ties": t[4]}
+
+
 def check_warp(frame, min_by_warp, **kw):
+    warp_trace()
     got, by_warp = host_render_warp(frame, **kw)
+    trace = warp_trace()
     want = O.render_frame(frame)
     assert by_warp >= min_by_warp
     assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+    return trace
 
 
 @pytest.mark.parametrize("seed", [1, 2])
@@ -227,15 +241,32 @@ def test_warp_scan_random_scene(seed):
     between would change pixels."""
     frame = S.serialize_flat(G.random_shapes(seed=5, width=64, height=48, n_shapes=12),
                              L.make_spec(32, 32, 4096, 127, 8))
-    check_warp(frame, 128, dense_min=0, seed=seed)
+    trace = check_warp(frame, 128, dense_min=0, seed=seed)
+    assert trace["split_warp"] > 0
 
 
 def test_warp_scan_dense_multiword_stack():
     """Canvas-wide shapes: bands of dozens of sections (several chunks of 32), a
-    multi-word stack, batched and merged insertion of split parts on lane 0."""
+    multi-word stack, the band step's splits, sorts and merges across the lanes."""
     frame = S.serialize_flat(G.random_shapes(seed=91, width=40, height=30, n_shapes=120),
                              L.make_spec(8, 64, 4096, 255, 4, max_strands_per_tile=1 << 24))
-    check_warp(frame, 1000, dense_min=0, seed=3)
+    trace = check_warp(frame, 1000, dense_min=0, seed=3)
+    assert trace["split_warp"] > 10000 and trace["sort_rounds"] > 10000 and trace["sort_lane0"] > 0
+
+
+def test_warp_scan_equal_keys():
+    """Every outline drawn twice (two colours): split parts with equal keys, which the
+    per-lane order puts latest first."""
+    rng = G._rng(44)
+    specs = []
+    for sp in G.random_shape_specs(rng, 48, 40, 30, 8, 20):
+        twin = dataclasses.replace(sp, leaves=[[a.copy() for a in leaf] for leaf in sp.leaves],
+                                   color=(1.0 - sp.color[0], sp.color[1], 1.0 - sp.color[2], sp.color[3]))
+        specs += [sp, twin]
+    frame = S.serialize_flat(G.flat_from_specs(specs, 48, 40, G.WHITE),
+                             L.make_spec(8, 64, 8192, 255, 4, max_strands_per_tile=1 << 24))
+    trace = check_warp(frame, 1000, dense_min=0, seed=9)
+    assert trace["ties"] > 0
 
 
 def test_warp_scan_all_substances_and_jitter():
@@ -250,12 +281,16 @@ def test_warp_scan_all_substances_and_jitter():
 
 
 def test_warp_scan_capacity_and_mixed_columns():
-    """A working capacity below the longest queue (those columns go to the
-    full-capacity pass), and a threshold that leaves short queues on their lanes."""
+    """Slabs only just large enough (the band step falls back to lane 0 where the
+    queue has no room below it), a working capacity below the longest queue (those
+    columns go to the full-capacity pass), and a threshold that leaves short queues on
+    their lanes."""
     frame = S.serialize_flat(G.random_shapes(seed=301, width=40, height=32, n_shapes=80),
                              L.make_spec(8, 64, 8192, 255, 4, max_strands_per_tile=1 << 24))
     st = {}
     O.render_frame(frame, stats=st)
+    trace = check_warp(frame, 1000, dense_min=0, seed=6, capacity=st["max_queue"] + 2)
+    assert trace["split_lane0"] > 0
     check_warp(frame, 1000, dense_min=0, seed=7, capacity=st["max_queue"] // 2)
     got, by_warp = host_render_warp(frame, dense_min=st["max_queue"] // 2, seed=8)
     assert 0 < by_warp < 1280
