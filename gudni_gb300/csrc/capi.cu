@@ -86,6 +86,7 @@ struct gudni_ctx {
   size_t picture_bytes = 0;
   DevBuf<gudni_picture_use> uses;
   size_t n_uses = 0;
+  uint64_t uses_extent = 0;           // furthest picture-pile byte the uploaded usages read
   DevBuf<gudni_radial> radials;
   size_t n_radials = 0;
   DevBuf<float> random_field;
@@ -394,6 +395,22 @@ int upload(gudni_ctx* ctx, DevBuf<T>& buf, const void* src, size_t count, const 
 
 int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes);
 
+// Every picture usage must read inside a picture pile of `picture_bytes` bytes, from a
+// 4-byte aligned offset; *extent receives the furthest byte any of them reads.
+int check_picture_uses(gudni_ctx* ctx, const gudni_picture_use* uses, size_t n, size_t picture_bytes,
+                       uint64_t* extent) {
+  uint64_t far = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const gudni_picture_use& u = uses[i];
+    const uint64_t end = (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y;
+    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 || end > picture_bytes)
+      return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
+    far = std::max(far, end);
+  }
+  *extent = far;
+  return GUDNI_OK;
+}
+
 int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
                           size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
                           const gudni_picture_use* picture_uses, size_t n_picture_uses,
@@ -402,14 +419,10 @@ int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_
       (n_picture_uses && !picture_uses) || (n_radials && !radials))
     return fail(ctx, GUDNI_ERR_BAD_INPUT, "null buffer with non-zero size");
   if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
-  for (size_t i = 0; i < n_picture_uses; ++i) {
-    const gudni_picture_use& u = picture_uses[i];
-    if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 ||
-        (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
-      return fail(ctx, GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i) + " points outside the picture pile");
-  }
+  uint64_t extent = 0;
+  int rc = check_picture_uses(ctx, picture_uses, n_picture_uses, picture_bytes, &extent);
+  if (rc) return rc;
   ctx->common_ready = false;
-  int rc;
   if ((rc = upload(ctx, ctx->geometry, geometry, geometry_bytes, "geometry upload"))) return rc;
   if ((rc = upload(ctx, ctx->substances, substances, n_substances, "substance upload"))) return rc;
   if ((rc = upload(ctx, ctx->pictures, pictures, picture_bytes, "picture upload"))) return rc;
@@ -423,6 +436,7 @@ int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_
   ctx->n_substances = n_substances;
   ctx->picture_bytes = picture_bytes;
   ctx->n_uses = n_picture_uses;
+  ctx->uses_extent = extent;
   ctx->n_radials = n_radials;
   return GUDNI_OK;
 }
@@ -642,6 +656,72 @@ int gudni_upload_common(gudni_ctx* ctx, const void* geometry, size_t geometry_by
   if (rc) return rc;
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "upload");
+  ctx->common_ready = true;
+  return GUDNI_OK;
+}
+
+int gudni_upload_pictures(gudni_ctx* ctx, const uint8_t* pictures, size_t picture_bytes) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (picture_bytes && !pictures) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null picture pile with non-zero size");
+  cudaSetDevice(ctx->device);
+  ctx->batch_ready = false;  // a batch's usages index the pile its own upload brought
+  drop_graph(ctx);
+  // the uploaded frame stays usable only while its usages still read inside the pile
+  const bool keep_frame = ctx->common_ready && ctx->uses_extent <= picture_bytes;
+  ctx->common_ready = false;
+  ctx->picture_bytes = 0;
+  int rc = upload(ctx, ctx->pictures, pictures, picture_bytes, "picture upload");
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "picture upload");
+  ctx->picture_bytes = picture_bytes;
+  ctx->common_ready = keep_frame;
+  return GUDNI_OK;
+}
+
+int gudni_upload_random_field(gudni_ctx* ctx, const float* random_field) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  drop_graph(ctx);
+  ctx->has_random = false;
+  if (!random_field) return GUDNI_OK;
+  int rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload");
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "random field upload");
+  ctx->has_random = true;
+  return GUDNI_OK;
+}
+
+int gudni_upload_frame(gudni_ctx* ctx, const void* geometry, size_t geometry_bytes, const float* substances,
+                       size_t n_substances, const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                       const gudni_radial* radials, size_t n_radials) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  cudaSetDevice(ctx->device);
+  ctx->batch_ready = false;
+  drop_graph(ctx);
+  if ((geometry_bytes && !geometry) || (n_substances && !substances) || (n_picture_uses && !picture_uses) ||
+      (n_radials && !radials))
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "null buffer with non-zero size");
+  if (geometry_bytes % 16 != 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "geometry pile must be a multiple of 16 bytes");
+  uint64_t extent = 0;
+  int rc = check_picture_uses(ctx, picture_uses, n_picture_uses, ctx->picture_bytes, &extent);
+  if (rc) return rc;
+  ctx->common_ready = false;
+  if ((rc = upload(ctx, ctx->geometry, geometry, geometry_bytes, "geometry upload"))) return rc;
+  if ((rc = upload(ctx, ctx->substances, substances, n_substances, "substance upload"))) return rc;
+  if ((rc = upload(ctx, ctx->uses, picture_uses, n_picture_uses, "picture use upload"))) return rc;
+  if ((rc = upload(ctx, ctx->radials, radials, n_radials, "radial upload"))) return rc;
+  cudaError_t e;
+  if (!ctx->pictures.ptr && (e = ctx->pictures.reserve(0)) != cudaSuccess)  // never hand the kernels a null pile
+    return cuda_fail(ctx, e, "picture pile");
+  if ((rc = build_strand_table(ctx, static_cast<const uint8_t*>(geometry), geometry_bytes))) return rc;
+  ctx->geometry_bytes = geometry_bytes;
+  ctx->n_substances = n_substances;
+  ctx->n_uses = n_picture_uses;
+  ctx->uses_extent = extent;
+  ctx->n_radials = n_radials;
+  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "upload");
   ctx->common_ready = true;
   return GUDNI_OK;
 }

@@ -167,6 +167,12 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_last_error.argtypes = [vp]
     lib.gudni_upload_common.restype = C.c_int
     lib.gudni_upload_common.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp]
+    lib.gudni_upload_pictures.restype = C.c_int
+    lib.gudni_upload_pictures.argtypes = [vp, vp, sz]
+    lib.gudni_upload_random_field.restype = C.c_int
+    lib.gudni_upload_random_field.argtypes = [vp, vp]
+    lib.gudni_upload_frame.restype = C.c_int
+    lib.gudni_upload_frame.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz]
     job_args = [vp, vp, sz, vp, sz, i32, i32, i32, i32, i32, i32, vp, vp]
     lib.gudni_raster_job.restype = C.c_int
     lib.gudni_raster_job.argtypes = job_args

@@ -2,6 +2,9 @@
 
   Rasterizer(spec)           setupOpenCL        (OpenCL/Setup.hs:102-147)
   Rasterizer.upload_common   BuffersInCommon    (OpenCL/CallKernels.hs:208-240)
+  Rasterizer.upload_pictures / upload_random_field / upload_frame
+                             the same buffers split into a resident part (pictures,
+                             random field) and a per-frame part
   Rasterizer.raster_job      raster/generateCall (OpenCL/CallKernels.hs:88-206)
   Rasterizer.queue_jobs      queueRasterJobs    (OpenCL/CallKernels.hs:218-242)
 
@@ -62,6 +65,27 @@ class Rasterizer:
             len(frame.substances), L.ptr(frame.pictures), frame.pictures.size, L.ptr(frame.picture_uses),
             len(frame.picture_uses), L.ptr(frame.radials), len(frame.radials), L.ptr(rf)))
 
+    def upload_pictures(self, pictures) -> None:
+        """Upload a picture pile that stays on the device across frames
+        (gudni_upload_pictures): a scene.PictureLibrary or a uint8 array."""
+        pile = np.ascontiguousarray(getattr(pictures, "pile", pictures), dtype=np.uint8)
+        self._check(self.lib.gudni_upload_pictures(self.ctx, L.ptr(pile), pile.size))
+
+    def upload_random_field(self, random_field: Optional[np.ndarray]) -> None:
+        """Upload the random field kept across frames (None removes it)."""
+        rf = None if random_field is None else np.ascontiguousarray(random_field, dtype=np.float32)
+        if rf is not None and rf.size != L.RANDOM_FIELD_SIZE:
+            raise ValueError(f"the random field holds {L.RANDOM_FIELD_SIZE} floats")
+        self._check(self.lib.gudni_upload_random_field(self.ctx, L.ptr(rf)))
+
+    def upload_frame(self, frame) -> None:
+        """Upload a frame's own piles (gudni_upload_frame); its picture usages point
+        into the resident picture pile (a frame serialized from
+        PictureLibrary.bind)."""
+        self._check(self.lib.gudni_upload_frame(
+            self.ctx, L.ptr(frame.geometry), frame.geometry.size, L.ptr(frame.substances), len(frame.substances),
+            L.ptr(frame.picture_uses), len(frame.picture_uses), L.ptr(frame.radials), len(frame.radials)))
+
     def raster_job(self, frame, job_index: int, out: np.ndarray, frame_number: int = 0) -> None:
         """Rasterize one job into the host bitmap `out` ((H, W) uint32)."""
         job = frame.jobs[job_index]
@@ -72,11 +96,19 @@ class Rasterizer:
             frame.canvas_w, frame.canvas_h, frame.compute_depth, frame_number, job_index, bg.ctypes.data,
             out.ctypes.data))
 
-    def queue_jobs(self, frame, out: Optional[np.ndarray] = None, frame_number: int = 0) -> np.ndarray:
-        """Upload the common buffers and rasterize every job (host buffers)."""
+    def queue_jobs(self, frame, out: Optional[np.ndarray] = None, frame_number: int = 0,
+                   upload: str = "common") -> np.ndarray:
+        """Upload the common buffers and rasterize every job (host buffers).
+        upload="frame" uploads only the frame's own piles and keeps the resident
+        pictures and random field (upload_pictures / upload_random_field)."""
         if out is None:
             out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
-        self.upload_common(frame)
+        if upload == "frame":
+            self.upload_frame(frame)
+        elif upload == "common":
+            self.upload_common(frame)
+        else:
+            raise ValueError(f"upload must be 'common' or 'frame', not {upload!r}")
         for j in range(len(frame.jobs)):
             self.raster_job(frame, j, out, frame_number)
         return out

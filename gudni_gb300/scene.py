@@ -262,6 +262,58 @@ class FlatScene:
     pictures: np.ndarray          # picture pile bytes
     picture_size: np.ndarray
     picture_offset: np.ndarray
+    # the scene's name of each picture in the pile (None: the pictures are numbered)
+    picture_names: Optional[list] = None
+
+
+class PictureLibrary:
+    """Pictures packed once into one RGBA8 pile that stays on the device across
+    frames.
+
+    The reference packs the scene's whole picture map into a fresh pile, and uploads
+    it, for every frame (makePictData, Figure/Picture.hs:159-167, from queueRasterJobs,
+    OpenCL/CallKernels.hs:228-240).  Here every picture gets a fixed 4-byte aligned
+    offset in one pile, uploaded once (Rasterizer.upload_pictures); bind() points a
+    scene's picture usages at those offsets, so a frame uploads only its own piles
+    (Rasterizer.upload_frame).  Texels are read exactly as from a per-frame pile."""
+
+    def __init__(self, pictures):
+        """pictures: a mapping from names to Picture (or (h, w, 4) uint8 arrays), or a
+        sequence of them named 0, 1, ..."""
+        items = pictures.items() if hasattr(pictures, "items") else enumerate(pictures)
+        self.offsets: dict = {}
+        self.sizes: dict = {}
+        chunks, off = [], 0
+        for key, p in items:
+            px = np.ascontiguousarray(getattr(p, "pixels", p), dtype=np.uint8)
+            if px.ndim != 3 or px.shape[2] != 4:
+                raise ValueError(f"picture {key!r} is not an (h, w, 4) RGBA8 bitmap")
+            self.offsets[key] = off
+            self.sizes[key] = (int(px.shape[1]), int(px.shape[0]))
+            chunks.append(px.reshape(-1))
+            off += px.size
+        if off > np.iinfo(np.int32).max:
+            raise ValueError("picture pile beyond 2 GB (offsets are 32-bit)")
+        self.pile = np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)
+
+    def bind(self, flat: "FlatScene") -> "FlatScene":
+        """The same scene with its pictures looked up in this library: usages point
+        into the library's pile and the scene carries no picture bytes of its own."""
+        import dataclasses
+        n = int(flat.picture_offset.size)
+        names = list(flat.picture_names) if flat.picture_names is not None else list(range(n))
+        sizes, offsets = [], []
+        for i, key in enumerate(names):
+            if key not in self.offsets:
+                raise KeyError(f"cannot find picture {key!r} in the picture library")
+            if tuple(int(v) for v in flat.picture_size[i]) != self.sizes[key]:
+                raise ValueError(f"picture {key!r} differs in size from the library's")
+            sizes.append(self.sizes[key])
+            offsets.append(self.offsets[key])
+        return dataclasses.replace(
+            flat, pictures=np.zeros(0, np.uint8),
+            picture_size=np.asarray(sizes, dtype=np.int32).reshape(-1, 2),
+            picture_offset=np.asarray(offsets, dtype=np.int32), picture_names=names)
 
 
 def flatten(scene: Scene, canvas_w: int, canvas_h: int) -> FlatScene:
@@ -387,6 +439,7 @@ def flatten(scene: Scene, canvas_w: int, canvas_h: int) -> FlatScene:
         pictures=np.concatenate(chunks) if chunks else np.zeros(0, np.uint8),
         picture_size=np.asarray(sizes, dtype=np.int32).reshape(-1, 2),
         picture_offset=np.asarray(offsets, dtype=np.int32),
+        picture_names=list(pic_names),
     )
 
 

@@ -130,6 +130,34 @@ int gudni_upload_common(gudni_ctx* ctx,
                         const gudni_radial* radials, size_t n_radials,
                         const float* random_field);
 
+/* Buffers that persist across frames.  The reference re-packs every picture of the
+ * scene's picture map into a fresh pile and re-uploads it, with the random field, for
+ * every frame (makePictData, Figure/Picture.hs:159-167, called from queueRasterJobs,
+ * OpenCL/CallKernels.hs:228-240).  Here a picture pile (RGBA8 bytes, pictures at
+ * 4-byte aligned offsets) and the random field can be uploaded once and kept on the
+ * device; each frame then uploads only its geometry, substances, picture usages and
+ * gradients with gudni_upload_frame.  gudni_upload_common replaces all of them.
+ *
+ * gudni_upload_pictures: the frame already uploaded stays usable when its picture
+ * usages still read inside the new pile; otherwise the next raster call returns
+ * GUDNI_ERR_NOT_READY until gudni_upload_frame is called.  An uploaded batch is
+ * dropped (gudni_batch_upload again).  Like gudni_upload_common, call these when no
+ * launch of this context is in flight.  Host pointers; copies are made before the call
+ * returns.
+ * gudni_upload_random_field: GUDNI_RANDOM_FIELD_SIZE floats; NULL removes the field. */
+int gudni_upload_pictures(gudni_ctx* ctx, const uint8_t* pictures, size_t picture_bytes);
+int gudni_upload_random_field(gudni_ctx* ctx, const float* random_field);
+
+/* Upload one frame's own buffers (the per-frame part of BuffersInCommon,
+ * OpenCL/CallKernels.hs:208-240): geometry pile, substance pile, picture usages --
+ * whose offsets point into the resident picture pile and are checked against it --
+ * and radial gradients.  The resident picture pile and random field are kept. */
+int gudni_upload_frame(gudni_ctx* ctx,
+                       const void* geometry, size_t geometry_bytes,
+                       const float* substances, size_t n_substances,
+                       const gudni_picture_use* picture_uses, size_t n_picture_uses,
+                       const gudni_radial* radials, size_t n_radials);
+
 /* Rasterize one job: the generateThresholds -> sortThresholds -> renderThresholds
  * sequence of generateCall (OpenCL/CallKernels.hs:88-179), fused into one launch.
  * shapes/tiles/out are HOST pointers; `out` receives bitmap_w*bitmap_h BGRA words

@@ -190,3 +190,44 @@ def test_dense_canvas_wide_shapes(tile, tpt):
     want = O.render_frame(frame)
     assert_parity(got, want)
     assert np.array_equal(got, want)
+
+
+def test_resident_pictures_across_frames():
+    """A picture pile uploaded once (gudni_upload_pictures) and frames that upload only
+    their own piles (gudni_upload_frame): two frames with different usages of one
+    texture render exactly as through gudni_upload_common, and within the parity bar of
+    the oracle.  A pile too small for the uploaded frame's usages makes the frame stale
+    (not ready) and is refused for a new frame (bad input)."""
+    import dataclasses
+    spec = L.make_spec(32, 32, 4096, 511, 8)
+    first = G.glyph_page(seed=4, width=320, height=180, n_glyphs=80, n_shapes=12, texture_frac=0.5)
+    xf = first.substance_picture_xform.copy()
+    xf[:, 0] += np.float32(13.0)
+    xf[:, 1] -= np.float32(7.0)
+    xf[:, 2] *= np.float32(1.5)
+    second = dataclasses.replace(first, substance_picture_xform=xf)
+    lib = S.PictureLibrary({1: G.noise_texture(seed=10, size=64), 0: first.pictures.reshape(1024, 1024, 4)})
+    images = []
+    with Rasterizer(spec) as r:
+        r.upload_pictures(lib)
+        r.upload_random_field(S.default_random_field())
+        for flat in (first, second):
+            frame = S.serialize_flat(lib.bind(flat), spec)
+            assert len(frame.picture_uses) > 0
+            r.upload_frame(frame)
+            got = r.raster_frame(frame, upload_common=False)
+            assert np.array_equal(got, render(S.serialize_flat(flat, spec)))
+            assert_parity(got, O.render_frame(dataclasses.replace(frame, pictures=lib.pile)))
+            images.append(got)
+        assert not np.array_equal(images[0], images[1])
+        r.upload_pictures(lib.pile[:16])
+        with pytest.raises(RasterError) as err:
+            r.raster_frame(frame, upload_common=False)
+        assert err.value.code == -6
+        with pytest.raises(RasterError) as err:
+            r.upload_frame(frame)
+        assert err.value.code == -1
+        r.upload_pictures(lib)
+        r.upload_frame(frame)
+        r.upload_pictures(lib)  # the frame's usages still fit: it stays uploaded
+        assert np.array_equal(r.raster_frame(frame, upload_common=False), images[1])
