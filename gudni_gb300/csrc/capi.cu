@@ -24,7 +24,9 @@
 
 #include "adjoint_kernels.h"
 #include "gudni_cuda.h"
+#include "gudni_serialize.h"
 #include "raster_kernels.h"
+#include "serialize_device.cuh"
 #include "strand_table.h"
 
 using gudni::TileLaunch;
@@ -155,6 +157,14 @@ struct gudni_ctx {
   DevBuf<float4> a_bit_grad;
   DevBuf<float4> a_layers;
   DevBuf<int32_t> a_layer_bits;
+  // serializer on the device: the scene's arrays, pass temporaries, the frame's piles
+  DevBuf<int32_t> ser_sub_start, ser_compound, ser_outline_start, ser_pair_start;
+  DevBuf<float> ser_pairs;
+  DevBuf<uint64_t> ser_sub_tag;
+  DevBuf<uint8_t> ser_tmp[gudni::ser::kSlots];
+  DevBuf<gudni_shape> ds_shapes;
+  DevBuf<gudni_tile_info> ds_tiles;
+  DevBuf<int32_t> ds_tile_jobs;
   uint64_t launches = 0;
   cudaStream_t last_stream = nullptr;
 };
@@ -568,6 +578,109 @@ bool adjoint_pointers_ok(const float* target, const float* image, const float* g
          ((uintptr_t)image & 15) == 0 && ((uintptr_t)grad_geometry & 3) == 0 && ((uintptr_t)grad_substances & 3) == 0;
 }
 
+// ---------------------------------------------------------------- device serializer
+// The executor that runs the serializer's passes (serialize_device.cuh) as kernels on
+// the context's stream; results land in the context's frame buffers.
+
+template <class Pass>
+__global__ void __launch_bounds__(256) ser_pass_kernel(Pass pass, uint64_t n) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) pass(i);
+}
+
+constexpr int kScanBlock = 1024;
+
+// Exclusive prefix sum of n values by one block, kScanBlock values per step carried
+// from step to step; out[n] receives the total.
+__global__ void __launch_bounds__(kScanBlock) ser_scan_kernel(const uint64_t* in, uint64_t* out, uint64_t n) {
+  __shared__ uint64_t warp_total[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t carry = 0;
+  for (uint64_t base = 0; base < n; base += kScanBlock) {
+    const uint64_t i = base + threadIdx.x;
+    const uint64_t v = i < n ? in[i] : 0;
+    uint64_t x = v;  // inclusive scan within the warp
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_total[warp] = x;
+    __syncthreads();
+    if (warp == 0) {  // inclusive scan of the warps' totals
+      uint64_t w = warp_total[lane];
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= d) w += y;
+      }
+      warp_total[lane] = w;
+    }
+    __syncthreads();
+    if (i < n) out[i] = carry + (warp ? warp_total[warp - 1] : 0) + (x - v);
+    carry += warp_total[kScanBlock / 32 - 1];
+    __syncthreads();  // warp_total is rewritten by the next step
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+struct SerExec {
+  gudni_ctx* ctx;
+  cudaStream_t stream;
+  cudaError_t err = cudaSuccess;
+
+  int check(cudaError_t e) {
+    if (e == cudaSuccess) return 0;
+    err = e;
+    return -1;
+  }
+  template <class U>
+  void* grow(DevBuf<U>& b, uint64_t bytes) {
+    if (check(b.reserve((size_t)((bytes + sizeof(U) - 1) / sizeof(U))))) return nullptr;
+    return b.ptr;
+  }
+  template <class T>
+  T* alloc(gudni::ser::Slot slot, uint64_t n) {
+    const uint64_t bytes = n * sizeof(T);
+    void* p;
+    switch (slot) {
+      case gudni::ser::kGeometry: p = grow(ctx->geometry, bytes); break;
+      case gudni::ser::kStrandTable: p = grow(ctx->strand_table, bytes); break;
+      case gudni::ser::kStrandY: p = grow(ctx->strand_y, bytes); break;
+      case gudni::ser::kStrandFirst: p = grow(ctx->strand_first, bytes); break;
+      case gudni::ser::kShapes: p = grow(ctx->ds_shapes, bytes); break;
+      case gudni::ser::kTiles: p = grow(ctx->ds_tiles, bytes); break;
+      case gudni::ser::kTileJobs: p = grow(ctx->ds_tile_jobs, bytes); break;
+      default: p = grow(ctx->ser_tmp[slot], bytes); break;
+    }
+    return static_cast<T*>(p);
+  }
+  template <class Pass>
+  int forEach(uint64_t n, const Pass& pass) {
+    if (n == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
+    ser_pass_kernel<Pass><<<grid, 256, 0, stream>>>(pass, n);
+    ctx->launches += 1;
+    return check(cudaGetLastError());
+  }
+  int scan(const uint64_t* in, uint64_t* out, uint64_t n) {
+    ser_scan_kernel<<<1, kScanBlock, 0, stream>>>(in, out, n);
+    ctx->launches += 1;
+    return check(cudaGetLastError());
+  }
+  int read(void* dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    return check(e);
+  }
+  int copy(void* dst, const void* src, size_t bytes) {
+    return check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream));
+  }
+  int upload(void* dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // src may be a temporary
+    return check(e);
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -634,6 +747,10 @@ void gudni_destroy(gudni_ctx* ctx) {
   ctx->a_thr.release(); ctx->a_hdr.release(); ctx->a_prov.release(); ctx->a_lines.release();
   ctx->a_line_grad.release(); ctx->a_idx.release(); ctx->a_bit_grad.release(); ctx->a_layers.release();
   ctx->a_layer_bits.release();
+  ctx->ser_sub_start.release(); ctx->ser_compound.release(); ctx->ser_outline_start.release();
+  ctx->ser_pair_start.release(); ctx->ser_pairs.release(); ctx->ser_sub_tag.release();
+  for (auto& b : ctx->ser_tmp) b.release();
+  ctx->ds_shapes.release(); ctx->ds_tiles.release(); ctx->ds_tile_jobs.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -723,6 +840,94 @@ int gudni_upload_frame(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   ctx->n_radials = n_radials;
   if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "upload");
   ctx->common_ready = true;
+  return GUDNI_OK;
+}
+
+int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* s, gudni_device_frame* frame) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!s || !frame) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null scene or frame");
+  gudni::ser::Scene sc;
+  int64_t n_pairs = 0;
+  std::vector<float4> subs;
+  std::vector<gudni_picture_use> uses;
+  std::vector<gudni_radial> rads;
+  std::vector<uint64_t> tags;
+  const char* why = gudni::ser::checkScene(s, ctx->spec, sc, n_pairs);
+  if (!why) why = gudni::ser::buildSubstances(s, subs, uses, rads, tags);
+  if (why) return fail(ctx, GUDNI_ERR_BAD_INPUT, why);
+  uint64_t extent = 0;
+  int rc = check_picture_uses(ctx, uses.data(), uses.size(), ctx->picture_bytes, &extent);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  ctx->batch_ready = false;
+  drop_graph(ctx);
+  ctx->common_ready = false;
+  const size_t n_sub = (size_t)s->n_substances;
+  if ((rc = upload(ctx, ctx->substances, subs.data(), subs.size(), "substance upload"))) return rc;
+  if ((rc = upload(ctx, ctx->uses, uses.data(), uses.size(), "picture use upload"))) return rc;
+  if ((rc = upload(ctx, ctx->radials, rads.data(), rads.size(), "radial upload"))) return rc;
+  if ((rc = upload(ctx, ctx->ser_sub_tag, tags.data(), tags.size(), "scene upload"))) return rc;
+  if ((rc = upload(ctx, ctx->ser_sub_start, s->substance_shape_start, n_sub ? n_sub + 1 : 0, "scene upload"))) return rc;
+  const size_t shapes_end = (size_t)sc.shape1, outlines_end = (size_t)sc.outline1;
+  const bool any_shape = sc.shape1 > sc.shape0, any_outline = sc.outline1 > sc.outline0;
+  if ((rc = upload(ctx, ctx->ser_compound, s->shape_compound, any_shape ? shapes_end : 0, "scene upload"))) return rc;
+  if ((rc = upload(ctx, ctx->ser_outline_start, s->shape_outline_start, any_shape ? shapes_end + 1 : 0, "scene upload")))
+    return rc;
+  if ((rc = upload(ctx, ctx->ser_pair_start, s->outline_pair_start, any_outline ? outlines_end + 1 : 0, "scene upload")))
+    return rc;
+  if ((rc = upload(ctx, ctx->ser_pairs, s->pairs, any_outline ? 4 * (size_t)n_pairs : 0, "scene upload"))) return rc;
+  cudaError_t e;
+  if (!ctx->pictures.ptr && (e = ctx->pictures.reserve(0)) != cudaSuccess) return cuda_fail(ctx, e, "picture pile");
+  sc.substance_shape_start = ctx->ser_sub_start.ptr;
+  sc.substance_tag = ctx->ser_sub_tag.ptr;
+  sc.shape_compound = ctx->ser_compound.ptr;
+  sc.shape_outline_start = ctx->ser_outline_start.ptr;
+  sc.outline_pair_start = ctx->ser_pair_start.ptr;
+  sc.pairs = ctx->ser_pairs.ptr;
+  gudni::ser::Limits lim{ctx->spec.max_tile_size, ctx->spec.threads_per_tile, ctx->spec.max_tiles_per_call,
+                         ctx->spec.max_shape, (int64_t)ctx->spec.max_strands_per_tile};
+  SerExec ex{ctx, ctx->stream};
+  gudni::ser::Result res;
+  rc = gudni::ser::serialize(ex, sc, lim, res);
+  if (rc == -2) return fail(ctx, GUDNI_ERR_BAD_INPUT, "scene too large for the device serializer");
+  if (rc) return cuda_fail(ctx, ex.err, "device serializer");
+  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "device serializer");
+  ctx->geometry_bytes = res.geometry_bytes;
+  ctx->n_strands = res.n_strands;
+  ctx->n_units = res.geometry_bytes / 16;
+  ctx->n_substances = subs.size();
+  ctx->n_uses = uses.size();
+  ctx->uses_extent = extent;
+  ctx->n_radials = rads.size();
+  ctx->common_ready = true;
+  frame->geometry_bytes = res.geometry_bytes;
+  frame->n_strands = res.n_strands;
+  frame->n_shapes = res.n_shapes;
+  frame->n_tiles = res.n_tiles;
+  frame->n_jobs = res.n_jobs;
+  std::memcpy(frame->stats, res.stats, sizeof(frame->stats));
+  frame->geometry = res.geometry;
+  frame->shapes = res.shapes;
+  frame->tiles = res.tiles;
+  frame->tile_jobs = res.tile_jobs;
+  return GUDNI_OK;
+}
+
+int gudni_device_frame_download(gudni_ctx* ctx, const gudni_device_frame* frame, uint8_t* geometry,
+                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (!frame) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null frame");
+  cudaSetDevice(ctx->device);
+  cudaError_t e = cudaSuccess;
+  auto get = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && dst && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+  };
+  get(geometry, frame->geometry, frame->geometry_bytes);
+  get(shapes, frame->shapes, frame->n_shapes * sizeof(gudni_shape));
+  get(tiles, frame->tiles, frame->n_tiles * sizeof(gudni_tile_info));
+  get(tile_jobs, frame->tile_jobs, frame->n_tiles * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "device frame download");
   return GUDNI_OK;
 }
 

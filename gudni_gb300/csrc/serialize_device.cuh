@@ -1,0 +1,1034 @@
+// The serializer on the device: a flattened scene -> the piles the raster kernels read
+// (geometry pile with its strand table, and the frame's shape and tile piles with the
+// job of every tile), computed by data-parallel passes instead of the host walk.
+//
+// The output is byte for byte the host serializer's (serialize.cpp, which restates
+// Raster/Strand.hs:153-206, Deknob.hs:61-108, ReorderTable.hs:92-110,
+// TileTree.hs:81-204, Job.hs:132-178 and CallKernels.hs:244-255); only the order of
+// the work differs:
+//
+//  * strands: one work item per outline.  A counting pass gives every outline its
+//    byte and strand count, exclusive scans give it its place in the pile, and a
+//    writing pass emits its strands there with their strand-table rows.
+//  * tile tree: the reference inserts shapes one at a time and splits a leaf the first
+//    time an insertion finds it full (checkTileSpace, TileTree.hs:167-172).  A leaf
+//    receives, in insertion order, exactly the shapes whose boxes pass the cut tests
+//    on its path, whenever it was created (a split re-inserts the old contents in
+//    order), and its counts only grow, so it splits if and only if that whole list
+//    holds at least MAXSHAPE shapes or at least max_strands_per_tile strands and the
+//    leaf is wider (HLeaf) or taller (VLeaf) than 8 pixels.  The tree is therefore
+//    built top down, one level of splits per pass: the base tiles' lists first, then
+//    each splitting tile's two children filtered from its list in order.
+//  * jobs: the leaves in the traversal order of traverseTileTree, cut into jobs of
+//    max_tiles_per_call tiles, the last job built first (CallKernels.hs:255), each
+//    tile's shapes newest first; emitted as the concatenated layout of
+//    gudni_raster_tiles_device (one shape pile, tile slices into it, a job per tile).
+//
+// Every pass is a functor over an index range, run by an executor: CUDA kernels in the
+// library (capi.cu), plain loops in the CPU tests, so the arithmetic and indexing
+// checked on the CPU are the ones the GPU runs.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "gudni_cuda.h"
+#include "gudni_serialize.h"
+
+#if defined(__CUDACC__)
+#define GUDNI_SHD __host__ __device__
+#else
+#define GUDNI_SHD
+#endif
+
+namespace gudni {
+namespace ser {
+
+constexpr int kMaxCurves = 16;                  // curves per strand (Strand.hs:178, mAXsECTIONsIZE/2)
+constexpr int kMaxPoints = 2 * kMaxCurves + 1;  // points of the largest strand
+constexpr int kRows = kMaxCurves + 1;           // reorder rows, by curve count
+constexpr int kMinTileSide = 8;                 // mINtILEsIZE (TileTree.hs:170)
+constexpr int kMaxKnobSteps = 64;               // the knob bisection ends in <= 15 steps
+constexpr int kMaxLevels = 64;                  // split passes (each halves a side >= 16)
+constexpr uint32_t kNoStrand = 0xFFFFFFFFu;     // strand map: no strand starts here
+
+struct P2 {
+  float x, y;
+};
+struct Bez {  // start, control, end (Figure/Bezier.hs Bez)
+  P2 a, c, b;
+};
+struct Box {
+  float left, top, right, bottom;
+};
+
+// A shape kept after the canvas test, with what the tile tree needs.
+struct KeptShape {
+  uint64_t tag;
+  uint32_t geo_start;    // 16-byte units
+  uint32_t num_strands;
+  Box box;
+};
+
+// A tile of the tree under construction.  kind: 0 = VLeaf (splits across y),
+// 1 = HLeaf (splits across x); open: may still split.
+struct Node {
+  int32_t left, top, right, bottom;
+  int16_t hdepth, vdepth;
+  uint8_t kind, open;
+  uint8_t pad[2];
+  uint64_t list;     // first entry of its shape list in the pool (kept-shape indices)
+  uint64_t count;    // shapes in the list
+  uint64_t strands;  // their strands
+};
+
+// ------------------------------------------------------------ knobs (Deknob.hs)
+GUDNI_SHD inline P2 between(float t, P2 v0, P2 v1) {  // Deknob.hs:40-41
+  const float u = 1.0f - t;
+  return P2{v0.x * u + v1.x * t, v0.y * u + v1.y * t};
+}
+
+// findSplit (Deknob.hs:61-79): halve the parameter interval toward the half that still
+// bulges in the knob's direction; the point there splits the curve.
+GUDNI_SHD inline void findSplit(bool left, const Bez& z, P2& mid0, P2& on, P2& mid1) {
+  float lo = 0.0f, hi = 1.0f, t = 0.5f;
+  for (int step = 0; step < kMaxKnobSteps; ++step) {
+    mid0 = between(t, z.a, z.c);
+    mid1 = between(t, z.c, z.b);
+    on = between(t, mid0, mid1);
+    if (hi - lo <= 0.0001f) return;
+    if (left ? (mid1.x < on.x) : (mid1.x > on.x)) {
+      const float next = t + ((hi - t) / 2.0f);
+      lo = t;
+      t = next;
+    } else if (left ? (mid0.x < on.x) : (mid0.x > on.x)) {
+      const float next = lo + ((t - lo) / 2.0f);
+      hi = t;
+      t = next;
+    } else {
+      return;
+    }
+  }
+}
+
+// fixKnob (Deknob.hs:85-100): a curve whose control lies left (right) of both ends is
+// split in two; returns the number of curves written to out.
+GUDNI_SHD inline int fixKnob(const Bez& z, Bez out[2]) {
+  const bool left = z.c.x < z.a.x && z.c.x < z.b.x;
+  const bool right = !left && z.c.x > z.a.x && z.c.x > z.b.x;
+  if (!left && !right) {
+    out[0] = z;
+    return 1;
+  }
+  P2 mid0, on, mid1;
+  findSplit(left, z, mid0, on, mid1);
+  out[0] = Bez{z.a, mid0, on};
+  out[1] = Bez{on, mid1, z.b};
+  return 2;
+}
+
+// Consecutive curves share a strand when both run the same horizontal way
+// (Strand.hs:77-81).
+GUDNI_SHD inline int runX(const Bez& z) { return z.a.x < z.b.x ? -1 : (z.a.x > z.b.x ? 1 : 0); }
+GUDNI_SHD inline bool connectable(const Bez& p, const Bez& q) {
+  const int h = runX(p);
+  return h != 0 && h == runX(q);
+}
+
+// The de-knobbed curves of one closed outline in order, produced on the fly: pair i
+// (on-curve point, control) runs to the on-curve point of pair i + 1 (the last back to
+// the first), and each such curve yields one or two curves.
+struct CurveCursor {
+  const float* pairs;
+  int n, i, half, parts;
+  Bez part[2];
+  GUDNI_SHD void start(const float* p, int count) {
+    pairs = p;
+    n = count;
+    i = 0;
+    half = 0;
+    load();
+  }
+  GUDNI_SHD void load() {
+    if (i >= n) return;
+    const int j = i + 1 < n ? i + 1 : 0;
+    const Bez z{P2{pairs[4 * i], pairs[4 * i + 1]}, P2{pairs[4 * i + 2], pairs[4 * i + 3]},
+                P2{pairs[4 * j], pairs[4 * j + 1]}};
+    parts = fixKnob(z, part);
+  }
+  GUDNI_SHD bool done() const { return i >= n; }
+  GUDNI_SHD const Bez& get() const { return part[half]; }
+  GUDNI_SHD void next() {
+    if (++half >= parts) {
+      half = 0;
+      ++i;
+      load();
+    }
+  }
+};
+
+// ------------------------------------------------------------ reorder rows
+// The order in which a strand of k curves (2k + 1 points) stores its points
+// (ReorderTable.hs:44-110): the right end, the left end and its control, then the
+// remaining point/control pairs as a complete binary search tree laid out breadth
+// first.  Computed on the host into rows[k][0 .. 2k].
+inline int treePartition(int n) {  // size of the left subtree of n sorted keys
+  int p = 1;
+  while (p <= n / 2) p *= 2;
+  return (p / 2) - 1 <= n - p ? p - 1 : n - p / 2;
+}
+
+inline void buildReorderRows(int rows[kRows][kMaxPoints]) {
+  for (int k = 0; k < kRows; ++k)
+    for (int i = 0; i < kMaxPoints; ++i) rows[k][i] = -1;
+  for (int k = 1; k < kRows; ++k) {
+    const int size = 2 * k + 1;
+    int* row = rows[k];
+    int m = 0;
+    row[m++] = size - 1;
+    row[m++] = 0;
+    row[m++] = 1;
+    // the (size - 3) / 2 remaining pairs as a search tree over their pair indices,
+    // visited level by level, left to right
+    int lo[kMaxCurves], hi[kMaxCurves];
+    int head = 0, tail = 0;
+    const int pairs = (size - 3) / 2;
+    if (pairs > 0) {
+      lo[tail] = 0;
+      hi[tail] = pairs;
+      ++tail;
+    }
+    while (head < tail) {
+      const int a = lo[head], b = hi[head];
+      ++head;
+      const int root = a + treePartition(b - a);
+      row[m++] = 2 * root + 2;
+      row[m++] = 2 * root + 3;
+      if (root > a) {
+        lo[tail] = a;
+        hi[tail] = root;
+        ++tail;
+      }
+      if (b > root + 1) {
+        lo[tail] = root + 1;
+        hi[tail] = b;
+        ++tail;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ strands of an outline
+// Bytes and strands an outline serializes to (outlineToStrands, Strand.hs:153-178):
+// runs of connectable curves, each cut into strands of at most 16 curves; a strand of
+// k curves takes an 8-byte header and 2k + 1 points of 8 bytes.
+GUDNI_SHD inline void outlineSize(const float* pairs, int n_pairs, uint64_t& bytes, uint64_t& strands) {
+  bytes = 0;
+  strands = 0;
+  if (n_pairs < 2) return;
+  CurveCursor c;
+  c.start(pairs, n_pairs);
+  Bez prev = c.get();
+  c.next();
+  uint64_t run = 1, curves = 1, chunks = 0;
+  while (!c.done()) {
+    const Bez z = c.get();
+    if (!connectable(prev, z)) {
+      chunks += (run + kMaxCurves - 1) / kMaxCurves;
+      run = 0;
+    }
+    ++run;
+    ++curves;
+    prev = z;
+    c.next();
+  }
+  chunks += (run + kMaxCurves - 1) / kMaxCurves;
+  bytes = 16 * chunks + 16 * curves;
+  strands = chunks;
+}
+
+// Where an outline's strands go: the geometry pile, the strand table (offset in 8-byte
+// units, size, left x and right x bits), the y range of each strand's points and the
+// strand starting at each 16-byte unit (strand_table.h builds the same by walking a
+// finished pile).
+struct StrandOut {
+  uint8_t* geo;
+  uint4* table;
+  float2* ys;
+  uint32_t* first;
+  const int* rows;  // kRows x kMaxPoints
+};
+
+GUDNI_SHD inline uint32_t floatBits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
+// One strand: reverseIfBackwards (Strand.hs:137-143), beziersToPoints (:130-134), then
+// the header and the points in reorder-row order (:190-206).
+GUDNI_SHD inline void writeStrand(const Bez* chunk, int m, uint64_t off, uint32_t index, const StrandOut& o) {
+  P2 pts[kMaxPoints];
+  const bool backwards = chunk[0].a.x > chunk[m - 1].b.x;
+  for (int k = 0; k < m; ++k) {
+    const Bez& z = backwards ? chunk[m - 1 - k] : chunk[k];
+    pts[2 * k] = backwards ? z.b : z.a;
+    pts[2 * k + 1] = z.c;
+  }
+  pts[2 * m] = backwards ? chunk[0].a : chunk[m - 1].b;
+  const int len = 2 * m + 1;
+  const uint32_t size = (uint32_t)(1 + len);  // in 8-byte units, header included
+  uint32_t* hdr = reinterpret_cast<uint32_t*>(o.geo + off);
+  hdr[0] = size;
+  hdr[1] = 0u;
+  const int* row = o.rows + m * kMaxPoints;
+  float lo = INFINITY, hi = -INFINITY;
+  bool nan = false;
+  float* p = reinterpret_cast<float*>(o.geo + off + 8);
+  for (int i = 0; i < len; ++i) {
+    const P2 q = pts[row[i]];
+    p[2 * i] = q.x;
+    p[2 * i + 1] = q.y;
+    if (q.y != q.y) nan = true;
+    lo = q.y < lo ? q.y : lo;
+    hi = hi < q.y ? q.y : hi;
+  }
+  o.table[index] = make_uint4((uint32_t)(off / 8), size, floatBits(p[2]), floatBits(p[0]));
+  o.ys[index] = nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+  o.first[off / 16] = index;
+}
+
+// All strands of one outline from byte `off` and strand index `index` on: the run
+// that ends the outline first, then the others in order (the fold's final
+// accumulator heads the list, Strand.hs:98-102), each cut every 16 curves.
+GUDNI_SHD inline void outlineWrite(const float* pairs, int n_pairs, uint64_t off, uint32_t index,
+                                   const StrandOut& o) {
+  if (n_pairs < 2) return;
+  CurveCursor c;
+  c.start(pairs, n_pairs);
+  CurveCursor last = c;  // start of the final run
+  uint64_t last_at = 0, curves = 1;
+  Bez prev = c.get();
+  c.next();
+  while (!c.done()) {
+    const Bez z = c.get();
+    if (!connectable(prev, z)) {
+      last = c;
+      last_at = curves;
+    }
+    prev = z;
+    ++curves;
+    c.next();
+  }
+  Bez chunk[kMaxCurves];
+  for (int pass = 0; pass < 2; ++pass) {
+    CurveCursor cur = last;
+    uint64_t todo = curves - last_at;
+    if (pass == 1) {
+      cur.start(pairs, n_pairs);
+      todo = last_at;
+    }
+    int m = 0;
+    for (uint64_t k = 0; k < todo; ++k) {
+      const Bez z = cur.get();
+      cur.next();
+      if (m > 0 && (m == kMaxCurves || !connectable(chunk[m - 1], z))) {
+        writeStrand(chunk, m, off, index, o);
+        off += 8 + 8 * (uint64_t)(2 * m + 1);
+        ++index;
+        m = 0;
+      }
+      chunk[m++] = z;
+    }
+    if (m > 0) {
+      writeStrand(chunk, m, off, index, o);
+      off += 8 + 8 * (uint64_t)(2 * m + 1);
+      ++index;
+    }
+  }
+}
+
+// ------------------------------------------------------------ tile tree helpers
+GUDNI_SHD inline int adjustedLog(int x) {  // TileTree.hs:74-75: smallest d, 2^d >= x
+  int d = 0;
+  while (d < 31 && (1LL << d) < (long long)x) ++d;
+  return x < 1 ? 0 : d;
+}
+
+// A base tile of the tree (buildTileTree, TileTree.hs:95-109) is reached by a shape
+// when its box passes every cut on the way: left of a cut c when box.left < c, right
+// of it when box.right > c (above / below alike).  The tile's own edges are the
+// nearest such cuts, so the edges inside the canvas square decide.
+GUDNI_SHD inline bool reachesRect(const Box& b, int l, int t, int r, int bo, int side) {
+  return (r == side || b.left < (float)r) && (l == 0 || b.right > (float)l) && (bo == side || b.top < (float)bo) &&
+         (t == 0 || b.bottom > (float)t);
+}
+
+// Base tile number `r` in traversal order: the tree cuts across y, then across x, at
+// every level from the canvas square down to the tile size, visiting top before
+// bottom and left before right, so r interleaves the bits of the tile's row (higher)
+// and column (lower).
+GUDNI_SHD inline void baseTileOf(uint64_t r, int levels, int& col, int& row) {
+  col = 0;
+  row = 0;
+  for (int k = 0; k < levels; ++k) {
+    col |= (int)((r >> (2 * k)) & 1u) << k;
+    row |= (int)((r >> (2 * k + 1)) & 1u) << k;
+  }
+}
+
+// The split rule of checkTileSpace over a whole list (see the file comment).
+GUDNI_SHD inline bool splits(const Node& n, int max_shape, int64_t max_strands) {
+  if (!n.open || n.count == 0) return false;
+  const int side = n.kind == 0 ? n.bottom - n.top : n.right - n.left;
+  if (side <= kMinTileSide) return false;
+  return n.count >= (uint64_t)(max_shape < 0 ? 0 : max_shape) || (int64_t)n.strands >= max_strands;
+}
+
+// The cut of a splitting node and the test its children apply (insertShapeV /
+// insertShapeH, TileTree.hs:117-151; vSplit / hSplit, :175-190).
+GUDNI_SHD inline int cutOf(const Node& n) {
+  return n.kind == 0 ? n.top + (n.bottom - n.top) / 2 : n.left + (n.right - n.left) / 2;
+}
+GUDNI_SHD inline bool inChild(const Node& n, int cut, int child, const Box& b) {
+  const float c = (float)cut;
+  if (n.kind == 0) return child == 0 ? b.top < c : b.bottom > c;
+  return child == 0 ? b.left < c : b.right > c;
+}
+GUDNI_SHD inline Node childOf(const Node& n, int cut, int child) {
+  Node k = n;
+  k.open = 1;
+  if (n.kind == 0) {  // VLeaf -> VTree over two HLeafs
+    k.kind = 1;
+    k.vdepth = (int16_t)(n.vdepth - 1);
+    if (child == 0) k.bottom = cut; else k.top = cut;
+  } else {            // HLeaf -> HTree over two VLeafs
+    k.kind = 0;
+    k.hdepth = (int16_t)(n.hdepth - 1);
+    if (child == 0) k.right = cut; else k.left = cut;
+  }
+  return k;
+}
+
+// ------------------------------------------------------------ passes
+// The flattened scene (gudni_scene_desc) on the executing side; shape, outline and
+// pair indices are the scene's own (absolute), the passes cover [shape0, shape1) and
+// [outline0, outline1).
+struct Scene {
+  int32_t canvas_w, canvas_h;
+  int32_t n_substances;
+  const int32_t* substance_shape_start;
+  const uint64_t* substance_tag;   // per substance: type bits | id (ShapeInfo.hs:89-99)
+  const int32_t* shape_compound;
+  const int32_t* shape_outline_start;
+  const int32_t* outline_pair_start;
+  const float* pairs;
+  int32_t shape0, shape1, outline0, outline1;
+};
+
+struct Limits {
+  int32_t max_tile_size, threads_per_tile, max_tiles_per_call, max_shape;
+  int64_t max_strands;
+};
+
+// per substance: the substance of each of its shapes
+struct ShapeSubstancePass {
+  Scene s;
+  int32_t* shape_sub;
+  GUDNI_SHD void operator()(uint64_t sub) const {
+    for (int32_t sh = s.substance_shape_start[sub]; sh < s.substance_shape_start[sub + 1]; ++sh)
+      shape_sub[sh - s.shape0] = (int32_t)sub;
+  }
+};
+
+// per shape: its box over every pair (boxOf includes the control point), the canvas
+// test (excludeBox, Serialize.hs:97-104) and the shape of each of its outlines
+struct ShapeBoxPass {
+  Scene s;
+  Box* box;
+  uint64_t* keep;
+  int32_t* outline_shape;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    const int32_t sh = s.shape0 + (int32_t)i;
+    Box b{INFINITY, INFINITY, -INFINITY, -INFINITY};
+    for (int32_t o = s.shape_outline_start[sh]; o < s.shape_outline_start[sh + 1]; ++o) {
+      outline_shape[o - s.outline0] = sh;
+      for (int32_t p = s.outline_pair_start[o]; p < s.outline_pair_start[o + 1]; ++p) {
+        const float* q = s.pairs + 4 * (int64_t)p;
+        for (int k = 0; k < 2; ++k) {
+          const float x = q[2 * k], y = q[2 * k + 1];
+          b.left = b.left <= x ? b.left : x;
+          b.top = b.top <= y ? b.top : y;
+          b.right = b.right <= x ? x : b.right;
+          b.bottom = b.bottom <= y ? y : b.bottom;
+        }
+      }
+    }
+    box[i] = b;
+    const bool out = b.left >= (float)s.canvas_w || b.top >= (float)s.canvas_h || b.right <= 0.0f || b.bottom <= 0.0f;
+    keep[i] = out ? 0 : 1;
+  }
+};
+
+// per outline: its bytes and strands (none for an excluded shape's outlines)
+struct OutlineSizePass {
+  Scene s;
+  const int32_t* outline_shape;
+  const uint64_t* keep;
+  uint64_t* bytes;
+  uint64_t* strands;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    const int32_t o = s.outline0 + (int32_t)i;
+    uint64_t b = 0, n = 0;
+    if (keep[outline_shape[i] - s.shape0]) {
+      const int32_t p0 = s.outline_pair_start[o];
+      outlineSize(s.pairs + 4 * (int64_t)p0, s.outline_pair_start[o + 1] - p0, b, n);
+    }
+    bytes[i] = b;
+    strands[i] = n;
+  }
+};
+
+struct FillPass {
+  uint32_t* out;
+  uint32_t value;
+  GUDNI_SHD void operator()(uint64_t i) const { out[i] = value; }
+};
+
+struct OutlineWritePass {
+  Scene s;
+  const int32_t* outline_shape;
+  const uint64_t* keep;
+  const uint64_t* byte_at;    // exclusive scan of the outlines' bytes
+  const uint64_t* strand_at;  // exclusive scan of their strands
+  StrandOut out;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    if (!keep[outline_shape[i] - s.shape0]) return;
+    const int32_t o = s.outline0 + (int32_t)i;
+    const int32_t p0 = s.outline_pair_start[o];
+    outlineWrite(s.pairs + 4 * (int64_t)p0, s.outline_pair_start[o + 1] - p0, byte_at[i], (uint32_t)strand_at[i], out);
+  }
+};
+
+// per shape: the kept shapes in order, with tag, geometry start and strand count
+// (onShape, Serialize.hs:148-177; the tag by makeTag, ShapeInfo.hs:89-99)
+struct KeptPass {
+  Scene s;
+  const int32_t* shape_sub;
+  const Box* box;
+  const uint64_t* keep;
+  const uint64_t* kept_at;
+  const uint64_t* byte_at;
+  const uint64_t* strand_at;
+  KeptShape* kept;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    if (!keep[i]) return;
+    const int32_t sh = s.shape0 + (int32_t)i;
+    const int32_t o0 = s.shape_outline_start[sh] - s.outline0, o1 = s.shape_outline_start[sh + 1] - s.outline0;
+    KeptShape k;
+    const uint64_t comb = s.shape_compound[sh] == GUDNI_COMPOUND_SUBTRACT ? GUDNI_TAG_SUBTRACT : GUDNI_TAG_ADD;
+    k.tag = s.substance_tag[shape_sub[i]] | comb;
+    k.geo_start = (uint32_t)(byte_at[o0] / 16);
+    k.num_strands = (uint32_t)(strand_at[o1] - strand_at[o0]);
+    k.box = box[i];
+    kept[kept_at[i]] = k;
+  }
+};
+
+// per base tile: its place in the tree and the kept shapes that reach it (count pass
+// with list == nullptr, then the fill pass)
+struct BaseTilePass {
+  const KeptShape* kept;
+  uint64_t n_kept;
+  int levels, tile_side, side, depth;
+  Node* nodes;
+  const uint64_t* list_at;  // fill pass: exclusive scan of the counts
+  uint32_t* list;
+  GUDNI_SHD void operator()(uint64_t r) const {
+    int col, row;
+    baseTileOf(r, levels, col, row);
+    const int l = col * tile_side, t = row * tile_side, rr = l + tile_side, b = t + tile_side;
+    uint64_t count = 0, strands = 0;
+    for (uint64_t k = 0; k < n_kept; ++k) {
+      if (!reachesRect(kept[k].box, l, t, rr, b, side)) continue;
+      if (list) list[list_at[r] + count] = (uint32_t)k;
+      ++count;
+      strands += kept[k].num_strands;
+    }
+    if (list) return;
+    Node n;
+    n.left = l;
+    n.top = t;
+    n.right = rr;
+    n.bottom = b;
+    n.hdepth = (int16_t)depth;
+    n.vdepth = (int16_t)depth;
+    n.kind = 0;
+    n.open = 1;
+    n.pad[0] = n.pad[1] = 0;
+    n.list = 0;
+    n.count = count;
+    n.strands = strands;
+    nodes[r] = n;
+  }
+};
+
+struct BaseListAtPass {
+  Node* nodes;
+  const uint64_t* list_at;
+  GUDNI_SHD void operator()(uint64_t r) const { nodes[r].list = list_at[r]; }
+};
+
+// per node of a level: whether it splits, and its children's list sizes
+struct SplitCountPass {
+  const Node* nodes;
+  const KeptShape* kept;
+  const uint32_t* pool;
+  Limits lim;
+  uint64_t* out_nodes;   // nodes it becomes on the next level (1 or 2)
+  uint64_t* out_list;    // list entries its children take
+  uint64_t* child_size;  // 2 per node: children's counts
+  uint64_t* child_strands;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    const Node& n = nodes[i];
+    child_size[2 * i] = child_size[2 * i + 1] = 0;
+    child_strands[2 * i] = child_strands[2 * i + 1] = 0;
+    if (!splits(n, lim.max_shape, lim.max_strands)) {
+      out_nodes[i] = 1;
+      out_list[i] = 0;
+      return;
+    }
+    const int cut = cutOf(n);
+    uint64_t c[2] = {0, 0}, st[2] = {0, 0};
+    for (uint64_t k = 0; k < n.count; ++k) {
+      const KeptShape& s = kept[pool[n.list + k]];
+      for (int ch = 0; ch < 2; ++ch)
+        if (inChild(n, cut, ch, s.box)) {
+          ++c[ch];
+          st[ch] += s.num_strands;
+        }
+    }
+    out_nodes[i] = 2;
+    out_list[i] = c[0] + c[1];
+    child_size[2 * i] = c[0];
+    child_size[2 * i + 1] = c[1];
+    child_strands[2 * i] = st[0];
+    child_strands[2 * i + 1] = st[1];
+  }
+};
+
+// per node of a level: itself (closed) or its two children on the next level, the
+// children's lists filtered from its own in order and appended to the pool
+struct SplitEmitPass {
+  const Node* nodes;
+  const KeptShape* kept;
+  uint32_t* pool;
+  uint64_t pool_used;          // where this level's new lists start
+  Limits lim;
+  const uint64_t* node_at;     // exclusive scan of out_nodes
+  const uint64_t* list_at;     // exclusive scan of out_list
+  const uint64_t* child_size;
+  const uint64_t* child_strands;
+  Node* next;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    const Node& n = nodes[i];
+    const uint64_t at = node_at[i];
+    if (!splits(n, lim.max_shape, lim.max_strands)) {
+      Node k = n;
+      k.open = 0;
+      next[at] = k;
+      return;
+    }
+    const int cut = cutOf(n);
+    uint64_t w[2] = {pool_used + list_at[i], pool_used + list_at[i] + child_size[2 * i]};
+    for (int ch = 0; ch < 2; ++ch) {
+      Node k = childOf(n, cut, ch);
+      k.list = w[ch];
+      k.count = child_size[2 * i + ch];
+      k.strands = child_strands[2 * i + ch];
+      next[at + ch] = k;
+    }
+    for (uint64_t k = 0; k < n.count; ++k) {
+      const uint32_t id = pool[n.list + k];
+      for (int ch = 0; ch < 2; ++ch)
+        if (inChild(n, cut, ch, kept[id].box)) pool[w[ch]++] = id;
+    }
+  }
+};
+
+// Leaf r (traversal order) in the concatenated layout: its job is built r / M; jobs
+// are listed last built first, so the tiles of later jobs come first.
+GUDNI_SHD inline uint64_t leafPosition(uint64_t r, uint64_t leaves, uint64_t per_job) {
+  const uint64_t b = r / per_job;
+  const uint64_t end = (b + 1) * per_job < leaves ? (b + 1) * per_job : leaves;
+  return (leaves - end) + (r - b * per_job);
+}
+
+struct LeafCountPass {
+  const Node* nodes;
+  uint64_t leaves, per_job;
+  uint64_t* counts;  // by position
+  GUDNI_SHD void operator()(uint64_t r) const { counts[leafPosition(r, leaves, per_job)] = nodes[r].count; }
+};
+
+// per leaf: its tile record, its job and its shapes, newest first
+// (accumulateRasterJobs, Job.hs:132-178)
+struct LeafEmitPass {
+  const Node* nodes;
+  const KeptShape* kept;
+  const uint32_t* pool;
+  uint64_t leaves, per_job, n_jobs;
+  int32_t threads_per_tile;
+  const uint64_t* shape_at;  // by position: exclusive scan of the counts
+  gudni_tile_info* tiles;
+  int32_t* tile_jobs;
+  gudni_shape* shapes;
+  GUDNI_SHD void operator()(uint64_t r) const {
+    const Node& n = nodes[r];
+    const uint64_t pos = leafPosition(r, leaves, per_job);
+    const uint64_t b = r / per_job;
+    gudni_tile_info t;
+    t.left = n.left;
+    t.top = n.top;
+    t.right = n.right;
+    t.bottom = n.bottom;
+    t.hdepth = n.hdepth;
+    t.vdepth = n.vdepth;
+    t.column_allocation = (int32_t)((r - b * per_job) * (uint64_t)threads_per_tile);
+    t.shapes.start = (uint32_t)shape_at[pos];
+    t.shapes.length = (uint32_t)n.count;
+    tiles[pos] = t;
+    tile_jobs[pos] = (int32_t)(n_jobs - 1 - b);
+    for (uint64_t k = 0; k < n.count; ++k) {
+      const KeptShape& s = kept[pool[n.list + n.count - 1 - k]];
+      gudni_shape g;
+      g.tag = s.tag;
+      g.geo_start = s.geo_start;
+      g.num_strands = s.num_strands;
+      shapes[shape_at[pos] + k] = g;
+    }
+  }
+};
+
+struct NodeCount {
+  const Node* nodes;
+  uint64_t* out;
+  GUDNI_SHD void operator()(uint64_t i) const { out[i] = nodes[i].count; }
+};
+struct NodeStrands {
+  const Node* nodes;
+  uint64_t* out;
+  GUDNI_SHD void operator()(uint64_t i) const { out[i] = nodes[i].strands; }
+};
+// one item: the largest of n values into out[n] (a short sequential pass over the leaves)
+struct MaxPass {
+  const uint64_t* in;
+  uint64_t n;
+  uint64_t* out;
+  GUDNI_SHD void operator()(uint64_t) const {
+    uint64_t m = 0;
+    for (uint64_t i = 0; i < n; ++i) m = in[i] > m ? in[i] : m;
+    out[n] = m;
+  }
+};
+
+// ------------------------------------------------------------ host side
+// The scene's index arrays: non-negative and non-decreasing over the ranges the
+// passes cover (the shapes the substances list, their outlines, their pairs).
+// Returns nullptr, or why the scene is refused.
+inline const char* checkScene(const gudni_scene_desc* s, const gudni_spec& spec, Scene& sc, int64_t& n_pairs) {
+  auto rising = [](const int32_t* a, int32_t from, int32_t to) {
+    if (a[from] < 0) return false;
+    for (int32_t i = from; i < to; ++i)
+      if (a[i + 1] < a[i]) return false;
+    return true;
+  };
+  if (s->canvas_w <= 0 || s->canvas_h <= 0) return "canvas must be positive";
+  if (spec.max_tile_size <= 0 || spec.max_tiles_per_call <= 0 || spec.threads_per_tile <= 0)
+    return "spec sizes must be positive";
+  if (s->n_substances < 0) return "negative substance count";
+  sc = Scene{};
+  sc.canvas_w = s->canvas_w;
+  sc.canvas_h = s->canvas_h;
+  sc.n_substances = s->n_substances;
+  n_pairs = 0;
+  if (s->n_substances == 0) return nullptr;
+  if (!s->substance_kind || !s->substance_shape_start) return "missing substance arrays";
+  if (!rising(s->substance_shape_start, 0, s->n_substances))
+    return "substance shape starts must be non-negative and non-decreasing";
+  sc.shape0 = s->substance_shape_start[0];
+  sc.shape1 = s->substance_shape_start[s->n_substances];
+  if (sc.shape1 == sc.shape0) return nullptr;
+  if (!s->shape_compound || !s->shape_outline_start) return "missing shape arrays";
+  if (!rising(s->shape_outline_start, sc.shape0, sc.shape1))
+    return "shape outline starts must be non-negative and non-decreasing";
+  sc.outline0 = s->shape_outline_start[sc.shape0];
+  sc.outline1 = s->shape_outline_start[sc.shape1];
+  if (sc.outline1 == sc.outline0) return nullptr;
+  if (!s->outline_pair_start) return "missing outline array";
+  if (!rising(s->outline_pair_start, sc.outline0, sc.outline1))
+    return "outline pair starts must be non-negative and non-decreasing";
+  n_pairs = s->outline_pair_start[sc.outline1];
+  if (n_pairs > 0 && !s->pairs) return "missing pairs";
+  return nullptr;
+}
+
+// Substance records, picture usages and gradients, one per substance in order, and
+// each substance's tag without its compound bits (onSubstance, Serialize.hs:226-264;
+// makeTag, ShapeInfo.hs:89-99): the host serializer's records.  Built on the host:
+// one short record per substance.
+inline const char* buildSubstances(const gudni_scene_desc* s, std::vector<float4>& subs,
+                                   std::vector<gudni_picture_use>& uses, std::vector<gudni_radial>& rads,
+                                   std::vector<uint64_t>& tags) {
+  for (int sub = 0; sub < s->n_substances; ++sub) {
+    const int kind = s->substance_kind[sub];
+    float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint64_t type;
+    if (kind == GUDNI_SUBSTANCE_SOLID) {
+      if (!s->substance_color) return "solid substance without colour";
+      std::memcpy(&rec, s->substance_color + 4 * (size_t)sub, 16);
+      type = GUDNI_TAG_SOLID;
+    } else if (kind == GUDNI_SUBSTANCE_PICTURE) {
+      if (!s->substance_picture || !s->substance_picture_xform || !s->picture_size || !s->picture_offset)
+        return "picture substance without picture arrays";
+      const int pid = s->substance_picture[sub];
+      if (pid < 0 || pid >= s->n_pictures) return "picture index out of range";
+      gudni_picture_use u;
+      u.translate_x = s->substance_picture_xform[3 * (size_t)sub + 0];
+      u.translate_y = s->substance_picture_xform[3 * (size_t)sub + 1];
+      u.size_x = s->picture_size[2 * pid];
+      u.size_y = s->picture_size[2 * pid + 1];
+      u.mem_offset = s->picture_offset[pid];
+      u.scale = s->substance_picture_xform[3 * (size_t)sub + 2];
+      const uint32_t id = (uint32_t)uses.size();
+      uses.push_back(u);
+      std::memcpy(&rec.x, &id, 4);
+      type = GUDNI_TAG_PICTURE;
+    } else if (kind == GUDNI_SUBSTANCE_RADIAL) {
+      if (!s->substance_radial) return "radial substance without gradient";
+      const uint32_t id = (uint32_t)rads.size();
+      rads.push_back(s->substance_radial[sub]);
+      std::memcpy(&rec.x, &id, 4);
+      type = GUDNI_TAG_RADIAL;
+    } else {
+      return "unknown substance kind";
+    }
+    subs.push_back(rec);
+    tags.push_back(type | ((uint64_t)sub & GUDNI_TAG_ID_MASK));
+  }
+  return nullptr;
+}
+
+// ------------------------------------------------------------ the whole serializer
+enum Slot {
+  kGeometry, kStrandTable, kStrandY, kStrandFirst, kShapes, kTiles, kTileJobs,  // results
+  kShapeSub, kBox, kKeep, kKeptAt, kOutlineShape, kOutlineBytes, kByteAt, kOutlineStrands, kStrandAt,
+  kKept, kNodesA, kNodesB, kPoolA, kPoolB, kOutNodes, kNodeAt, kOutList, kListAt, kChildSize,
+  kChildStrands, kLeafCounts, kShapeAt, kReorder,
+  kSlots
+};
+
+struct Result {
+  uint64_t geometry_bytes = 0, n_strands = 0, n_shapes = 0, n_tiles = 0, n_jobs = 0;
+  int64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // as gudni_frame_stats
+  const uint8_t* geometry = nullptr;
+  const uint4* strand_table = nullptr;
+  const float2* strand_y = nullptr;
+  const uint32_t* strand_first = nullptr;
+  const gudni_shape* shapes = nullptr;
+  const gudni_tile_info* tiles = nullptr;
+  const int32_t* tile_jobs = nullptr;
+};
+
+// Runs every pass with executor `ex`:
+//   T* ex.template alloc<T>(Slot, n)     storage for n elements (contents undefined)
+//   int ex.forEach(n, pass)              pass(i) for every i < n (any order)
+//   int ex.scan(in, out, n)              out[i] = in[0] + ... + in[i-1], i <= n
+//   int ex.read(host_dst, src, bytes)    copy to the host
+//   int ex.copy(dst, src, bytes)         copy on the executing side
+//   int ex.upload(dst, host_src, bytes)  copy from the host
+// each returning 0 or an error code; the first error ends the run.
+template <class Ex>
+int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res) {
+  int rc;
+#define GUDNI_SER_TRY(x) \
+  if ((rc = (x)) != 0) return rc
+  const uint64_t n_shapes = (uint64_t)(s.shape1 - s.shape0);
+  const uint64_t n_outlines = (uint64_t)(s.outline1 - s.outline0);
+
+  // reorder rows
+  int rows_h[kRows][kMaxPoints];
+  buildReorderRows(rows_h);
+  int* rows = ex.template alloc<int>(kReorder, (uint64_t)kRows * kMaxPoints);
+  if (!rows) return -1;
+  GUDNI_SER_TRY(ex.upload(rows, &rows_h[0][0], sizeof(rows_h)));
+
+  // shapes: substance, box, canvas test; outlines: their shape and size
+  int32_t* shape_sub = ex.template alloc<int32_t>(kShapeSub, n_shapes);
+  Box* box = ex.template alloc<Box>(kBox, n_shapes);
+  uint64_t* keep = ex.template alloc<uint64_t>(kKeep, n_shapes + 1);
+  uint64_t* kept_at = ex.template alloc<uint64_t>(kKeptAt, n_shapes + 1);
+  int32_t* outline_shape = ex.template alloc<int32_t>(kOutlineShape, n_outlines);
+  uint64_t* obytes = ex.template alloc<uint64_t>(kOutlineBytes, n_outlines + 1);
+  uint64_t* byte_at = ex.template alloc<uint64_t>(kByteAt, n_outlines + 1);
+  uint64_t* ostrands = ex.template alloc<uint64_t>(kOutlineStrands, n_outlines + 1);
+  uint64_t* strand_at = ex.template alloc<uint64_t>(kStrandAt, n_outlines + 1);
+  if (!shape_sub || !box || !keep || !kept_at || !outline_shape || !obytes || !byte_at || !ostrands || !strand_at)
+    return -1;
+  GUDNI_SER_TRY(ex.forEach((uint64_t)s.n_substances, ShapeSubstancePass{s, shape_sub}));
+  GUDNI_SER_TRY(ex.forEach(n_shapes, ShapeBoxPass{s, box, keep, outline_shape}));
+  GUDNI_SER_TRY(ex.forEach(n_outlines, OutlineSizePass{s, outline_shape, keep, obytes, ostrands}));
+  GUDNI_SER_TRY(ex.scan(keep, kept_at, n_shapes));
+  GUDNI_SER_TRY(ex.scan(obytes, byte_at, n_outlines));
+  GUDNI_SER_TRY(ex.scan(ostrands, strand_at, n_outlines));
+  uint64_t n_kept = 0, geo_bytes = 0, n_strands = 0;
+  GUDNI_SER_TRY(ex.read(&n_kept, kept_at + n_shapes, 8));
+  GUDNI_SER_TRY(ex.read(&geo_bytes, byte_at + n_outlines, 8));
+  GUDNI_SER_TRY(ex.read(&n_strands, strand_at + n_outlines, 8));
+  if (n_strands >= 0xFFFFFFF0ull || geo_bytes / 16 > 0xFFFFFFFFull) return -2;
+
+  // the geometry pile and its strand table
+  StrandOut so;
+  so.geo = ex.template alloc<uint8_t>(kGeometry, geo_bytes);
+  so.table = ex.template alloc<uint4>(kStrandTable, n_strands);
+  so.ys = ex.template alloc<float2>(kStrandY, n_strands);
+  so.first = ex.template alloc<uint32_t>(kStrandFirst, geo_bytes / 16);
+  so.rows = rows;
+  if (!so.geo || !so.table || !so.ys || !so.first) return -1;
+  GUDNI_SER_TRY(ex.forEach(geo_bytes / 16, FillPass{so.first, kNoStrand}));
+  GUDNI_SER_TRY(ex.forEach(n_outlines, OutlineWritePass{s, outline_shape, keep, byte_at, strand_at, so}));
+  KeptShape* kept = ex.template alloc<KeptShape>(kKept, n_kept);
+  if (!kept) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_shapes, KeptPass{s, shape_sub, box, keep, kept_at, byte_at, strand_at, kept}));
+
+  // the tile tree: base tiles (buildTileTree, TileTree.hs:81-109)
+  const int canvas_depth = adjustedLog(s.canvas_w > s.canvas_h ? s.canvas_w : s.canvas_h);
+  const int tile_depth = adjustedLog(lim.max_tile_size);
+  const int depth = canvas_depth > tile_depth ? tile_depth : canvas_depth;
+  const int levels = canvas_depth - depth;
+  if (levels > 15) return -2;
+  uint64_t n_nodes = 1ull << (2 * levels);
+  Node* nodes = ex.template alloc<Node>(kNodesA, n_nodes);
+  uint64_t* counts = ex.template alloc<uint64_t>(kOutNodes, n_nodes + 1);
+  uint64_t* list_at = ex.template alloc<uint64_t>(kListAt, n_nodes + 1);
+  if (!nodes || !counts || !list_at) return -1;
+  BaseTilePass base{kept, n_kept, levels, 1 << depth, 1 << canvas_depth, depth, nodes, nullptr, nullptr};
+  GUDNI_SER_TRY(ex.forEach(n_nodes, base));
+  GUDNI_SER_TRY(ex.forEach(n_nodes, NodeCount{nodes, counts}));
+  GUDNI_SER_TRY(ex.scan(counts, list_at, n_nodes));
+  uint64_t pool_used = 0;
+  GUDNI_SER_TRY(ex.read(&pool_used, list_at + n_nodes, 8));
+  uint64_t pool_cap = pool_used + pool_used / 2 + 1024;
+  int pool_slot = kPoolA;
+  uint32_t* pool = ex.template alloc<uint32_t>(Slot(pool_slot), pool_cap);
+  if (!pool) return -1;
+  base.list = pool;
+  base.list_at = list_at;
+  GUDNI_SER_TRY(ex.forEach(n_nodes, base));
+  GUDNI_SER_TRY(ex.forEach(n_nodes, BaseListAtPass{nodes, list_at}));
+
+  // splits, one level per pass, until no tile splits
+  int node_slot = kNodesA;
+  int64_t n_splits = 0;
+  for (int level = 0; level < kMaxLevels; ++level) {
+    uint64_t* out_nodes = ex.template alloc<uint64_t>(kOutNodes, n_nodes + 1);
+    uint64_t* node_at = ex.template alloc<uint64_t>(kNodeAt, n_nodes + 1);
+    uint64_t* out_list = ex.template alloc<uint64_t>(kOutList, n_nodes + 1);
+    uint64_t* lat = ex.template alloc<uint64_t>(kListAt, n_nodes + 1);
+    uint64_t* csize = ex.template alloc<uint64_t>(kChildSize, 2 * n_nodes);
+    uint64_t* cstr = ex.template alloc<uint64_t>(kChildStrands, 2 * n_nodes);
+    if (!out_nodes || !node_at || !out_list || !lat || !csize || !cstr) return -1;
+    GUDNI_SER_TRY(ex.forEach(n_nodes, SplitCountPass{nodes, kept, pool, lim, out_nodes, out_list, csize, cstr}));
+    GUDNI_SER_TRY(ex.scan(out_nodes, node_at, n_nodes));
+    GUDNI_SER_TRY(ex.scan(out_list, lat, n_nodes));
+    uint64_t next_nodes = 0, new_entries = 0;
+    GUDNI_SER_TRY(ex.read(&next_nodes, node_at + n_nodes, 8));
+    GUDNI_SER_TRY(ex.read(&new_entries, lat + n_nodes, 8));
+    if (next_nodes == n_nodes) break;  // nothing split: every node is a leaf
+    n_splits += (int64_t)(next_nodes - n_nodes);
+    if (pool_used + new_entries > pool_cap) {  // grow the pool, keeping its lists
+      const uint64_t cap = 2 * (pool_used + new_entries);
+      const int other = pool_slot == kPoolA ? kPoolB : kPoolA;
+      uint32_t* grown = ex.template alloc<uint32_t>(Slot(other), cap);
+      if (!grown) return -1;
+      if (pool_used) GUDNI_SER_TRY(ex.copy(grown, pool, pool_used * 4));
+      pool = grown;
+      pool_cap = cap;
+      pool_slot = other;
+    }
+    const int other_nodes = node_slot == kNodesA ? kNodesB : kNodesA;
+    Node* next = ex.template alloc<Node>(Slot(other_nodes), next_nodes);
+    if (!next) return -1;
+    GUDNI_SER_TRY(ex.forEach(n_nodes, SplitEmitPass{nodes, kept, pool, pool_used, lim, node_at, lat, csize, cstr, next}));
+    pool_used += new_entries;
+    nodes = next;
+    node_slot = other_nodes;
+    n_nodes = next_nodes;
+    if (level == kMaxLevels - 1) return -2;
+  }
+
+  // jobs: leaves in traversal order, max_tiles_per_call per job, last built first
+  const uint64_t per_job = (uint64_t)lim.max_tiles_per_call;
+  const uint64_t n_jobs = (n_nodes + per_job - 1) / per_job;
+  uint64_t* leaf_counts = ex.template alloc<uint64_t>(kLeafCounts, n_nodes + 1);
+  uint64_t* shape_at = ex.template alloc<uint64_t>(kShapeAt, n_nodes + 1);
+  if (!leaf_counts || !shape_at) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_nodes, LeafCountPass{nodes, n_nodes, per_job, leaf_counts}));
+  GUDNI_SER_TRY(ex.scan(leaf_counts, shape_at, n_nodes));
+  uint64_t n_refs = 0;
+  GUDNI_SER_TRY(ex.read(&n_refs, shape_at + n_nodes, 8));
+  if (n_refs > 0xFFFFFFFFull) return -2;
+  gudni_tile_info* tiles = ex.template alloc<gudni_tile_info>(kTiles, n_nodes);
+  int32_t* tile_jobs = ex.template alloc<int32_t>(kTileJobs, n_nodes);
+  gudni_shape* shapes = ex.template alloc<gudni_shape>(kShapes, n_refs);
+  if (!tiles || !tile_jobs || !shapes) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_nodes, LeafEmitPass{nodes, kept, pool, n_nodes, per_job, n_jobs, lim.threads_per_tile,
+                                                 shape_at, tiles, tile_jobs, shapes}));
+
+  // the largest leaf lists (gudni_frame_stats [5], [6])
+  uint64_t most_shapes = 0, most_strands = 0;
+  {
+    uint64_t* per = ex.template alloc<uint64_t>(kLeafCounts, n_nodes + 1);
+    if (!per) return -1;
+    GUDNI_SER_TRY(ex.forEach(n_nodes, NodeCount{nodes, per}));
+    GUDNI_SER_TRY(ex.forEach(1, MaxPass{per, n_nodes, per}));
+    GUDNI_SER_TRY(ex.read(&most_shapes, per + n_nodes, 8));
+    GUDNI_SER_TRY(ex.forEach(n_nodes, NodeStrands{nodes, per}));
+    GUDNI_SER_TRY(ex.forEach(1, MaxPass{per, n_nodes, per}));
+    GUDNI_SER_TRY(ex.read(&most_strands, per + n_nodes, 8));
+  }
+#undef GUDNI_SER_TRY
+
+  res.geometry_bytes = geo_bytes;
+  res.n_strands = n_strands;
+  res.n_shapes = n_refs;
+  res.n_tiles = n_nodes;
+  res.n_jobs = n_jobs;
+  res.stats[0] = (int64_t)n_kept;
+  res.stats[1] = (int64_t)(n_shapes - n_kept);
+  res.stats[2] = (int64_t)n_strands;
+  res.stats[3] = (int64_t)n_nodes;
+  res.stats[4] = n_splits;
+  res.stats[5] = (int64_t)most_shapes;
+  res.stats[6] = (int64_t)most_strands;
+  res.stats[7] = (int64_t)n_refs;
+  res.geometry = so.geo;
+  res.strand_table = so.table;
+  res.strand_y = so.ys;
+  res.strand_first = so.first;
+  res.shapes = shapes;
+  res.tiles = tiles;
+  res.tile_jobs = tile_jobs;
+  return 0;
+}
+
+}  // namespace ser
+}  // namespace gudni

@@ -5,6 +5,7 @@
   Rasterizer.upload_pictures / upload_random_field / upload_frame
                              the same buffers split into a resident part (pictures,
                              random field) and a per-frame part
+  Rasterizer.serialize_device the host serializer's piles built by kernels
   Rasterizer.raster_job      raster/generateCall (OpenCL/CallKernels.hs:88-206)
   Rasterizer.queue_jobs      queueRasterJobs    (OpenCL/CallKernels.hs:218-242)
 
@@ -139,6 +140,39 @@ class Rasterizer:
         self._check(self.lib.gudni_raster_tiles_device(
             self.ctx, shapes_ptr, n_shapes, tiles_ptr, tile_jobs_ptr or None, n_tiles, frame.canvas_w,
             frame.canvas_h, frame.compute_depth, frame_number, bg.ctypes.data, out_ptr, stream or None))
+
+    def serialize_device(self, flat) -> L.DeviceFrame:
+        """Serialize a flattened scene (scene.FlatScene) on the device
+        (gudni_serialize_device): the same piles as scene.serialize_flat, computed by
+        kernels and kept on the device as this context's current frame.  Its picture
+        offsets point into the resident picture pile (upload_pictures)."""
+        from . import scene as S
+        desc, keep = S.scene_desc(flat)
+        frame = L.DeviceFrame()
+        self._check(self.lib.gudni_serialize_device(self.ctx, C.byref(desc), C.byref(frame)))
+        del keep
+        return frame
+
+    def download_device_frame(self, frame: L.DeviceFrame):
+        """The piles of a device-serialized frame on the host: (geometry, shapes,
+        tiles, tile_jobs), the last three in the concatenated layout
+        (scene.concatenated_piles)."""
+        geo = np.empty(frame.geometry_bytes, np.uint8)
+        shapes = np.empty(frame.n_shapes, L.SHAPE_DTYPE)
+        tiles = np.empty(frame.n_tiles, L.TILE_DTYPE)
+        jobs = np.empty(frame.n_tiles, np.int32)
+        self._check(self.lib.gudni_device_frame_download(self.ctx, C.byref(frame), L.ptr(geo), L.ptr(shapes),
+                                                         L.ptr(tiles), L.ptr(jobs)))
+        return geo, shapes, tiles, jobs
+
+    def raster_device_frame(self, frame: L.DeviceFrame, canvas_w: int, canvas_h: int, background, out_ptr: int,
+                            stream: int = 0, frame_number: int = 0) -> None:
+        """Enqueue the render of a device-serialized frame into the device bitmap at
+        `out_ptr` (canvas_h * canvas_w BGRA words)."""
+        bg = np.ascontiguousarray(background, np.float32)
+        self._check(self.lib.gudni_raster_tiles_device(
+            self.ctx, frame.shapes, frame.n_shapes, frame.tiles, frame.tile_jobs, frame.n_tiles, canvas_w, canvas_h,
+            L.compute_depth(self.spec.threads_per_tile), frame_number, bg.ctypes.data, out_ptr, stream or None))
 
     def enable_counters(self, on: bool = True) -> None:
         self._check(self.lib.gudni_enable_counters(self.ctx, 1 if on else 0))

@@ -551,8 +551,9 @@ def serialize(scene: Scene, canvas_w: int, canvas_h: int, spec: L.Spec,
     return serialize_flat(flat, spec, random_field)
 
 
-def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndarray] = None) -> Frame:
-    lib = L.load_host()
+def scene_desc(flat: FlatScene):
+    """The gudni_scene_desc of a flattened scene, and the arrays it points into (keep
+    them alive while the descriptor is in use)."""
     d = L.SceneDesc()
     d.canvas_w, d.canvas_h = flat.canvas_w, flat.canvas_h
     for i in range(4):
@@ -578,6 +579,12 @@ def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndar
     d.n_pictures = int(flat.picture_offset.size)
     d.picture_size = a(flat.picture_size)
     d.picture_offset = a(flat.picture_offset)
+    return d, keep
+
+
+def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndarray] = None) -> Frame:
+    lib = L.load_host()
+    d, keep = scene_desc(flat)
     h = lib.gudni_serialize(C.byref(d), C.byref(spec))
     if not h:
         raise ValueError("serialize failed: " + lib.gudni_serialize_error().decode())

@@ -158,6 +158,43 @@ int gudni_upload_frame(gudni_ctx* ctx,
                        const gudni_picture_use* picture_uses, size_t n_picture_uses,
                        const gudni_radial* radials, size_t n_radials);
 
+/* The serializer on the device.  gudni_serialize (include/gudni_serialize.h) restates
+ * the reference's host path (Raster/Strand.hs, Deknob.hs, ReorderTable.hs,
+ * TileTree.hs, Job.hs; OpenCL/CallKernels.hs:244-255) as one walk on the CPU; this
+ * entry point computes the same piles on the GPU, byte for byte: the geometry pile
+ * (with the strand table the raster kernels read), and the frame's shape and tile
+ * piles with the job of every tile, concatenated as gudni_raster_tiles_device takes
+ * them (job 0 -- the last job built -- first).  The substance pile, picture usages and
+ * radial gradients are built on the host (one record per substance) and uploaded.
+ * The result is the context's current frame, as after gudni_upload_frame: picture
+ * offsets in `scene` point into the resident picture pile (gudni_upload_pictures) and
+ * are checked against it, and the random field is the resident one.  `scene` holds
+ * host pointers; its index arrays must be non-decreasing.  Render it with
+ * gudni_raster_tiles_device(ctx, frame->shapes, frame->n_shapes, frame->tiles,
+ * frame->tile_jobs, frame->n_tiles, ...).  The device pointers in `frame` stay valid
+ * until the next upload or serialization on this context.  Blocks until done. */
+typedef struct gudni_device_frame {
+    size_t geometry_bytes;
+    size_t n_strands;
+    size_t n_shapes;               /* shape records of all jobs */
+    size_t n_tiles;
+    size_t n_jobs;
+    int64_t stats[8];              /* as gudni_frame_stats */
+    const uint8_t* geometry;       /* device */
+    const gudni_shape* shapes;     /* device: the jobs' shape piles, job 0 first */
+    const gudni_tile_info* tiles;  /* device: shape slices index `shapes` */
+    const int32_t* tile_jobs;      /* device: job index of every tile */
+} gudni_device_frame;
+
+struct gudni_scene_desc;  /* include/gudni_serialize.h */
+int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* scene, gudni_device_frame* frame);
+
+/* Copy a device-serialized frame's piles to host memory (any pointer may be NULL to
+ * skip that pile): geometry_bytes bytes, n_shapes shapes, n_tiles tiles and job
+ * indices.  Blocks until the copies are done. */
+int gudni_device_frame_download(gudni_ctx* ctx, const gudni_device_frame* frame, uint8_t* geometry,
+                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs);
+
 /* Rasterize one job: the generateThresholds -> sortThresholds -> renderThresholds
  * sequence of generateCall (OpenCL/CallKernels.hs:88-179), fused into one launch.
  * shapes/tiles/out are HOST pointers; `out` receives bitmap_w*bitmap_h BGRA words

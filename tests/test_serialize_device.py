@@ -1,0 +1,184 @@
+"""The serializer's device passes (gudni_gb300/csrc/serialize_device.cuh) run on the
+CPU (tests/host_serialize: plain loops in a seeded random item order, built with
+AddressSanitizer and UBSan) against the host serializer (gudni_serialize): the
+geometry pile, the strand table the raster kernels read, the substance, picture-use
+and gradient piles, the concatenated shape and tile piles with every tile's job, and
+the frame counters, byte for byte."""
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+import fixture_scenes as F  # noqa: E402
+from gudni_gb300 import lib as L  # noqa: E402
+from gudni_gb300 import scene as S  # noqa: E402
+from gudni_gb300 import scenes as G  # noqa: E402
+
+pytestmark = pytest.mark.skipif(shutil.which("g++") is None or not os.path.isdir("/usr/local/cuda/include"),
+                                reason="needs g++ and the CUDA headers")
+
+
+def _write(path, arrays):
+    with open(path, "wb") as f:
+        for name, a in arrays.items():
+            b = np.ascontiguousarray(a).tobytes() if not isinstance(a, (bytes, bytearray)) else bytes(a)
+            f.write(np.uint32(len(name)).tobytes() + name.encode() + np.uint64(len(b)).tobytes() + b)
+
+
+def _read(path):
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    at = 0
+    while at < len(data):
+        n = int(np.frombuffer(data, np.uint32, 1, at)[0])
+        name = data[at + 4:at + 4 + n].decode()
+        size = int(np.frombuffer(data, np.uint64, 1, at + 4 + n)[0])
+        out[name] = data[at + 12 + n:at + 12 + n + size]
+        at += 12 + n + size
+    return out
+
+
+def device_passes(flat, spec, seed=1):
+    """The device serializer's output, computed by its passes on the CPU."""
+    from host_serialize.build import build
+    arrays = {
+        "header": np.array([flat.canvas_w, flat.canvas_h, flat.substance_kind.size, flat.picture_offset.size],
+                           np.int32),
+        "spec": bytes(spec),
+        "substance_kind": flat.substance_kind.astype(np.int32),
+        "substance_color": flat.substance_color.astype(np.float32),
+        "substance_picture": flat.substance_picture.astype(np.int32),
+        "substance_picture_xform": flat.substance_picture_xform.astype(np.float32),
+        "substance_radial": flat.substance_radial,
+        "substance_shape_start": flat.substance_shape_start.astype(np.int32),
+        "shape_compound": flat.shape_compound.astype(np.int32),
+        "shape_outline_start": flat.shape_outline_start.astype(np.int32),
+        "outline_pair_start": flat.outline_pair_start.astype(np.int32),
+        "pairs": flat.pairs.astype(np.float32),
+        "picture_size": flat.picture_size.astype(np.int32),
+        "picture_offset": flat.picture_offset.astype(np.int32),
+    }
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = os.path.join(d, "scene.bin"), os.path.join(d, "out.bin")
+        _write(src, arrays)
+        r = subprocess.run([build(), src, dst, str(seed)], capture_output=True, text=True,
+                           env=dict(os.environ, ASAN_OPTIONS="detect_leaks=0"))
+        assert r.returncode == 0, r.stderr[-4000:]
+        return _read(dst)
+
+
+def host_strand_table(geometry):
+    from host_column.build import load
+    lib = load()
+    cap = max(1, geometry.size // 32)
+    table = np.zeros((cap, 4), np.uint32)
+    ys = np.zeros((cap, 2), np.float32)
+    first = np.zeros(geometry.size // 16, np.uint32)
+    n = lib.host_strand_table(geometry.ctypes.data, geometry.size, 1, table.ctypes.data, ys.ctypes.data,
+                              first.ctypes.data, cap)
+    return table[:n], ys[:n], first
+
+
+def check(flat, spec, seeds=(1,)):
+    frame = S.serialize_flat(flat, spec)
+    shapes, tiles, jobs = S.concatenated_piles(frame)
+    table, ys, first = host_strand_table(frame.geometry)
+    for seed in seeds:
+        got = device_passes(flat, spec, seed)
+        assert "error" not in got, got.get("error")
+        assert got["geometry"] == frame.geometry.tobytes()
+        assert got["strand_table"] == table.tobytes()
+        assert got["strand_y"] == ys.tobytes()
+        assert got["strand_first"] == first.tobytes()
+        assert got["substances"] == np.ascontiguousarray(frame.substances, np.float32).tobytes()
+        assert got["picture_uses"] == frame.picture_uses.tobytes()
+        assert got["radials"] == frame.radials.tobytes()
+        assert got["shapes"] == shapes.tobytes()
+        assert got["tiles"] == tiles.tobytes()
+        assert got["tile_jobs"] == jobs.tobytes()
+        assert int(np.frombuffer(got["n_jobs"], np.uint64)[0]) == len(frame.jobs)
+        stats = np.frombuffer(got["stats"], np.int64)
+        assert list(stats) == [frame.stats[k] for k in ("shapes", "excluded", "strands", "tiles", "splits",
+                                                        "max_tile_shapes", "max_tile_strands", "tile_shape_refs")]
+    return frame
+
+
+@pytest.mark.parametrize("name", list(F.SCENES))
+def test_fixture_scenes(name):
+    fn, w, h, spec, _ = F.SCENES[name]
+    check(S.flatten(fn(), w, h), spec)
+
+
+@pytest.mark.parametrize("name", list(F.RANDOM))
+def test_random_fixture_scenes(name):
+    gen, sk = F.RANDOM[name]
+    check(G.random_shapes(**gen), L.make_spec(**sk), seeds=(1, 2))
+
+
+@pytest.mark.parametrize("tile,tpt,max_shape,max_strands,per_call", [
+    (32, 32, 127, 4094, 1024),
+    (16, 64, 7, 4094, 5),      # tiles split down to the 8-pixel minimum
+    (64, 256, 127, 40, 3),     # the strand limit splits; many jobs
+    (8, 32, 3, 4094, 1),       # one tile per job
+    (128, 128, 1, 4094, 7),    # MAXSHAPE 1: every shape splits a tile
+])
+def test_random_scene_specs(tile, tpt, max_shape, max_strands, per_call):
+    spec = L.make_spec(tile, tpt, 4096, 127, 8)
+    spec.max_shape = max_shape
+    spec.max_strands_per_tile = max_strands
+    spec.max_tiles_per_call = per_call
+    frame = check(G.random_shapes(seed=21, width=150, height=97, n_shapes=30), spec, seeds=(3, 4))
+    if tile > 8 and (max_shape < 127 or max_strands < 4094):
+        assert frame.stats["splits"] > 0
+
+
+def test_glyph_page_all_substances():
+    flat = G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25)
+    frame = check(flat, L.make_spec(32, 32, 4096, 511, 8))
+    assert len(frame.radials) > 0 and len(frame.picture_uses) > 0
+
+
+def test_dense_small_canvas_splits_to_the_minimum():
+    flat = G.random_shapes(seed=8, width=87, height=75, n_shapes=300)
+    frame = check(flat, L.make_spec(32, 32, 4096, 127, 8))
+    assert frame.stats["splits"] > 0 and frame.stats["max_tile_shapes"] > 127
+
+
+def test_degenerate_shapes():
+    """Shapes off the canvas (excluded), one-pair outlines (no strands), knobs in both
+    directions, vertical and horizontal runs, NaN and infinite control points, and a
+    substance without shapes."""
+    flat = G.random_shapes(seed=9, width=64, height=48, n_shapes=12, seg_lo=1, seg_hi=6)
+    pairs = flat.pairs.copy()
+    pairs[3] = [np.nan, 5.0, np.inf, 7.0]
+    pairs[7, 2] = -np.inf
+    pairs[10:12] = [[10.0, 10.0, 10.0, 20.0], [10.0, 30.0, 10.0, 40.0]]
+    pairs[-4:] += np.float32(500.0)  # the last shape leaves the canvas
+    sub_start = flat.substance_shape_start.copy()
+    sub_start[2] = sub_start[1]  # substance 1 keeps no shape
+    import dataclasses
+    flat = dataclasses.replace(flat, pairs=pairs, substance_shape_start=sub_start)
+    frame = check(flat, L.make_spec(16, 16, 512, 127, 8))
+    assert frame.stats["excluded"] >= 1
+
+
+def test_one_pixel_canvas_and_empty_scene():
+    check(G.random_shapes(seed=10, width=1, height=1, n_shapes=3), L.make_spec(8, 8, 512, 127, 8))
+    empty = G.random_shapes(seed=10, width=40, height=30, n_shapes=0)
+    check(empty, L.make_spec(16, 16, 512, 127, 8))
+
+
+def test_page_4k():
+    """The 3840x2160 page (12,000 shapes, 16,384 base tiles) at its bench spec."""
+    flat = G.glyph_page()
+    spec = L.make_spec(32, 32, 4096, 127, 8)
+    spec.max_strands_per_tile = 4094
+    check(flat, spec)
