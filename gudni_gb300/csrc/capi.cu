@@ -582,46 +582,6 @@ bool adjoint_pointers_ok(const float* target, const float* image, const float* g
 // The executor that runs the serializer's passes (serialize_device.cuh) as kernels on
 // the context's stream; results land in the context's frame buffers.
 
-template <class Pass>
-__global__ void __launch_bounds__(256) ser_pass_kernel(Pass pass, uint64_t n) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) pass(i);
-}
-
-constexpr int kScanBlock = 1024;
-
-// Exclusive prefix sum of n values by one block, kScanBlock values per step carried
-// from step to step; out[n] receives the total.
-__global__ void __launch_bounds__(kScanBlock) ser_scan_kernel(const uint64_t* in, uint64_t* out, uint64_t n) {
-  __shared__ uint64_t warp_total[kScanBlock / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t carry = 0;
-  for (uint64_t base = 0; base < n; base += kScanBlock) {
-    const uint64_t i = base + threadIdx.x;
-    const uint64_t v = i < n ? in[i] : 0;
-    uint64_t x = v;  // inclusive scan within the warp
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint64_t y = __shfl_up_sync(0xffffffffu, x, d);
-      if (lane >= d) x += y;
-    }
-    if (lane == 31) warp_total[warp] = x;
-    __syncthreads();
-    if (warp == 0) {  // inclusive scan of the warps' totals
-      uint64_t w = warp_total[lane];
-      for (int d = 1; d < 32; d <<= 1) {
-        const uint64_t y = __shfl_up_sync(0xffffffffu, w, d);
-        if (lane >= d) w += y;
-      }
-      warp_total[lane] = w;
-    }
-    __syncthreads();
-    if (i < n) out[i] = carry + (warp ? warp_total[warp - 1] : 0) + (x - v);
-    carry += warp_total[kScanBlock / 32 - 1];
-    __syncthreads();  // warp_total is rewritten by the next step
-  }
-  if (threadIdx.x == 0) out[n] = carry;
-}
-
 struct SerExec {
   gudni_ctx* ctx;
   cudaStream_t stream;
@@ -656,13 +616,14 @@ struct SerExec {
   template <class Pass>
   int forEach(uint64_t n, const Pass& pass) {
     if (n == 0) return 0;
-    const int grid = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
-    ser_pass_kernel<Pass><<<grid, 256, 0, stream>>>(pass, n);
+    const int grid = (int)std::min<uint64_t>((n + gudni::ser::kPassBlock - 1) / gudni::ser::kPassBlock,
+                                              (uint64_t)ctx->sm_count * 8);
+    gudni::ser::pass_kernel<Pass><<<grid, gudni::ser::kPassBlock, 0, stream>>>(pass, n);
     ctx->launches += 1;
     return check(cudaGetLastError());
   }
   int scan(const uint64_t* in, uint64_t* out, uint64_t n) {
-    ser_scan_kernel<<<1, kScanBlock, 0, stream>>>(in, out, n);
+    gudni::ser::scan_kernel<<<1, gudni::ser::kScanBlock, 0, stream>>>(in, out, n);
     ctx->launches += 1;
     return check(cudaGetLastError());
   }

@@ -740,6 +740,52 @@ struct MaxPass {
   }
 };
 
+// ------------------------------------------------------------ kernels of the executor
+#if defined(__CUDACC__)
+constexpr int kPassBlock = 256;
+constexpr int kScanBlock = 1024;
+
+// A pass over items [0, n): grid-stride, one item per thread at a time.
+template <class Pass>
+__global__ void __launch_bounds__(kPassBlock) pass_kernel(Pass pass, uint64_t n) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) pass(i);
+}
+
+// Exclusive prefix sum of n values by one block of kScanBlock threads, kScanBlock
+// values per step with the running total carried from step to step; out[n] receives
+// the total.
+__global__ void __launch_bounds__(kScanBlock) scan_kernel(const uint64_t* in, uint64_t* out, uint64_t n) {
+  __shared__ uint64_t warp_total[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t carry = 0;
+  for (uint64_t base = 0; base < n; base += kScanBlock) {
+    const uint64_t i = base + threadIdx.x;
+    const uint64_t v = i < n ? in[i] : 0;
+    uint64_t x = v;  // inclusive scan within the warp
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_total[warp] = x;
+    __syncthreads();
+    if (warp == 0) {  // inclusive scan of the warps' totals
+      uint64_t w = warp_total[lane];
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= d) w += y;
+      }
+      warp_total[lane] = w;
+    }
+    __syncthreads();
+    if (i < n) out[i] = carry + (warp ? warp_total[warp - 1] : 0) + (x - v);
+    carry += warp_total[kScanBlock / 32 - 1];
+    __syncthreads();  // warp_total is rewritten by the next step
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+#endif
+
 // ------------------------------------------------------------ host side
 // The scene's index arrays: non-negative and non-decreasing over the ranges the
 // passes cover (the shapes the substances list, their outlines, their pairs).

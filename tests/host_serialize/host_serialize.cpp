@@ -11,6 +11,10 @@
 //   host_serialize <scene file> <result file> <seed>
 //
 // Both files are lists of named arrays: u32 name length, name, u64 byte count, bytes.
+//
+// Compiled by nvcc (as CUDA source) the same program runs the passes as the library's
+// kernels (pass_kernel, scan_kernel) with a device executor, so the GPU's result can be
+// compared with the CPU's file byte for byte.
 
 #include <cuda_runtime.h>
 
@@ -72,7 +76,78 @@ struct HostExec {
     std::memcpy(dst, src, bytes);
     return 0;
   }
+  std::vector<uint8_t> fetch(const void* src, size_t bytes) {
+    const uint8_t* p = static_cast<const uint8_t*>(src);
+    return std::vector<uint8_t>(p, p + bytes);
+  }
+  const void* place(const void* host, size_t) { return host; }
 };
+
+#if defined(__CUDACC__)
+// The passes as kernels on the default stream, each slot one device allocation.
+struct DeviceExec {
+  void* ptr[ser::kSlots] = {};
+  size_t cap[ser::kSlots] = {};
+  std::vector<void*> extra;
+  uint64_t rng;
+  int sm_count = 1;
+  ~DeviceExec() {
+    for (void* p : ptr) cudaFree(p);
+    for (void* p : extra) cudaFree(p);
+  }
+  template <class T>
+  T* alloc(ser::Slot s, uint64_t n) {
+    const size_t bytes = (size_t)(n ? n * sizeof(T) : 1);
+    if (bytes > cap[s]) {
+      cudaFree(ptr[s]);
+      ptr[s] = nullptr;
+      cap[s] = 0;
+      if (cudaMalloc(&ptr[s], bytes) != cudaSuccess) return nullptr;
+      cap[s] = bytes;
+    }
+    cudaMemset(ptr[s], 0xA5, bytes);
+    return static_cast<T*>(ptr[s]);
+  }
+  template <class Pass>
+  int forEach(uint64_t n, const Pass& pass) {
+    if (n == 0) return 0;
+    const uint64_t blocks = (n + ser::kPassBlock - 1) / ser::kPassBlock;
+    const int grid = (int)(blocks < (uint64_t)sm_count * 8 ? blocks : (uint64_t)sm_count * 8);
+    ser::pass_kernel<Pass><<<grid, ser::kPassBlock>>>(pass, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
+  int scan(const uint64_t* in, uint64_t* out, uint64_t n) {
+    ser::scan_kernel<<<1, ser::kScanBlock>>>(in, out, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+  }
+  int read(void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : -1;
+  }
+  int copy(void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToDevice) == cudaSuccess ? 0 : -1;
+  }
+  int upload(void* dst, const void* src, size_t bytes) {
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess ? 0 : -1;
+  }
+  std::vector<uint8_t> fetch(const void* src, size_t bytes) {
+    std::vector<uint8_t> v(bytes);
+    if (bytes) cudaMemcpy(v.data(), src, bytes, cudaMemcpyDeviceToHost);
+    return v;
+  }
+  // a device copy of a host array the passes read
+  const void* place(const void* host, size_t bytes) {
+    if (!host || !bytes) return host;
+    void* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+    cudaMemcpy(d, host, bytes, cudaMemcpyHostToDevice);
+    extra.push_back(d);
+    return d;
+  }
+};
+using Exec = DeviceExec;
+#else
+using Exec = HostExec;
+#endif
 
 using Arrays = std::map<std::string, std::vector<uint8_t>>;
 
@@ -148,16 +223,23 @@ int main(int argc, char** argv) {
     std::fclose(out);
     return 0;
   }
-  sc.substance_shape_start = d.substance_shape_start;
-  sc.substance_tag = tags.data();
-  sc.shape_compound = d.shape_compound;
-  sc.shape_outline_start = d.shape_outline_start;
-  sc.outline_pair_start = d.outline_pair_start;
-  sc.pairs = d.pairs;
+  Exec ex;
+  ex.rng = std::strtoull(argv[3], nullptr, 10);
+#if defined(__CUDACC__)
+  cudaDeviceGetAttribute(&ex.sm_count, cudaDevAttrMultiProcessorCount, 0);
+#endif
+  auto bytes_of = [&](const char* name) -> size_t {
+    auto it = a.find(name);
+    return it == a.end() ? 0 : it->second.size();
+  };
+  sc.substance_shape_start = (const int32_t*)ex.place(d.substance_shape_start, bytes_of("substance_shape_start"));
+  sc.substance_tag = (const uint64_t*)ex.place(tags.data(), tags.size() * 8);
+  sc.shape_compound = (const int32_t*)ex.place(d.shape_compound, bytes_of("shape_compound"));
+  sc.shape_outline_start = (const int32_t*)ex.place(d.shape_outline_start, bytes_of("shape_outline_start"));
+  sc.outline_pair_start = (const int32_t*)ex.place(d.outline_pair_start, bytes_of("outline_pair_start"));
+  sc.pairs = (const float*)ex.place(d.pairs, bytes_of("pairs"));
   ser::Limits lim{spec->max_tile_size, spec->threads_per_tile, spec->max_tiles_per_call, spec->max_shape,
                   (int64_t)spec->max_strands_per_tile};
-  HostExec ex;
-  ex.rng = std::strtoull(argv[3], nullptr, 10);
   ser::Result r;
   const int rc = ser::serialize(ex, sc, lim, r);
   if (rc) {
@@ -165,13 +247,17 @@ int main(int argc, char** argv) {
     std::fclose(out);
     return 0;
   }
-  put(out, "geometry", r.geometry, r.geometry_bytes);
-  put(out, "strand_table", r.strand_table, r.n_strands * sizeof(uint4));
-  put(out, "strand_y", r.strand_y, r.n_strands * sizeof(float2));
-  put(out, "strand_first", r.strand_first, r.geometry_bytes / 16 * 4);
-  put(out, "shapes", r.shapes, r.n_shapes * sizeof(gudni_shape));
-  put(out, "tiles", r.tiles, r.n_tiles * sizeof(gudni_tile_info));
-  put(out, "tile_jobs", r.tile_jobs, r.n_tiles * 4);
+  auto put_fetched = [&](const char* name, const void* src, size_t bytes) {
+    const std::vector<uint8_t> v = ex.fetch(src, bytes);
+    put(out, name, v.data(), bytes);
+  };
+  put_fetched("geometry", r.geometry, r.geometry_bytes);
+  put_fetched("strand_table", r.strand_table, r.n_strands * sizeof(uint4));
+  put_fetched("strand_y", r.strand_y, r.n_strands * sizeof(float2));
+  put_fetched("strand_first", r.strand_first, r.geometry_bytes / 16 * 4);
+  put_fetched("shapes", r.shapes, r.n_shapes * sizeof(gudni_shape));
+  put_fetched("tiles", r.tiles, r.n_tiles * sizeof(gudni_tile_info));
+  put_fetched("tile_jobs", r.tile_jobs, r.n_tiles * 4);
   put(out, "substances", subs.data(), subs.size() * sizeof(float4));
   put(out, "picture_uses", uses.data(), uses.size() * sizeof(gudni_picture_use));
   put(out, "radials", rads.data(), rads.size() * sizeof(gudni_radial));
