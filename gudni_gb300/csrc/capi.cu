@@ -165,6 +165,9 @@ struct gudni_ctx {
   DevBuf<gudni_shape> ds_shapes;
   DevBuf<gudni_tile_info> ds_tiles;
   DevBuf<int32_t> ds_tile_jobs;
+  DevBuf<uint32_t> ds_point_offsets;
+  DevBuf<int32_t> ds_point_sources;
+  DevBuf<float> ds_point_weights;
   uint64_t launches = 0;
   cudaStream_t last_stream = nullptr;
 };
@@ -609,6 +612,9 @@ struct SerExec {
       case gudni::ser::kShapes: p = grow(ctx->ds_shapes, bytes); break;
       case gudni::ser::kTiles: p = grow(ctx->ds_tiles, bytes); break;
       case gudni::ser::kTileJobs: p = grow(ctx->ds_tile_jobs, bytes); break;
+      case gudni::ser::kPointOffsets: p = grow(ctx->ds_point_offsets, bytes); break;
+      case gudni::ser::kPointSources: p = grow(ctx->ds_point_sources, bytes); break;
+      case gudni::ser::kPointWeights: p = grow(ctx->ds_point_weights, bytes); break;
       default: p = grow(ctx->ser_tmp[slot], bytes); break;
     }
     return static_cast<T*>(p);
@@ -712,6 +718,7 @@ void gudni_destroy(gudni_ctx* ctx) {
   ctx->ser_pair_start.release(); ctx->ser_pairs.release(); ctx->ser_sub_tag.release();
   for (auto& b : ctx->ser_tmp) b.release();
   ctx->ds_shapes.release(); ctx->ds_tiles.release(); ctx->ds_tile_jobs.release();
+  ctx->ds_point_offsets.release(); ctx->ds_point_sources.release(); ctx->ds_point_weights.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -804,7 +811,7 @@ int gudni_upload_frame(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   return GUDNI_OK;
 }
 
-int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* s, gudni_device_frame* frame) {
+int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* s, int flags, gudni_device_frame* frame) {
   if (!ctx) return GUDNI_ERR_BAD_INPUT;
   if (!s || !frame) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null scene or frame");
   gudni::ser::Scene sc;
@@ -849,7 +856,7 @@ int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* s, gud
                          ctx->spec.max_shape, (int64_t)ctx->spec.max_strands_per_tile};
   SerExec ex{ctx, ctx->stream};
   gudni::ser::Result res;
-  rc = gudni::ser::serialize(ex, sc, lim, res);
+  rc = gudni::ser::serialize(ex, sc, lim, res, (flags & GUDNI_SERIALIZE_PROVENANCE) != 0);
   if (rc == -2) return fail(ctx, GUDNI_ERR_BAD_INPUT, "scene too large for the device serializer");
   if (rc) return cuda_fail(ctx, ex.err, "device serializer");
   if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "device serializer");
@@ -871,11 +878,16 @@ int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* s, gud
   frame->shapes = res.shapes;
   frame->tiles = res.tiles;
   frame->tile_jobs = res.tile_jobs;
+  frame->n_points = res.n_points;
+  frame->point_offsets = res.point_offsets;
+  frame->point_sources = res.point_sources;
+  frame->point_weights = res.point_weights;
   return GUDNI_OK;
 }
 
 int gudni_device_frame_download(gudni_ctx* ctx, const gudni_device_frame* frame, uint8_t* geometry,
-                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs) {
+                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs,
+                                uint32_t* point_offsets, int32_t* point_sources, float* point_weights) {
   if (!ctx) return GUDNI_ERR_BAD_INPUT;
   if (!frame) return fail(ctx, GUDNI_ERR_BAD_INPUT, "null frame");
   cudaSetDevice(ctx->device);
@@ -887,6 +899,10 @@ int gudni_device_frame_download(gudni_ctx* ctx, const gudni_device_frame* frame,
   get(shapes, frame->shapes, frame->n_shapes * sizeof(gudni_shape));
   get(tiles, frame->tiles, frame->n_tiles * sizeof(gudni_tile_info));
   get(tile_jobs, frame->tile_jobs, frame->n_tiles * sizeof(int32_t));
+  if (frame->n_points && !frame->point_offsets) return fail(ctx, GUDNI_ERR_BAD_INPUT, "frame has no provenance");
+  get(point_offsets, frame->point_offsets, frame->n_points * sizeof(uint32_t));
+  get(point_sources, frame->point_sources, frame->n_points * 3 * sizeof(int32_t));
+  get(point_weights, frame->point_weights, frame->n_points * 3 * sizeof(float));
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "device frame download");
   return GUDNI_OK;

@@ -66,6 +66,17 @@ struct Box {
   float left, top, right, bottom;
 };
 
+// Provenance of a serialized point: a fixed combination of at most three points of
+// the scene (2 * pair for a pair's on-curve point, 2 * pair + 1 for its control; -1
+// unused), used to carry gradients on the geometry pile back to the scene.
+struct Prov {
+  int32_t src[3];
+  float w[3];
+};
+struct BezProv {
+  Prov a, c, b;
+};
+
 // A shape kept after the canvas test, with what the tile tree needs.
 struct KeptShape {
   uint64_t tag;
@@ -94,13 +105,13 @@ GUDNI_SHD inline P2 between(float t, P2 v0, P2 v1) {  // Deknob.hs:40-41
 
 // findSplit (Deknob.hs:61-79): halve the parameter interval toward the half that still
 // bulges in the knob's direction; the point there splits the curve.
-GUDNI_SHD inline void findSplit(bool left, const Bez& z, P2& mid0, P2& on, P2& mid1) {
+GUDNI_SHD inline float findSplit(bool left, const Bez& z, P2& mid0, P2& on, P2& mid1) {
   float lo = 0.0f, hi = 1.0f, t = 0.5f;
   for (int step = 0; step < kMaxKnobSteps; ++step) {
     mid0 = between(t, z.a, z.c);
     mid1 = between(t, z.c, z.b);
     on = between(t, mid0, mid1);
-    if (hi - lo <= 0.0001f) return;
+    if (hi - lo <= 0.0001f) return t;
     if (left ? (mid1.x < on.x) : (mid1.x > on.x)) {
       const float next = t + ((hi - t) / 2.0f);
       lo = t;
@@ -110,24 +121,34 @@ GUDNI_SHD inline void findSplit(bool left, const Bez& z, P2& mid0, P2& on, P2& m
       hi = t;
       t = next;
     } else {
-      return;
+      return t;
     }
   }
+  return t;
 }
 
 // fixKnob (Deknob.hs:85-100): a curve whose control lies left (right) of both ends is
-// split in two; returns the number of curves written to out.
-GUDNI_SHD inline int fixKnob(const Bez& z, Bez out[2]) {
+// split in two; returns the number of curves written to out, with their points'
+// provenance (the split points are the de Casteljau combinations at the split t).
+GUDNI_SHD inline int fixKnob(const Bez& z, const BezProv& zp, Bez out[2], BezProv outp[2]) {
   const bool left = z.c.x < z.a.x && z.c.x < z.b.x;
   const bool right = !left && z.c.x > z.a.x && z.c.x > z.b.x;
   if (!left && !right) {
     out[0] = z;
+    outp[0] = zp;
     return 1;
   }
   P2 mid0, on, mid1;
-  findSplit(left, z, mid0, on, mid1);
+  const float t = findSplit(left, z, mid0, on, mid1);
   out[0] = Bez{z.a, mid0, on};
   out[1] = Bez{on, mid1, z.b};
+  const int32_t ia = zp.a.src[0], ic = zp.c.src[0], ib = zp.b.src[0];
+  const float u = 1.0f - t;
+  const Prov pm0{{ia, ic, -1}, {u, t, 0.0f}};
+  const Prov pm1{{ic, ib, -1}, {u, t, 0.0f}};
+  const Prov pon{{ia, ic, ib}, {u * u, 2.0f * t * u, t * t}};
+  outp[0] = BezProv{zp.a, pm0, pon};
+  outp[1] = BezProv{pon, pm1, zp.b};
   return 2;
 }
 
@@ -142,12 +163,17 @@ GUDNI_SHD inline bool connectable(const Bez& p, const Bez& q) {
 // The de-knobbed curves of one closed outline in order, produced on the fly: pair i
 // (on-curve point, control) runs to the on-curve point of pair i + 1 (the last back to
 // the first), and each such curve yields one or two curves.
+GUDNI_SHD inline Prov prov1(int32_t id) { return Prov{{id, -1, -1}, {1.0f, 0.0f, 0.0f}}; }
+
 struct CurveCursor {
   const float* pairs;
+  int32_t pair0;  // scene index of the outline's first pair
   int n, i, half, parts;
   Bez part[2];
-  GUDNI_SHD void start(const float* p, int count) {
+  BezProv partp[2];
+  GUDNI_SHD void start(const float* p, int count, int32_t first_pair) {
     pairs = p;
+    pair0 = first_pair;
     n = count;
     i = 0;
     half = 0;
@@ -158,10 +184,12 @@ struct CurveCursor {
     const int j = i + 1 < n ? i + 1 : 0;
     const Bez z{P2{pairs[4 * i], pairs[4 * i + 1]}, P2{pairs[4 * i + 2], pairs[4 * i + 3]},
                 P2{pairs[4 * j], pairs[4 * j + 1]}};
-    parts = fixKnob(z, part);
+    const BezProv zp{prov1(2 * (pair0 + i)), prov1(2 * (pair0 + i) + 1), prov1(2 * (pair0 + j))};
+    parts = fixKnob(z, zp, part, partp);
   }
   GUDNI_SHD bool done() const { return i >= n; }
   GUDNI_SHD const Bez& get() const { return part[half]; }
+  GUDNI_SHD const BezProv& getProv() const { return partp[half]; }
   GUDNI_SHD void next() {
     if (++half >= parts) {
       half = 0;
@@ -231,7 +259,7 @@ GUDNI_SHD inline void outlineSize(const float* pairs, int n_pairs, uint64_t& byt
   strands = 0;
   if (n_pairs < 2) return;
   CurveCursor c;
-  c.start(pairs, n_pairs);
+  c.start(pairs, n_pairs, 0);
   Bez prev = c.get();
   c.next();
   uint64_t run = 1, curves = 1, chunks = 0;
@@ -261,6 +289,11 @@ struct StrandOut {
   float2* ys;
   uint32_t* first;
   const int* rows;  // kRows x kMaxPoints
+  // optional point provenance, in pile order: 3 sources and 3 weights per point and
+  // the float index of its x in the pile (null: not wanted)
+  int32_t* psrc;
+  float* pw;
+  uint32_t* pat;
 };
 
 GUDNI_SHD inline uint32_t floatBits(float f) {
@@ -275,7 +308,8 @@ GUDNI_SHD inline uint32_t floatBits(float f) {
 
 // One strand: reverseIfBackwards (Strand.hs:137-143), beziersToPoints (:130-134), then
 // the header and the points in reorder-row order (:190-206).
-GUDNI_SHD inline void writeStrand(const Bez* chunk, int m, uint64_t off, uint32_t index, const StrandOut& o) {
+GUDNI_SHD inline void writeStrand(const Bez* chunk, const BezProv* chunkp, int m, uint64_t off, uint32_t index,
+                                  const StrandOut& o) {
   P2 pts[kMaxPoints];
   const bool backwards = chunk[0].a.x > chunk[m - 1].b.x;
   for (int k = 0; k < m; ++k) {
@@ -284,6 +318,26 @@ GUDNI_SHD inline void writeStrand(const Bez* chunk, int m, uint64_t off, uint32_
     pts[2 * k + 1] = z.c;
   }
   pts[2 * m] = backwards ? chunk[0].a : chunk[m - 1].b;
+  if (o.psrc) {  // the points' provenance follows them through the reversal
+    Prov pp[kMaxPoints];
+    for (int k = 0; k < m; ++k) {
+      const BezProv& z = backwards ? chunkp[m - 1 - k] : chunkp[k];
+      pp[2 * k] = backwards ? z.b : z.a;
+      pp[2 * k + 1] = z.c;
+    }
+    pp[2 * m] = backwards ? chunkp[0].a : chunkp[m - 1].b;
+    const int* prow = o.rows + m * kMaxPoints;
+    const uint64_t point0 = (off - 8 * (uint64_t)index) / 8;  // points before this strand
+    for (int i = 0; i < 2 * m + 1; ++i) {
+      const Prov& q = pp[prow[i]];
+      const uint64_t k = point0 + (uint64_t)i;
+      for (int j = 0; j < 3; ++j) {
+        o.psrc[3 * k + j] = q.src[j];
+        o.pw[3 * k + j] = q.w[j];
+      }
+      o.pat[k] = (uint32_t)((off + 8 + 8 * (uint64_t)i) / 4);
+    }
+  }
   const int len = 2 * m + 1;
   const uint32_t size = (uint32_t)(1 + len);  // in 8-byte units, header included
   uint32_t* hdr = reinterpret_cast<uint32_t*>(o.geo + off);
@@ -309,11 +363,11 @@ GUDNI_SHD inline void writeStrand(const Bez* chunk, int m, uint64_t off, uint32_
 // All strands of one outline from byte `off` and strand index `index` on: the run
 // that ends the outline first, then the others in order (the fold's final
 // accumulator heads the list, Strand.hs:98-102), each cut every 16 curves.
-GUDNI_SHD inline void outlineWrite(const float* pairs, int n_pairs, uint64_t off, uint32_t index,
+GUDNI_SHD inline void outlineWrite(const float* pairs, int n_pairs, int32_t pair0, uint64_t off, uint32_t index,
                                    const StrandOut& o) {
   if (n_pairs < 2) return;
   CurveCursor c;
-  c.start(pairs, n_pairs);
+  c.start(pairs, n_pairs, pair0);
   CurveCursor last = c;  // start of the final run
   uint64_t last_at = 0, curves = 1;
   Bez prev = c.get();
@@ -329,27 +383,31 @@ GUDNI_SHD inline void outlineWrite(const float* pairs, int n_pairs, uint64_t off
     c.next();
   }
   Bez chunk[kMaxCurves];
+  BezProv chunkp[kMaxCurves];
   for (int pass = 0; pass < 2; ++pass) {
     CurveCursor cur = last;
     uint64_t todo = curves - last_at;
     if (pass == 1) {
-      cur.start(pairs, n_pairs);
+      cur.start(pairs, n_pairs, pair0);
       todo = last_at;
     }
     int m = 0;
     for (uint64_t k = 0; k < todo; ++k) {
       const Bez z = cur.get();
+      const BezProv zp = cur.getProv();
       cur.next();
       if (m > 0 && (m == kMaxCurves || !connectable(chunk[m - 1], z))) {
-        writeStrand(chunk, m, off, index, o);
+        writeStrand(chunk, chunkp, m, off, index, o);
         off += 8 + 8 * (uint64_t)(2 * m + 1);
         ++index;
         m = 0;
       }
-      chunk[m++] = z;
+      chunk[m] = z;
+      if (o.psrc) chunkp[m] = zp;
+      ++m;
     }
     if (m > 0) {
-      writeStrand(chunk, m, off, index, o);
+      writeStrand(chunk, chunkp, m, off, index, o);
       off += 8 + 8 * (uint64_t)(2 * m + 1);
       ++index;
     }
@@ -514,7 +572,8 @@ struct OutlineWritePass {
     if (!keep[outline_shape[i] - s.shape0]) return;
     const int32_t o = s.outline0 + (int32_t)i;
     const int32_t p0 = s.outline_pair_start[o];
-    outlineWrite(s.pairs + 4 * (int64_t)p0, s.outline_pair_start[o + 1] - p0, byte_at[i], (uint32_t)strand_at[i], out);
+    outlineWrite(s.pairs + 4 * (int64_t)p0, s.outline_pair_start[o + 1] - p0, p0, byte_at[i], (uint32_t)strand_at[i],
+                 out);
   }
 };
 
@@ -878,7 +937,7 @@ enum Slot {
   kGeometry, kStrandTable, kStrandY, kStrandFirst, kShapes, kTiles, kTileJobs,  // results
   kShapeSub, kBox, kKeep, kKeptAt, kOutlineShape, kOutlineBytes, kByteAt, kOutlineStrands, kStrandAt,
   kKept, kNodesA, kNodesB, kPoolA, kPoolB, kOutNodes, kNodeAt, kOutList, kListAt, kChildSize,
-  kChildStrands, kLeafCounts, kShapeAt, kReorder,
+  kChildStrands, kLeafCounts, kShapeAt, kReorder, kPointSources, kPointWeights, kPointOffsets,
   kSlots
 };
 
@@ -892,6 +951,10 @@ struct Result {
   const gudni_shape* shapes = nullptr;
   const gudni_tile_info* tiles = nullptr;
   const int32_t* tile_jobs = nullptr;
+  uint64_t n_points = 0;                    // points of the pile (provenance, when asked)
+  const uint32_t* point_offsets = nullptr;  // float index of each point's x
+  const int32_t* point_sources = nullptr;   // 3 per point
+  const float* point_weights = nullptr;     // 3 per point
 };
 
 // Runs every pass with executor `ex`:
@@ -903,7 +966,7 @@ struct Result {
 //   int ex.upload(dst, host_src, bytes)  copy from the host
 // each returning 0 or an error code; the first error ends the run.
 template <class Ex>
-int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res) {
+int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool provenance = false) {
   int rc;
 #define GUDNI_SER_TRY(x) \
   if ((rc = (x)) != 0) return rc
@@ -949,6 +1012,16 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res) {
   so.first = ex.template alloc<uint32_t>(kStrandFirst, geo_bytes / 16);
   so.rows = rows;
   if (!so.geo || !so.table || !so.ys || !so.first) return -1;
+  const uint64_t n_points = (geo_bytes - 8 * n_strands) / 8;
+  so.psrc = nullptr;
+  so.pw = nullptr;
+  so.pat = nullptr;
+  if (provenance) {
+    so.psrc = ex.template alloc<int32_t>(kPointSources, 3 * n_points);
+    so.pw = ex.template alloc<float>(kPointWeights, 3 * n_points);
+    so.pat = ex.template alloc<uint32_t>(kPointOffsets, n_points);
+    if (!so.psrc || !so.pw || !so.pat) return -1;
+  }
   GUDNI_SER_TRY(ex.forEach(geo_bytes / 16, FillPass{so.first, kNoStrand}));
   GUDNI_SER_TRY(ex.forEach(n_outlines, OutlineWritePass{s, outline_shape, keep, byte_at, strand_at, so}));
   KeptShape* kept = ex.template alloc<KeptShape>(kKept, n_kept);
@@ -1073,6 +1146,10 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res) {
   res.shapes = shapes;
   res.tiles = tiles;
   res.tile_jobs = tile_jobs;
+  res.n_points = provenance ? n_points : 0;
+  res.point_offsets = so.pat;
+  res.point_sources = so.psrc;
+  res.point_weights = so.pw;
   return 0;
 }
 

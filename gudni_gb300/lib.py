@@ -142,7 +142,11 @@ class DeviceFrame(C.Structure):
     _fields_ = [("geometry_bytes", C.c_size_t), ("n_strands", C.c_size_t), ("n_shapes", C.c_size_t),
                 ("n_tiles", C.c_size_t), ("n_jobs", C.c_size_t), ("stats", C.c_int64 * 8),
                 ("geometry", C.c_void_p), ("shapes", C.c_void_p), ("tiles", C.c_void_p),
-                ("tile_jobs", C.c_void_p)]
+                ("tile_jobs", C.c_void_p), ("n_points", C.c_size_t), ("point_offsets", C.c_void_p),
+                ("point_sources", C.c_void_p), ("point_weights", C.c_void_p)]
+
+
+SERIALIZE_PROVENANCE = 1
 
 
 class JobDesc(C.Structure):
@@ -182,9 +186,9 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_upload_frame.restype = C.c_int
     lib.gudni_upload_frame.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz]
     lib.gudni_serialize_device.restype = C.c_int
-    lib.gudni_serialize_device.argtypes = [vp, C.POINTER(SceneDesc), C.POINTER(DeviceFrame)]
+    lib.gudni_serialize_device.argtypes = [vp, C.POINTER(SceneDesc), C.c_int, C.POINTER(DeviceFrame)]
     lib.gudni_device_frame_download.restype = C.c_int
-    lib.gudni_device_frame_download.argtypes = [vp, C.POINTER(DeviceFrame), vp, vp, vp, vp]
+    lib.gudni_device_frame_download.argtypes = [vp, C.POINTER(DeviceFrame), vp, vp, vp, vp, vp, vp, vp]
     job_args = [vp, vp, sz, vp, sz, i32, i32, i32, i32, i32, i32, vp, vp]
     lib.gudni_raster_job.restype = C.c_int
     lib.gudni_raster_job.argtypes = job_args

@@ -141,29 +141,35 @@ class Rasterizer:
             self.ctx, shapes_ptr, n_shapes, tiles_ptr, tile_jobs_ptr or None, n_tiles, frame.canvas_w,
             frame.canvas_h, frame.compute_depth, frame_number, bg.ctypes.data, out_ptr, stream or None))
 
-    def serialize_device(self, flat) -> L.DeviceFrame:
+    def serialize_device(self, flat, provenance: bool = False) -> L.DeviceFrame:
         """Serialize a flattened scene (scene.FlatScene) on the device
         (gudni_serialize_device): the same piles as scene.serialize_flat, computed by
-        kernels and kept on the device as this context's current frame.  Its picture
-        offsets point into the resident picture pile (upload_pictures)."""
+        kernels and kept on the device as this context's current frame, with the
+        points' provenance when asked.  Its picture offsets point into the resident
+        picture pile (upload_pictures)."""
         from . import scene as S
         desc, keep = S.scene_desc(flat)
         frame = L.DeviceFrame()
-        self._check(self.lib.gudni_serialize_device(self.ctx, C.byref(desc), C.byref(frame)))
+        flags = L.SERIALIZE_PROVENANCE if provenance else 0
+        self._check(self.lib.gudni_serialize_device(self.ctx, C.byref(desc), flags, C.byref(frame)))
         del keep
         return frame
 
-    def download_device_frame(self, frame: L.DeviceFrame):
-        """The piles of a device-serialized frame on the host: (geometry, shapes,
-        tiles, tile_jobs), the last three in the concatenated layout
-        (scene.concatenated_piles)."""
-        geo = np.empty(frame.geometry_bytes, np.uint8)
-        shapes = np.empty(frame.n_shapes, L.SHAPE_DTYPE)
-        tiles = np.empty(frame.n_tiles, L.TILE_DTYPE)
-        jobs = np.empty(frame.n_tiles, np.int32)
-        self._check(self.lib.gudni_device_frame_download(self.ctx, C.byref(frame), L.ptr(geo), L.ptr(shapes),
-                                                         L.ptr(tiles), L.ptr(jobs)))
-        return geo, shapes, tiles, jobs
+    def download_device_frame(self, frame: L.DeviceFrame) -> dict:
+        """The piles of a device-serialized frame on the host: geometry, and shapes,
+        tiles and tile_jobs in the concatenated layout (scene.concatenated_piles); with
+        provenance also point_offsets, point_sources and point_weights."""
+        out = {"geometry": np.empty(frame.geometry_bytes, np.uint8),
+               "shapes": np.empty(frame.n_shapes, L.SHAPE_DTYPE),
+               "tiles": np.empty(frame.n_tiles, L.TILE_DTYPE),
+               "tile_jobs": np.empty(frame.n_tiles, np.int32),
+               "point_offsets": np.empty(frame.n_points, np.uint32),
+               "point_sources": np.empty((frame.n_points, 3), np.int32),
+               "point_weights": np.empty((frame.n_points, 3), np.float32)}
+        self._check(self.lib.gudni_device_frame_download(
+            self.ctx, C.byref(frame), *[L.ptr(out[k]) for k in ("geometry", "shapes", "tiles", "tile_jobs",
+                                                                 "point_offsets", "point_sources", "point_weights")]))
+        return out
 
     def raster_device_frame(self, frame: L.DeviceFrame, canvas_w: int, canvas_h: int, background, out_ptr: int,
                             stream: int = 0, frame_number: int = 0) -> None:

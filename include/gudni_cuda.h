@@ -184,16 +184,27 @@ typedef struct gudni_device_frame {
     const gudni_shape* shapes;     /* device: the jobs' shape piles, job 0 first */
     const gudni_tile_info* tiles;  /* device: shape slices index `shapes` */
     const int32_t* tile_jobs;      /* device: job index of every tile */
+    /* with GUDNI_SERIALIZE_PROVENANCE: every point of the geometry pile, in pile order,
+     * as gudni_frame_point_* (include/gudni_serialize.h) gives it; else 0 / NULL */
+    size_t n_points;
+    const uint32_t* point_offsets; /* device: float index of the point's x in the pile */
+    const int32_t* point_sources;  /* device: 3 per point */
+    const float* point_weights;    /* device: 3 per point */
 } gudni_device_frame;
 
+#define GUDNI_SERIALIZE_PROVENANCE 1  /* also record every point's provenance */
+
 struct gudni_scene_desc;  /* include/gudni_serialize.h */
-int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* scene, gudni_device_frame* frame);
+int gudni_serialize_device(gudni_ctx* ctx, const struct gudni_scene_desc* scene, int flags,
+                           gudni_device_frame* frame);
 
 /* Copy a device-serialized frame's piles to host memory (any pointer may be NULL to
  * skip that pile): geometry_bytes bytes, n_shapes shapes, n_tiles tiles and job
- * indices.  Blocks until the copies are done. */
+ * indices, n_points point offsets and 3 * n_points sources and weights.  Blocks until
+ * the copies are done. */
 int gudni_device_frame_download(gudni_ctx* ctx, const gudni_device_frame* frame, uint8_t* geometry,
-                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs);
+                                gudni_shape* shapes, gudni_tile_info* tiles, int32_t* tile_jobs,
+                                uint32_t* point_offsets, int32_t* point_sources, float* point_weights);
 
 /* Rasterize one job: the generateThresholds -> sortThresholds -> renderThresholds
  * sequence of generateCall (OpenCL/CallKernels.hs:88-179), fused into one launch.

@@ -8,7 +8,7 @@
 // random order (the GPU runs them in any order), so a pass that reads another item's
 // output, or memory nobody wrote, changes the result.
 //
-//   host_serialize <scene file> <result file> <seed>
+//   host_serialize <scene file> <result file> <seed> [provenance]
 //
 // Both files are lists of named arrays: u32 name length, name, u64 byte count, bytes.
 //
@@ -241,7 +241,8 @@ int main(int argc, char** argv) {
   ser::Limits lim{spec->max_tile_size, spec->threads_per_tile, spec->max_tiles_per_call, spec->max_shape,
                   (int64_t)spec->max_strands_per_tile};
   ser::Result r;
-  const int rc = ser::serialize(ex, sc, lim, r);
+  const bool provenance = argc > 4 && std::atoi(argv[4]) != 0;
+  const int rc = ser::serialize(ex, sc, lim, r, provenance);
   if (rc) {
     put(out, "error", "serializer failed", 17);
     std::fclose(out);
@@ -258,6 +259,11 @@ int main(int argc, char** argv) {
   put_fetched("shapes", r.shapes, r.n_shapes * sizeof(gudni_shape));
   put_fetched("tiles", r.tiles, r.n_tiles * sizeof(gudni_tile_info));
   put_fetched("tile_jobs", r.tile_jobs, r.n_tiles * 4);
+  if (provenance) {
+    put_fetched("point_offsets", r.point_offsets, r.n_points * 4);
+    put_fetched("point_sources", r.point_sources, r.n_points * 12);
+    put_fetched("point_weights", r.point_weights, r.n_points * 12);
+  }
   put(out, "substances", subs.data(), subs.size() * sizeof(float4));
   put(out, "picture_uses", uses.data(), uses.size() * sizeof(gudni_picture_use));
   put(out, "radials", rads.data(), rads.size() * sizeof(gudni_radial));

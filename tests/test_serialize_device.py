@@ -46,7 +46,7 @@ def _read(path):
     return out
 
 
-def device_passes(flat, spec, seed=1):
+def device_passes(flat, spec, seed=1, provenance=True):
     """The device serializer's output, computed by its passes on the CPU."""
     from host_serialize.build import build
     arrays = {
@@ -69,7 +69,7 @@ def device_passes(flat, spec, seed=1):
     with tempfile.TemporaryDirectory() as d:
         src, dst = os.path.join(d, "scene.bin"), os.path.join(d, "out.bin")
         _write(src, arrays)
-        r = subprocess.run([build(), src, dst, str(seed)], capture_output=True, text=True,
+        r = subprocess.run([build(), src, dst, str(seed), "1" if provenance else "0"], capture_output=True, text=True,
                            env=dict(os.environ, ASAN_OPTIONS="detect_leaks=0"))
         assert r.returncode == 0, r.stderr[-4000:]
         return _read(dst)
@@ -91,8 +91,15 @@ def check(flat, spec, seeds=(1,)):
     frame = S.serialize_flat(flat, spec)
     shapes, tiles, jobs = S.concatenated_piles(frame)
     table, ys, first = host_strand_table(frame.geometry)
-    for seed in seeds:
-        got = device_passes(flat, spec, seed)
+    for n, seed in enumerate(seeds + (seeds[-1] + 100,)):
+        provenance = n < len(seeds)  # the last run without: the piles do not change
+        got = device_passes(flat, spec, seed, provenance)
+        if provenance:
+            assert got["point_offsets"] == frame.point_offsets.astype(np.uint32).tobytes()
+            assert got["point_sources"] == frame.point_sources.astype(np.int32).tobytes()
+            assert got["point_weights"] == frame.point_weights.astype(np.float32).tobytes()
+        else:
+            assert "point_offsets" not in got
         assert "error" not in got, got.get("error")
         assert got["geometry"] == frame.geometry.tobytes()
         assert got["strand_table"] == table.tobytes()

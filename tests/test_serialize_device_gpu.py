@@ -47,15 +47,21 @@ def test_device_serializer_matches_host_and_renders(name):
     with Rasterizer(spec) as r:
         r.upload_pictures(flat.pictures)
         r.upload_random_field(frame.random_field)
-        for _ in range(2):  # a second serialization reuses the context's buffers
-            df = r.serialize_device(flat)
-            geo, d_shapes, d_tiles, d_jobs = r.download_device_frame(df)
-            assert geo.tobytes() == frame.geometry.tobytes()
-            assert d_shapes.tobytes() == shapes.tobytes()
-            assert d_tiles.tobytes() == tiles.tobytes()
-            assert np.array_equal(d_jobs, jobs)
+        for provenance in (True, False):  # the second serialization reuses the context's buffers
+            df = r.serialize_device(flat, provenance=provenance)
+            got = r.download_device_frame(df)
+            assert got["geometry"].tobytes() == frame.geometry.tobytes()
+            assert got["shapes"].tobytes() == shapes.tobytes()
+            assert got["tiles"].tobytes() == tiles.tobytes()
+            assert np.array_equal(got["tile_jobs"], jobs)
             assert df.n_jobs == len(frame.jobs)
             assert list(df.stats) == [frame.stats[k] for k in STATS]
+            if provenance:
+                assert np.array_equal(got["point_offsets"], frame.point_offsets)
+                assert np.array_equal(got["point_sources"], frame.point_sources)
+                assert got["point_weights"].tobytes() == frame.point_weights.tobytes()
+            else:
+                assert df.n_points == 0
         r.raster_device_frame(df, flat.canvas_w, flat.canvas_h, flat.background, out.data_ptr(),
                               stream=L.current_stream_handle())
         r.sync_status()
