@@ -24,7 +24,8 @@ HOST_LIB = os.path.join(BUILD, "libgudni_host.so")
 CUDA_LIB = os.path.join(BUILD, "libgudni_cuda.so")
 
 HOST_SOURCES = [os.path.join(CSRC, "serialize.cpp")]
-CUDA_SOURCES = [os.path.join(CSRC, f) for f in ("raster.cu", "adjoint.cu", "capi.cu", "noalloc.cu")]
+CUDA_SOURCES = [os.path.join(CSRC, f) for f in ("raster.cu", "raster_counter.cu", "adjoint.cu", "capi.cu",
+                                                  "noalloc.cu")]
 HEADERS = [os.path.join(INCLUDE, h) for h in ("gudni_cuda.h", "gudni_serialize.h")] + [
     os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
 

@@ -144,6 +144,8 @@ struct gudni_ctx {
   DevBuf<int64_t> counters;
   bool counters_on = false;
   int dense_min = 0;  // gudni_set_dense_columns (0: per-lane scan only)
+  uint32_t random_mode = gudni::kRandomField;  // gudni_set_random_source
+  uint64_t random_seed = 0;
 
   // adjoint scratch: slots x capacity thresholds, provenance and line records
   int adj_grid = 0;
@@ -314,6 +316,8 @@ gudni::RasterInputs inputs(gudni_ctx* ctx, const gudni_shape* d_shapes, size_t n
   in.n_strands = (uint32_t)ctx->n_strands;
   in.strand_first = ctx->strand_first.ptr;
   in.n_units = (uint32_t)ctx->n_units;
+  in.random_mode = ctx->random_mode;
+  in.random_seed = ctx->random_seed;
   return in;
 }
 
@@ -1200,6 +1204,16 @@ int gudni_enable_counters(gudni_ctx* ctx, int enable) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
   ctx->counters_on = enable != 0;
+  return GUDNI_OK;
+}
+
+int gudni_set_random_source(gudni_ctx* ctx, int source, uint64_t seed) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if (source != GUDNI_RANDOM_FIELD && source != GUDNI_RANDOM_COUNTER)
+    return fail(ctx, GUDNI_ERR_BAD_INPUT, "unknown random source");
+  drop_graph(ctx);  // a captured batch holds the old setting
+  ctx->random_mode = source == GUDNI_RANDOM_COUNTER ? gudni::kRandomCounter : gudni::kRandomField;
+  ctx->random_seed = seed;
   return GUDNI_OK;
 }
 

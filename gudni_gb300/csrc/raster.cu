@@ -34,54 +34,12 @@
 
 #include <algorithm>
 
+#include "column_kernels.cuh"
 #include "raster_device.cuh"
 #include "raster_kernels.h"
 #include "warp_column.cuh"
 
 namespace gudni {
-
-template <int SECTIONS>
-__global__ void __launch_bounds__(kRasterBlock) raster_tiles_kernel(TileLaunch a) {
-  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
-  uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
-  uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
-  int status = 0;
-  for (;;) {
-    uint32_t k = 0;
-    if (lane == 0) k = atomicAdd(a.next_tile, 1u);
-    k = __shfl_sync(0xffffffffu, k, 0);
-    if (k >= a.n_units) break;
-    int tile, chunk;
-    unitOf(a.units, a.chunk_log2, k, tile, chunk);
-    bool ok;
-    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
-    if (!ok) continue;
-    const gudni_tile_info ti = in.tiles[tile];
-    if (!tileOk(ti, in.n_shapes) || in.log2_tpt < 0 || in.log2_tpt > kMaxLog2Tpt) {
-      status |= kStatusBadInput;
-      continue;
-    }
-    const int tpt = 1 << in.log2_tpt;
-    const int column = chunk * 32 + lane;
-    if (column < tpt) {
-      if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) {
-        if (a.overflow_items) {
-          const uint32_t n = atomicAdd(a.overflow_count, 1u);
-          if (n < a.overflow_cap) {
-            a.overflow_items[n] = (k << kLaneBits) | (uint32_t)lane;
-          } else {
-            status |= kStatusOverflow;
-          }
-        } else {
-          status |= kStatusOverflow;
-        }
-      }
-    }
-  }
-  if (status) atomicOr(a.status, status);
-}
 
 template <int SECTIONS>
 __global__ void __launch_bounds__(kRasterBlock) raster_tiles_warp_kernel(TileLaunch a) {
@@ -127,29 +85,6 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_warp_kernel(TileLau
         status |= kStatusOverflow;
       }
     }
-  }
-  if (status) atomicOr(a.status, status);
-}
-
-template <int SECTIONS>
-__global__ void __launch_bounds__(kRasterBlock) raster_list_kernel(TileLaunch a) {
-  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t nslots = gridDim.x * blockDim.x;
-  float4* thr = a.scratch.thr + (size_t)slot * (size_t)a.scratch.capacity;
-  uint32_t* hdr = a.scratch.hdr + (size_t)slot * (size_t)a.scratch.capacity;
-  uint32_t* idx = a.scratch.idx + (size_t)slot * (size_t)a.scratch.idx_stride;
-  int status = 0;
-  const uint32_t n_items = min(*a.list_count, a.list_cap);
-  for (uint32_t w = slot; w < n_items; w += nslots) {
-    const uint32_t item = a.list[w];
-    int tile, chunk;
-    unitOf(a.units, a.chunk_log2, item >> kLaneBits, tile, chunk);
-    const int column = chunk * 32 + (int)(item & ((1u << kLaneBits) - 1u));
-    bool ok;
-    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
-    if (!ok) continue;
-    const gudni_tile_info ti = in.tiles[tile];
-    if (runColumn<SECTIONS>(in, ti, column, thr, hdr, a.scratch.capacity, idx, status)) status |= kStatusOverflow;
   }
   if (status) atomicOr(a.status, status);
 }
@@ -219,16 +154,20 @@ int sections_for(int max_shape) {
 template <int S>
 static cudaError_t launch_s(const TileLaunch& a, bool list, int grid, cudaStream_t stream) {
   if (list) {
-    raster_list_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+    raster_list_kernel<S, false><<<grid, kRasterBlock, 0, stream>>>(a);
   } else if (a.dense_min > 0) {
     raster_tiles_warp_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
   } else {
-    raster_tiles_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+    raster_tiles_kernel<S, false><<<grid, kRasterBlock, 0, stream>>>(a);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream) {
+  // the counter-based jitter runs on its own instantiation of the per-lane kernels
+  // (raster_counter.cu; the warp-cooperative scan of dense columns is not used then)
+  if (a.in.random_mode == kRandomCounter && a.in.stochastic != 0.0f)
+    return launch_raster_counter(a, list, sections, grid, stream);
   switch (sections) {
     case 1: return launch_s<1>(a, list, grid, stream);
     case 2: return launch_s<2>(a, list, grid, stream);
@@ -243,12 +182,12 @@ cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid
 cudaError_t raster_occupancy(int sections, int* blocks_per_sm) {
   const void* fn = nullptr;
   switch (sections) {
-    case 1: fn = (const void*)raster_tiles_kernel<1>; break;
-    case 2: fn = (const void*)raster_tiles_kernel<2>; break;
-    case 4: fn = (const void*)raster_tiles_kernel<4>; break;
-    case 8: fn = (const void*)raster_tiles_kernel<8>; break;
-    case 16: fn = (const void*)raster_tiles_kernel<16>; break;
-    case 32: fn = (const void*)raster_tiles_kernel<32>; break;
+    case 1: fn = (const void*)raster_tiles_kernel<1, false>; break;
+    case 2: fn = (const void*)raster_tiles_kernel<2, false>; break;
+    case 4: fn = (const void*)raster_tiles_kernel<4, false>; break;
+    case 8: fn = (const void*)raster_tiles_kernel<8, false>; break;
+    case 16: fn = (const void*)raster_tiles_kernel<16, false>; break;
+    case 32: fn = (const void*)raster_tiles_kernel<32, false>; break;
     default: return cudaErrorInvalidValue;
   }
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kRasterBlock, 0);

@@ -80,7 +80,35 @@ struct RasterInputs {
   uint32_t n_strands;
   const uint32_t* strand_first;  // per 16-byte unit of the pile: strand index starting there
   uint32_t n_units;              // geometry_bytes / 16
+  // Source of the stochastic area jitter (read only when stochastic != 0):
+  // kRandomField, the reference's random field walked by a per-column cursor, or
+  // kRandomCounter, a counter-based hash of (random_seed, pixel, the section's ordinal
+  // in the column's scan), which needs no table and does not repeat every 4096
+  // sections.
+  uint32_t random_mode = 0;
+  uint64_t random_seed = 0;
 };
+
+constexpr uint32_t kRandomField = 0;
+constexpr uint32_t kRandomCounter = 1;
+
+// SplitMix64's output function (Steele, Lea and Flood, "Fast splittable pseudorandom
+// number generators", OOPSLA 2014): a bijective 64-bit mix.
+__host__ __device__ __forceinline__ uint64_t splitMix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// The counter-based jitter of pixel (x, y) for the section with ordinal k in its
+// column's scan: the top 24 bits of the mixed counter as a float in [0, 1) (exact:
+// 24 bits times 2^-24).
+__host__ __device__ __forceinline__ float counterRandom(uint64_t seed, int x, int y, uint32_t k) {
+  const uint64_t pixel = ((uint64_t)(uint32_t)x << 32) | (uint64_t)(uint32_t)y;
+  const uint64_t h = splitMix64(splitMix64(seed ^ pixel) + (uint64_t)k);
+  return (float)(uint32_t)(h >> 40) * (1.0f / 16777216.0f);
+}
 
 // A strand table entry (16 bytes, one load): x = byte offset / 8 of the strand in the
 // geometry pile, y = its size in 8-byte units, z = bits of the strand's left x,
@@ -955,7 +983,9 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 // K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
 // `image` (optional): instead of the BGRA word, write each pixel's colour before the
 // byte conversion and its section-area sum as a float4 (the adjoint's forward pass).
-template <int SECTIONS>
+// kCounterJitter: take the stochastic jitter from counterRandom (kRandomCounter) in
+// place of the random field; the default instantiation is the reference's scan.
+template <int SECTIONS, bool kCounterJitter = false>
 __device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
                                              ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
                                              int shapeBits, float4* image = nullptr) {
@@ -966,8 +996,8 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   p.sStartY = 0.0f;
   p.sEndX = kRight;
   p.sEndY = 0.0f;
-  int cursor = 0;
-  if (in.stochastic != 0.0f && in.random_field) {  // initRandomField K:1597-1606
+  int cursor = 0;  // the random field cursor, or the column's section ordinal (kCounterJitter)
+  if (!kCounterJitter && in.stochastic != 0.0f && in.random_field) {  // initRandomField K:1597-1606
     cursor = (int)(__float_as_uint(in.random_field[c.threadUnique & (GUDNI_RANDOM_FIELD_SIZE - 1)]) &
                    (GUDNI_RANDOM_FIELD_SIZE - 1));
   }
@@ -1024,8 +1054,14 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       }
       float area = (p.sEndX - p.sStartX) * (p.sEndY - p.sStartY);
       if (in.stochastic != 0.0f) {  // getRandom K:1608-1613
-        cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);
-        const float random = in.random_field ? in.random_field[cursor] : 0.0f;
+        float random;
+        if (kCounterJitter) {
+          random = counterRandom(in.random_seed, px, py, (uint32_t)cursor);
+          cursor += 1;
+        } else {
+          cursor = (cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);
+          random = in.random_field ? in.random_field[cursor] : 0.0f;
+        }
         area = area + (area * random * in.stochastic);
       }
       acc0 += color.x * area;
@@ -1054,7 +1090,7 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
 }
 
 // One column, start to finish.  Returns true when the queue overflowed `cap`.
-template <int SECTIONS>
+template <int SECTIONS, bool kCounterJitter = false>
 __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_tile_info& ti, int column,
                                           float4* thr, uint32_t* hdr, int cap, uint32_t* idx, int& status) {
   const ColumnState c = initColumn(in, ti, column, in.job_index);
@@ -1076,9 +1112,9 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
     one.clear();
     one.w[0] = stack.word(0);
     one.nz = one.w[0] ? 1u : 0u;
-    renderColumn<1>(in, c, q, one, idx, status, (int)bits);
+    renderColumn<1, kCounterJitter>(in, c, q, one, idx, status, (int)bits);
   } else {
-    renderColumn<SECTIONS>(in, c, q, stack, idx, status, (int)bits);
+    renderColumn<SECTIONS, kCounterJitter>(in, c, q, stack, idx, status, (int)bits);
   }
   return q.overflow;
 }

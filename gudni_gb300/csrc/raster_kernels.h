@@ -103,6 +103,8 @@ __device__ __forceinline__ RasterInputs sceneInputs(const RasterInputs& base, co
 
 int sections_for(int max_shape);
 cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream);
+// the same kernels with the counter-based jitter (raster_counter.cu)
+cudaError_t launch_raster_counter(const TileLaunch& a, bool list, int sections, int grid, cudaStream_t stream);
 // Cost-descending work units of a frame's tiles (3 launches); words128: 128 words of
 // scratch (bucket counts and cursors), units: n_tiles << chunk_log2 entries.
 cudaError_t launch_tile_order(const gudni_tile_info* tiles, uint32_t n_tiles, const gudni_shape* shapes,

@@ -147,6 +147,7 @@ class DeviceFrame(C.Structure):
 
 
 SERIALIZE_PROVENANCE = 1
+RANDOM_FIELD, RANDOM_COUNTER = 0, 1  # gudni_set_random_source
 
 
 class JobDesc(C.Structure):
@@ -185,6 +186,8 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_upload_random_field.argtypes = [vp, vp]
     lib.gudni_upload_frame.restype = C.c_int
     lib.gudni_upload_frame.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz]
+    lib.gudni_set_random_source.restype = C.c_int
+    lib.gudni_set_random_source.argtypes = [vp, C.c_int, C.c_uint64]
     lib.gudni_serialize_device.restype = C.c_int
     lib.gudni_serialize_device.argtypes = [vp, C.POINTER(SceneDesc), C.c_int, C.POINTER(DeviceFrame)]
     lib.gudni_device_frame_download.restype = C.c_int

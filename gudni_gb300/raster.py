@@ -183,6 +183,13 @@ class Rasterizer:
     def enable_counters(self, on: bool = True) -> None:
         self._check(self.lib.gudni_enable_counters(self.ctx, 1 if on else 0))
 
+    def set_random_source(self, source: int, seed: int = 0) -> None:
+        """Where the stochastic jitter comes from when the spec's stochastic_factor
+        is not 0 (gudni_set_random_source): lib.RANDOM_FIELD (the reference's random
+        field) or lib.RANDOM_COUNTER (a counter-based hash of seed, pixel and
+        section)."""
+        self._check(self.lib.gudni_set_random_source(self.ctx, int(source), int(seed)))
+
     def set_dense_columns(self, min_thresholds: int) -> None:
         """Scan columns whose queues hold at least `min_thresholds` thresholds with the
         whole warp (gudni_set_dense_columns); 0 keeps every column on its own lane.

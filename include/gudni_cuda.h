@@ -315,6 +315,19 @@ int gudni_batch_download(gudni_ctx* ctx, uint32_t* out);
 int gudni_enable_counters(gudni_ctx* ctx, int enable);
 int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
 
+/* Source of the stochastic area jitter (read only when the spec's stochastic_factor
+ * is not 0).  GUDNI_RANDOM_FIELD (default) is the reference's: the uploaded random
+ * field, walked one step per section from a start the column's position picks
+ * (initRandomField / getRandom, Kernels.cl:1597-1613).  GUDNI_RANDOM_COUNTER takes
+ * the jitter of pixel (x, y) for the section with ordinal k in its column's scan from
+ * a counter-based hash of (seed, x, y, k) instead: no table, no period of 4096
+ * sections, no sharing of values between neighbouring columns; a new seed per frame
+ * gives independent jitter per frame.  No reference
+ * counterpart.  Takes effect from the next launch. */
+#define GUDNI_RANDOM_FIELD   0
+#define GUDNI_RANDOM_COUNTER 1
+int gudni_set_random_source(gudni_ctx* ctx, int source, uint64_t seed);
+
 /* Warp-cooperative dense columns for the next launches of this context: a column
  * whose sorted queue holds at least `min_thresholds` thresholds is scanned by all 32
  * lanes of its warp together (sections dealt to the lanes, pixel sums taken in section

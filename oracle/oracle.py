@@ -59,6 +59,8 @@ def _load():
         lib.oracle_adjoint_job.restype = C.c_int
         lib.oracle_adjoint_job.argtypes = [vp, sz, vp, sz, vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int,
                                            C.c_int, vp, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int]
+        lib.oracle_set_random_source.restype = None
+        lib.oracle_set_random_source.argtypes = [C.c_int, C.c_uint64]
         _lib = lib
     return _lib
 
@@ -68,10 +70,12 @@ def _p(a):
 
 
 def render_frame(frame, n_threads: int = 0, max_thresholds: Optional[int] = None,
-                 stats: Optional[dict] = None) -> np.ndarray:
+                 stats: Optional[dict] = None, random_source: int = 0, random_seed: int = 0) -> np.ndarray:
     """Rasterize a serialized frame on the CPU; returns (H, W) uint32 BGRA words.
-    Pixels no job writes stay 0."""
+    Pixels no job writes stay 0.  random_source 1 takes the stochastic jitter from the
+    counter-based hash with `random_seed` instead of the random field."""
     lib = _load()
+    lib.oracle_set_random_source(int(random_source), int(random_seed))
     spec = frame.spec
     out = np.zeros((frame.canvas_h, frame.canvas_w), dtype=np.uint32)
     maxt = max_thresholds or spec.max_thresholds

@@ -412,7 +412,26 @@ struct Common {
   const gudni_shape* shapes;
   f4 background;
   float stochastic;
+  int random_mode;       // 0: the random field (K:1597-1613); 1: counter-based (below)
+  uint64_t random_seed;
 };
+
+// Counter-based jitter (no counterpart in the reference, which only has the random
+// field): the section with ordinal k in its column's scan, in pixel (x, y), takes the
+// top 24 bits of SplitMix64's output function (Steele, Lea and Flood, OOPSLA 2014)
+// applied twice, to seed ^ (x << 32 | y) and then to that plus k, as a float in
+// [0, 1).
+inline uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+inline float counterJitter(uint64_t seed, int x, int y, uint32_t k) {
+  const uint64_t key = seed ^ (((uint64_t)(uint32_t)x << 32) | (uint64_t)(uint32_t)y);
+  const uint64_t h = mix64(mix64(key) + (uint64_t)k);
+  return (float)(uint32_t)(h >> 40) / 16777216.0f;
+}
 
 inline f4 composite(f4 fg, f4 bg) {  // K:878-887
   float alphaOut = fg.w + bg.w * (1.0f - fg.w);
@@ -653,7 +672,7 @@ void runColumn(const Common& c, const gudni_tile_info* tiles, int tileIndex, int
     int startIx = ts.threadUnique & (GUDNI_RANDOM_FIELD_SIZE - 1);  // initRandomField K:1597-1606
     uint32_t bits = 0;
     if (c.random) std::memcpy(&bits, &c.random[startIx], 4);
-    p.cursor = (int)(bits & (GUDNI_RANDOM_FIELD_SIZE - 1));
+    p.cursor = c.random_mode == 1 ? 0 : (int)(bits & (GUDNI_RANDOM_FIELD_SIZE - 1));
   }
   int px = ts.deltaX, py = ts.deltaY;
   int yInt = -1;
@@ -664,8 +683,14 @@ void runColumn(const Common& c, const gudni_tile_info* tiles, int tileIndex, int
       verticalAdvance(q, ts, p, s);
       horizontalAdvance(q, p);
       f4 color = determineColor(c, s, maxShape, px, py);
-      p.cursor = (p.cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);  // getRandom K:1608-1613
-      float random = c.random ? c.random[p.cursor] : 0.0f;
+      float random;
+      if (c.random_mode == 1) {
+        random = counterJitter(c.random_seed, px, py, (uint32_t)p.cursor);
+        p.cursor += 1;
+      } else {
+        p.cursor = (p.cursor + 1) & (GUDNI_RANDOM_FIELD_SIZE - 1);  // getRandom K:1608-1613
+        random = c.random ? c.random[p.cursor] : 0.0f;
+      }
       float area = (p.sEnd.x - p.sStart.x) * (p.sEnd.y - p.sStart.y);
       float adj = area + (area * random * c.stochastic);
       p.acc[0] += color.x * adj;
@@ -706,6 +731,16 @@ typedef struct oracle_stats {
   int64_t overflow;       // 1 if a column overflowed max_thresholds
 } oracle_stats;
 
+static int g_random_mode = 0;
+static uint64_t g_random_seed = 0;
+
+// Source of the stochastic jitter for the following oracle_raster_job calls: 0 = the
+// random field, 1 = the counter-based jitter with `seed`.
+void oracle_set_random_source(int mode, uint64_t seed) {
+  g_random_mode = mode;
+  g_random_seed = seed;
+}
+
 // Rasterize one job on the CPU.  Arguments mirror gudni_raster_job plus the common
 // buffers and the spec knobs; `out` is bitmap_w*bitmap_h BGRA words.
 int oracle_raster_job(const uint8_t* geometry, const float* substances, const uint8_t* pictures,
@@ -727,6 +762,8 @@ int oracle_raster_job(const uint8_t* geometry, const float* substances, const ui
   c.shapes = shapes;
   c.background = f4{background[0], background[1], background[2], background[3]};
   c.stochastic = stochastic_factor;
+  c.random_mode = g_random_mode;
+  c.random_seed = g_random_seed;
   const long long total = (long long)n_tiles * threads_per_tile;
   Stats agg;
 #ifdef _OPENMP

@@ -37,6 +37,8 @@ def load():
                                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.host_warp_trace.restype = None
     lib.host_warp_trace.argtypes = [C.POINTER(C.c_longlong)]
+    lib.host_set_random_source.restype = None
+    lib.host_set_random_source.argtypes = [C.c_int, C.c_uint64]
     lib.host_strand_table.restype = sz
     lib.host_strand_table.argtypes = [vp, sz, C.c_uint, vp, vp, vp, sz]
     return lib

@@ -87,6 +87,10 @@ static inline unsigned atomicXor(unsigned* p, unsigned v) {
 
 namespace {
 
+// jitter source of the following host_column_* calls (host_set_random_source)
+uint32_t g_random_mode = gudni::kRandomField;
+uint64_t g_random_seed = 0;
+
 template <int SECTIONS>
 int run_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_tiles, int tpt, int cap,
             int* overflow) {
@@ -96,8 +100,12 @@ int run_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_t
   int status = 0;
   for (int t = 0; t < n_tiles; ++t) {
     for (int column = 0; column < tpt; ++column) {
-      if (gudni::runColumn<SECTIONS>(in, tiles[t], column, thr.data(), hdr.data(), cap, idx.data(), status))
-        *overflow = 1;
+      const bool over = in.random_mode == gudni::kRandomCounter && in.stochastic != 0.0f
+                            ? gudni::runColumn<SECTIONS, true>(in, tiles[t], column, thr.data(), hdr.data(), cap,
+                                                               idx.data(), status)
+                            : gudni::runColumn<SECTIONS>(in, tiles[t], column, thr.data(), hdr.data(), cap,
+                                                         idx.data(), status);
+      if (over) *overflow = 1;
     }
   }
   return status;
@@ -191,6 +199,8 @@ static gudni::RasterInputs host_inputs(HostTables& t, const uint8_t* geometry, s
   in.n_strands = (uint32_t)t.table.size();
   in.strand_first = t.first.data();
   in.n_units = (uint32_t)t.first.size();
+  in.random_mode = g_random_mode;
+  in.random_seed = g_random_seed;
   return in;
 }
 
@@ -328,6 +338,8 @@ extern "C" int host_column_raster_job(const uint8_t* geometry, size_t geometry_b
   in.n_strands = (uint32_t)table.size();
   in.strand_first = first.data();
   in.n_units = (uint32_t)first.size();
+  in.random_mode = g_random_mode;
+  in.random_seed = g_random_seed;
   *overflow = 0;
   const int tpt = 1 << compute_depth;
   int sections = 1;  // stack words for max_shape, a power of two (as the CUDA launch picks them)
@@ -398,4 +410,9 @@ extern "C" void host_warp_trace(long long out[gudni::kTraceEvents]) {
     out[i] = g_warp_trace[i];
     g_warp_trace[i] = 0;
   }
+}
+
+extern "C" void host_set_random_source(int mode, uint64_t seed) {
+  g_random_mode = mode == 1 ? gudni::kRandomCounter : gudni::kRandomField;
+  g_random_seed = seed;
 }

@@ -90,6 +90,28 @@ def test_stochastic_jitter(factor):
     assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
 
 
+@pytest.mark.parametrize("seed,tile,tpt,max_shape", [(12345, 32, 32, 127), (2 ** 63 + 7, 16, 64, 511)])
+def test_counter_jitter(seed, tile, tpt, max_shape):
+    """The counter-based jitter source (GUDNI_RANDOM_COUNTER, the scan instantiated
+    with kCounterJitter) matches the oracle bit for bit, one-word and multi-word
+    stacks; the image differs from the random field's and from another seed's."""
+    from host_column.build import load
+    lib = load()
+    spec = L.make_spec(tile, tpt, 4096, max_shape, 8, stochastic_factor=0.37)
+    frame = S.serialize_flat(G.glyph_page(seed=8, width=200, height=150, n_glyphs=50, n_shapes=12), spec)
+    field = O.render_frame(frame)
+    want = O.render_frame(frame, random_source=1, random_seed=seed)
+    other = O.render_frame(frame, random_source=1, random_seed=seed + 1)
+    assert not np.array_equal(want, field) and not np.array_equal(want, other)
+    lib.host_set_random_source(1, seed)
+    try:
+        got = host_render(frame)
+    finally:
+        lib.host_set_random_source(0, 0)
+    assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+    assert np.array_equal(host_render(frame), field)  # the field source again
+
+
 def test_non_finite_points():
     flat = G.random_shapes(seed=77, width=96, height=80, n_shapes=10)
     flat.pairs = flat.pairs.copy()

@@ -231,3 +231,20 @@ def test_resident_pictures_across_frames():
         r.upload_frame(frame)
         r.upload_pictures(lib)  # the frame's usages still fit: it stays uploaded
         assert np.array_equal(r.raster_frame(frame, upload_common=False), images[1])
+
+
+@pytest.mark.parametrize("source", [0, 1])
+def test_stochastic_jitter_sources(source):
+    """A non-zero STOCHASTIC_FACTOR with the reference's random field (source 0) and
+    with the counter-based jitter (source 1, gudni_set_random_source): the image
+    matches the oracle's bit for bit and differs from the unjittered one."""
+    flat = G.glyph_page(seed=8, width=200, height=150, n_glyphs=50, n_shapes=12)
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 127, 8, stochastic_factor=0.37))
+    plain = O.render_frame(S.serialize_flat(flat, L.make_spec(32, 32, 4096, 127, 8)))
+    seed = 987654321
+    with Rasterizer(frame.spec) as r:
+        r.set_random_source(source, seed)
+        got = r.queue_jobs(frame)
+    want = O.render_frame(frame, random_source=source, random_seed=seed)
+    assert not np.array_equal(want, plain)
+    assert np.array_equal(got, want), f"{int((got != want).sum())} pixels differ"
