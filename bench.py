@@ -22,7 +22,9 @@ gradient substance, so its arm renders the page with every gradient baked into a
 RGBA8 picture (scene.bake_radials, the reference's PictureFunction route); the line
 reports that image's parity with the oracle's rendering of the page itself.
 
-Other workloads (--workload): page1080 (a quarter page, the profiled size),
+Other workloads (--workload): scene4k (the page from its flattened scene to pixels:
+the serializer's passes on the device, gudni_serialize_device, then the raster
+launch, against the host serializer), page1080 (a quarter page, the profiled size),
 random512 (512x512, 64 random shapes), batch256 (the batched form: 256 scenes in one
 persistent launch, CUDA graph, autotuned tile shapes, against one launch pair per
 scene), adjoint1024 (forward vs fwd+adjoint on 1024x1024 with 500 shapes, gradients
@@ -95,6 +97,9 @@ WORKLOADS = {
                     "Mpixels/s (fwd+adjoint, 1024x1024 500 shapes, grads vs FP64 reference)"),
     # batched fitting (run_fit): 64 scenes of 256x256, 128 shapes each, Adam on points and colours
     "fit64": ("fit_64x256x256_shapes128", "steps/s (batched fwd+adjoint fitting, 64 scenes 256x256)"),
+    # scene to pixels on the device (run_scene): the page serialized by kernels, then rendered
+    "scene4k": ("scene_page_3840x2160_glyphs5000_shapes2000",
+                "Mpixels/s (scene to pixels: device serializer + raster, 3840x2160 page, <=1 LSB RGBA8)"),
 }
 
 
@@ -274,7 +279,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    if args.workload not in ("page4k", "page1080", "random512"):  # batch256, adjoint1024, fit64
+    if args.workload not in ("page4k", "page1080", "random512"):  # batch256, adjoint1024, fit64, scene4k
         print(json.dumps({"impl": "reference", "unavailable": f"workload {args.workload} has no reference "
                           "counterpart (the reference renders one scene per call and has no adjoint)"}))
         return 0
@@ -534,6 +539,93 @@ def run_adjoint(args):
     return 0
 
 
+def run_scene(args):
+    """Scene to pixels on the device: the page's flattened scene (host arrays, what a
+    host hands over) serialized by kernels (gudni_serialize_device) and rendered from
+    the frame left on the device; the host serializer (gudni_serialize, one host core)
+    is timed beside it.  A step is one serialization plus one render.  The piles are
+    checked byte for byte against the host serializer's and the image against the
+    render of the host-serialized frame."""
+    import torch
+    from gudni_gb300 import lib as L
+    from gudni_gb300 import scene as S
+    from gudni_gb300 import scenes as G
+    from gudni_gb300.raster import Rasterizer
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    tile, tpt = tile_override(args, *PLAIN_TILES["page4k"])
+    spec = L.make_spec(max_tile_size=tile, threads_per_tile=tpt, max_thresholds=4096, max_shape=127,
+                       stack_sections=8)
+    flat = G.glyph_page(seed=1)
+    host_ms = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        host = S.serialize_flat(flat, spec)
+        host_ms.append(1000 * (time.perf_counter() - t0))
+    shapes, tiles, jobs = S.concatenated_piles(host)
+    w, h = flat.canvas_w, flat.canvas_h
+    r = Rasterizer(spec)
+    r.upload_pictures(flat.pictures)
+    r.upload_random_field(host.random_field)
+    out = torch.zeros(w * h, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize()
+
+    def render(df):
+        r.raster_device_frame(df, w, h, flat.background, out.data_ptr(), stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        render(r.serialize_device(flat))
+        stream.synchronize()
+    r.sync_status()
+    ser_ms, ren_ms, tot_ms = [], [], []
+    launches0 = r.launch_count()
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            df = r.serialize_device(flat)  # returns once the piles are on the device
+            t1 = time.perf_counter()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            render(df)
+            b.record(stream)
+            b.synchronize()
+            t2 = time.perf_counter()
+            ser_ms.append(1000 * (t1 - t0))
+            ren_ms.append(a.elapsed_time(b))
+            tot_ms.append(1000 * (t2 - t0))
+    launches = r.launch_count() - launches0
+    r.sync_status()
+    got = r.download_device_frame(df)
+    piles = {"geometry": got["geometry"].tobytes() == host.geometry.tobytes(),
+             "shapes": got["shapes"].tobytes() == shapes.tobytes(),
+             "tiles": got["tiles"].tobytes() == tiles.tobytes(),
+             "tile_jobs": bool(np.array_equal(got["tile_jobs"], jobs))}
+    img = out.cpu().numpy().view(np.uint32).reshape(h, w)
+    ref = r.raster_frame(host)  # the host-serialized frame through the plain path
+    r.close()
+    ms = statistics.median(tot_ms)
+    line = {"metric": WORKLOADS["scene4k"][1], "value": w * h / (ms / 1000) / 1e6, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["scene4k"][0], "canvas": [w, h], "tile": tile,
+                       "threads_per_tile": tpt, "shapes": int(host.stats["shapes"]),
+                       "tiles": int(host.stats["tiles"]), "l2": "flushed between steps (256 MB write)",
+                       "inputs": "flattened scene arrays in host memory, uploaded inside each step"},
+            "device_serialize_ms": statistics.median(ser_ms), "render_ms": statistics.median(ren_ms),
+            "host_serialize_ms": statistics.median(host_ms),
+            "host_serializer_scene_to_pixels_ms": statistics.median(host_ms) + statistics.median(ren_ms),
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "parity": {"piles_identical_to_host_serializer": piles, "image_vs_host_frame": lsb_parity(img, ref)}}
+    print(json.dumps(line))
+    return 0
+
+
 FIT_SPEC = dict(max_tile_size=32, threads_per_tile=256, max_thresholds=4096, max_shape=255,
                 max_strands_per_tile=1 << 24)
 
@@ -615,6 +707,8 @@ def main():
         return run_adjoint(args)
     if args.workload == "fit64":
         return run_fit(args)
+    if args.workload == "scene4k":
+        return run_scene(args)
 
     import torch
 
