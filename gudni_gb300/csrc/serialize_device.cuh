@@ -602,48 +602,160 @@ struct KeptPass {
   }
 };
 
-// per base tile: its place in the tree and the kept shapes that reach it (count pass
-// with list == nullptr, then the fill pass)
-struct BaseTilePass {
+// The base tiles a box reaches along one axis of the grid (n tiles of `side` pixels):
+// tile i is reached when (i == n - 1 || lo_edge < (i + 1) * side) and
+// (i == 0 || hi_edge > i * side) -- reachesRect's tests, each monotone in i -- so the
+// reached tiles are [lo, hi] (none when lo > hi).  Binary searches with the same
+// float comparisons.
+GUDNI_SHD inline void reachRange(float lo_edge, float hi_edge, int n, int side, int& lo, int& hi) {
+  int a = 0, b = n - 1;  // last i with (i == 0 || hi_edge > i * side)
+  while (a < b) {
+    const int m = a + (b - a + 1) / 2;
+    if (hi_edge > (float)(m * side)) a = m; else b = m - 1;
+  }
+  hi = a;
+  a = 0;
+  b = n - 1;  // first i with (i == n - 1 || lo_edge < (i + 1) * side)
+  while (a < b) {
+    const int m = a + (b - a) / 2;
+    if (lo_edge < (float)((m + 1) * side)) b = m; else a = m + 1;
+  }
+  lo = a;
+}
+
+// The traversal number of the base tile in column `col`, row `row` (baseTileOf's
+// inverse).
+GUDNI_SHD inline uint32_t baseTileNumber(int col, int row, int levels) {
+  uint32_t r = 0;
+  for (int k = 0; k < levels; ++k)
+    r |= ((((uint32_t)col >> k) & 1u) << (2 * k)) | ((((uint32_t)row >> k) & 1u) << (2 * k + 1));
+  return r;
+}
+
+// per kept shape: the rectangle of base tiles its box reaches and their number
+struct ReachPass {
   const KeptShape* kept;
-  uint64_t n_kept;
-  int levels, tile_side, side, depth;
+  int n, side;  // tiles per axis, tile side in pixels
+  int4* rect;   // column range (x, y), row range (z, w)
+  uint64_t* count;
+  GUDNI_SHD void operator()(uint64_t k) const {
+    const Box& b = kept[k].box;
+    int c0, c1, r0, r1;
+    reachRange(b.left, b.right, n, side, c0, c1);
+    reachRange(b.top, b.bottom, n, side, r0, r1);
+    rect[k] = make_int4(c0, c1, r0, r1);
+    count[k] = (c0 <= c1 && r0 <= r1) ? (uint64_t)(c1 - c0 + 1) * (uint64_t)(r1 - r0 + 1) : 0;
+  }
+};
+
+// per kept shape: a (base tile, shape) pair for every tile it reaches
+struct PairPass {
+  const int4* rect;
+  const uint64_t* at;  // exclusive scan of the counts
+  int levels;
+  uint32_t* key;
+  uint32_t* val;
+  GUDNI_SHD void operator()(uint64_t k) const {
+    const int4 q = rect[k];
+    uint64_t j = at[k];
+    for (int row = q.z; row <= q.w; ++row)
+      for (int col = q.x; col <= q.y; ++col) {
+        key[j] = baseTileNumber(col, row, levels);
+        val[j] = (uint32_t)k;
+        ++j;
+      }
+  }
+};
+
+// Stable LSD radix sort of the pairs by tile, kRadixBits per pass, in blocks of
+// kRadixBlock pairs: each block counts its digits, a scan over (digit, block) gives
+// every block its place per digit, and each block scatters its pairs in order.  The
+// shapes of a tile thus keep their insertion order.
+constexpr int kRadixBits = 8;
+constexpr int kRadixDigits = 1 << kRadixBits;
+constexpr uint64_t kRadixBlock = 1024;
+
+struct RadixCountPass {
+  const uint32_t* key;
+  uint64_t n, blocks;
+  int shift;
+  uint64_t* hist;  // [digit * blocks + block]
+  GUDNI_SHD void operator()(uint64_t blk) const {
+    uint32_t c[kRadixDigits];
+    for (int d = 0; d < kRadixDigits; ++d) c[d] = 0;
+    const uint64_t end = (blk + 1) * kRadixBlock < n ? (blk + 1) * kRadixBlock : n;
+    for (uint64_t i = blk * kRadixBlock; i < end; ++i) ++c[(key[i] >> shift) & (kRadixDigits - 1)];
+    for (int d = 0; d < kRadixDigits; ++d) hist[(uint64_t)d * blocks + blk] = c[d];
+  }
+};
+
+struct RadixScatterPass {
+  const uint32_t* key;
+  const uint32_t* val;
+  uint64_t n, blocks;
+  int shift;
+  const uint64_t* at;  // exclusive scan of hist
+  uint32_t* key_out;
+  uint32_t* val_out;
+  GUDNI_SHD void operator()(uint64_t blk) const {
+    uint64_t next[kRadixDigits];
+    for (int d = 0; d < kRadixDigits; ++d) next[d] = at[(uint64_t)d * blocks + blk];
+    const uint64_t end = (blk + 1) * kRadixBlock < n ? (blk + 1) * kRadixBlock : n;
+    for (uint64_t i = blk * kRadixBlock; i < end; ++i) {
+      const uint64_t o = next[(key[i] >> shift) & (kRadixDigits - 1)]++;
+      key_out[o] = key[i];
+      val_out[o] = val[i];
+    }
+  }
+};
+
+struct Fill64Pass {
+  uint64_t* out;
+  uint64_t value;
+  GUDNI_SHD void operator()(uint64_t i) const { out[i] = value; }
+};
+
+// per sorted pair: where its tile's run starts and ends
+struct RunPass {
+  const uint32_t* key;
+  uint64_t n;
+  uint64_t* first;
+  uint64_t* end;
+  GUDNI_SHD void operator()(uint64_t i) const {
+    const uint32_t t = key[i];
+    if (i == 0 || key[i - 1] != t) first[t] = i;
+    if (i + 1 == n || key[i + 1] != t) end[t] = i + 1;
+  }
+};
+
+// per base tile: its place in the tree and its list -- its run of the sorted pairs
+struct BaseNodePass {
+  const KeptShape* kept;
+  const uint32_t* list;  // the sorted pairs' shapes (the start of the list pool)
+  const uint64_t* first;
+  const uint64_t* end;
+  int levels, tile_side, depth;
   Node* nodes;
-  const uint64_t* list_at;  // fill pass: exclusive scan of the counts
-  uint32_t* list;
   GUDNI_SHD void operator()(uint64_t r) const {
     int col, row;
     baseTileOf(r, levels, col, row);
-    const int l = col * tile_side, t = row * tile_side, rr = l + tile_side, b = t + tile_side;
-    uint64_t count = 0, strands = 0;
-    for (uint64_t k = 0; k < n_kept; ++k) {
-      if (!reachesRect(kept[k].box, l, t, rr, b, side)) continue;
-      if (list) list[list_at[r] + count] = (uint32_t)k;
-      ++count;
-      strands += kept[k].num_strands;
-    }
-    if (list) return;
     Node n;
-    n.left = l;
-    n.top = t;
-    n.right = rr;
-    n.bottom = b;
+    n.left = col * tile_side;
+    n.top = row * tile_side;
+    n.right = n.left + tile_side;
+    n.bottom = n.top + tile_side;
     n.hdepth = (int16_t)depth;
     n.vdepth = (int16_t)depth;
     n.kind = 0;
     n.open = 1;
     n.pad[0] = n.pad[1] = 0;
-    n.list = 0;
-    n.count = count;
+    n.list = first[r];
+    n.count = end[r] - first[r];
+    uint64_t strands = 0;
+    for (uint64_t i = first[r]; i < end[r]; ++i) strands += kept[list[i]].num_strands;
     n.strands = strands;
     nodes[r] = n;
   }
-};
-
-struct BaseListAtPass {
-  Node* nodes;
-  const uint64_t* list_at;
-  GUDNI_SHD void operator()(uint64_t r) const { nodes[r].list = list_at[r]; }
 };
 
 // per node of a level: whether it splits, and its children's list sizes
@@ -938,6 +1050,7 @@ enum Slot {
   kShapeSub, kBox, kKeep, kKeptAt, kOutlineShape, kOutlineBytes, kByteAt, kOutlineStrands, kStrandAt,
   kKept, kNodesA, kNodesB, kPoolA, kPoolB, kOutNodes, kNodeAt, kOutList, kListAt, kChildSize,
   kChildStrands, kLeafCounts, kShapeAt, kReorder, kPointSources, kPointWeights, kPointOffsets,
+  kRect, kPairCount, kPairAt, kKeysA, kKeysB, kHist, kHistAt, kTileFirst, kTileEnd,
   kSlots
 };
 
@@ -1035,24 +1148,52 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
   const int levels = canvas_depth - depth;
   if (levels > 15) return -2;
   uint64_t n_nodes = 1ull << (2 * levels);
-  Node* nodes = ex.template alloc<Node>(kNodesA, n_nodes);
-  uint64_t* counts = ex.template alloc<uint64_t>(kOutNodes, n_nodes + 1);
-  uint64_t* list_at = ex.template alloc<uint64_t>(kListAt, n_nodes + 1);
-  if (!nodes || !counts || !list_at) return -1;
-  BaseTilePass base{kept, n_kept, levels, 1 << depth, 1 << canvas_depth, depth, nodes, nullptr, nullptr};
-  GUDNI_SER_TRY(ex.forEach(n_nodes, base));
-  GUDNI_SER_TRY(ex.forEach(n_nodes, NodeCount{nodes, counts}));
-  GUDNI_SER_TRY(ex.scan(counts, list_at, n_nodes));
-  uint64_t pool_used = 0;
-  GUDNI_SER_TRY(ex.read(&pool_used, list_at + n_nodes, 8));
-  uint64_t pool_cap = pool_used + pool_used / 2 + 1024;
+  const int tile_side = 1 << depth;
+  const int grid_n = 1 << levels;
+  // the (base tile, shape) pairs, sorted by tile with each tile's shapes in order
+  int4* rect = ex.template alloc<int4>(kRect, n_kept);
+  uint64_t* pair_count = ex.template alloc<uint64_t>(kPairCount, n_kept + 1);
+  uint64_t* pair_at = ex.template alloc<uint64_t>(kPairAt, n_kept + 1);
+  if (!rect || !pair_count || !pair_at) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_kept, ReachPass{kept, grid_n, tile_side, rect, pair_count}));
+  GUDNI_SER_TRY(ex.scan(pair_count, pair_at, n_kept));
+  uint64_t n_pairs = 0;
+  GUDNI_SER_TRY(ex.read(&n_pairs, pair_at + n_kept, 8));
+  if (n_pairs > 0xFFFFFFFFull) return -2;
+  uint64_t pool_cap = n_pairs + n_pairs / 2 + 1024;
   int pool_slot = kPoolA;
-  uint32_t* pool = ex.template alloc<uint32_t>(Slot(pool_slot), pool_cap);
-  if (!pool) return -1;
-  base.list = pool;
-  base.list_at = list_at;
-  GUDNI_SER_TRY(ex.forEach(n_nodes, base));
-  GUDNI_SER_TRY(ex.forEach(n_nodes, BaseListAtPass{nodes, list_at}));
+  uint32_t* keys = ex.template alloc<uint32_t>(kKeysA, n_pairs);
+  uint32_t* pool = ex.template alloc<uint32_t>(kPoolA, pool_cap);
+  if (!keys || !pool) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_kept, PairPass{rect, pair_at, levels, keys, pool}));
+  const uint64_t blocks = (n_pairs + kRadixBlock - 1) / kRadixBlock;
+  int key_slot = kKeysA;
+  for (int shift = 0; shift < 2 * levels && n_pairs > 0; shift += kRadixBits) {
+    uint64_t* hist = ex.template alloc<uint64_t>(kHist, (uint64_t)kRadixDigits * blocks + 1);
+    uint64_t* hist_at = ex.template alloc<uint64_t>(kHistAt, (uint64_t)kRadixDigits * blocks + 1);
+    const int other_keys = key_slot == kKeysA ? kKeysB : kKeysA;
+    const int other_pool = pool_slot == kPoolA ? kPoolB : kPoolA;
+    uint32_t* keys_out = ex.template alloc<uint32_t>(Slot(other_keys), n_pairs);
+    uint32_t* pool_out = ex.template alloc<uint32_t>(Slot(other_pool), pool_cap);
+    if (!hist || !hist_at || !keys_out || !pool_out) return -1;
+    GUDNI_SER_TRY(ex.forEach(blocks, RadixCountPass{keys, n_pairs, blocks, shift, hist}));
+    GUDNI_SER_TRY(ex.scan(hist, hist_at, (uint64_t)kRadixDigits * blocks));
+    GUDNI_SER_TRY(ex.forEach(blocks, RadixScatterPass{keys, pool, n_pairs, blocks, shift, hist_at, keys_out, pool_out}));
+    keys = keys_out;
+    pool = pool_out;
+    key_slot = other_keys;
+    pool_slot = other_pool;
+  }
+  // the base tiles: their runs of the sorted pairs are their lists
+  Node* nodes = ex.template alloc<Node>(kNodesA, n_nodes);
+  uint64_t* first = ex.template alloc<uint64_t>(kTileFirst, n_nodes);
+  uint64_t* end = ex.template alloc<uint64_t>(kTileEnd, n_nodes);
+  if (!nodes || !first || !end) return -1;
+  GUDNI_SER_TRY(ex.forEach(n_nodes, Fill64Pass{first, 0}));
+  GUDNI_SER_TRY(ex.forEach(n_nodes, Fill64Pass{end, 0}));
+  GUDNI_SER_TRY(ex.forEach(n_pairs, RunPass{keys, n_pairs, first, end}));
+  GUDNI_SER_TRY(ex.forEach(n_nodes, BaseNodePass{kept, pool, first, end, levels, tile_side, depth, nodes}));
+  uint64_t pool_used = n_pairs;
 
   // splits, one level per pass, until no tile splits
   int node_slot = kNodesA;

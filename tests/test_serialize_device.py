@@ -189,3 +189,15 @@ def test_page_4k():
     spec = L.make_spec(32, 32, 4096, 127, 8)
     spec.max_strands_per_tile = 4094
     check(flat, spec)
+
+
+def test_wide_canvas_three_radix_passes():
+    """A 16384-wide canvas at 32-pixel tiles: 512 x 512 base tiles (18-bit tile
+    numbers, three radix passes) and many small local shapes."""
+    rng = np.random.default_rng(31)
+    specs = G.local_shape_specs(rng, 16384, 900, 3000, 4, 12)
+    for sp in specs:
+        sp.color = (float(rng.random()), float(rng.random()), float(rng.random()), 1.0)
+    flat = G.flat_from_specs(specs, 16384, 900, (1, 1, 1, 1))
+    frame = check(flat, L.make_spec(32, 32, 4096, 127, 8))
+    assert frame.stats["tiles"] >= 512 * 512
