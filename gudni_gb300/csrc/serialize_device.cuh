@@ -889,25 +889,19 @@ struct LeafEmitPass {
   }
 };
 
-struct NodeCount {
+// per leaf: the largest shape count and strand count over the leaves (out[0], out[1],
+// zero beforehand); the maximum does not depend on the order
+struct LeafMaxPass {
   const Node* nodes;
-  uint64_t* out;
-  GUDNI_SHD void operator()(uint64_t i) const { out[i] = nodes[i].count; }
-};
-struct NodeStrands {
-  const Node* nodes;
-  uint64_t* out;
-  GUDNI_SHD void operator()(uint64_t i) const { out[i] = nodes[i].strands; }
-};
-// one item: the largest of n values into out[n] (a short sequential pass over the leaves)
-struct MaxPass {
-  const uint64_t* in;
-  uint64_t n;
-  uint64_t* out;
-  GUDNI_SHD void operator()(uint64_t) const {
-    uint64_t m = 0;
-    for (uint64_t i = 0; i < n; ++i) m = in[i] > m ? in[i] : m;
-    out[n] = m;
+  unsigned long long* out;
+  GUDNI_SHD void operator()(uint64_t i) const {
+#if defined(__CUDA_ARCH__)
+    atomicMax(&out[0], (unsigned long long)nodes[i].count);
+    atomicMax(&out[1], (unsigned long long)nodes[i].strands);
+#else
+    out[0] = nodes[i].count > out[0] ? nodes[i].count : out[0];
+    out[1] = nodes[i].strands > out[1] ? nodes[i].strands : out[1];
+#endif
   }
 };
 
@@ -1254,17 +1248,15 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
                                                  shape_at, tiles, tile_jobs, shapes}));
 
   // the largest leaf lists (gudni_frame_stats [5], [6])
-  uint64_t most_shapes = 0, most_strands = 0;
+  uint64_t most[2] = {0, 0};
   {
-    uint64_t* per = ex.template alloc<uint64_t>(kLeafCounts, n_nodes + 1);
-    if (!per) return -1;
-    GUDNI_SER_TRY(ex.forEach(n_nodes, NodeCount{nodes, per}));
-    GUDNI_SER_TRY(ex.forEach(1, MaxPass{per, n_nodes, per}));
-    GUDNI_SER_TRY(ex.read(&most_shapes, per + n_nodes, 8));
-    GUDNI_SER_TRY(ex.forEach(n_nodes, NodeStrands{nodes, per}));
-    GUDNI_SER_TRY(ex.forEach(1, MaxPass{per, n_nodes, per}));
-    GUDNI_SER_TRY(ex.read(&most_strands, per + n_nodes, 8));
+    uint64_t* m = ex.template alloc<uint64_t>(kLeafCounts, 2);
+    if (!m) return -1;
+    GUDNI_SER_TRY(ex.forEach(2, Fill64Pass{m, 0}));
+    GUDNI_SER_TRY(ex.forEach(n_nodes, LeafMaxPass{nodes, reinterpret_cast<unsigned long long*>(m)}));
+    GUDNI_SER_TRY(ex.read(most, m, 16));
   }
+  const uint64_t most_shapes = most[0], most_strands = most[1];
 #undef GUDNI_SER_TRY
 
   res.geometry_bytes = geo_bytes;
