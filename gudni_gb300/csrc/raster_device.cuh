@@ -85,8 +85,8 @@ struct RasterInputs {
   // kRandomCounter, a counter-based hash of (random_seed, pixel, the section's ordinal
   // in the column's scan), which needs no table and does not repeat every 4096
   // sections.
-  uint32_t random_mode = 0;
-  uint64_t random_seed = 0;
+  uint32_t random_mode;
+  uint64_t random_seed;
 };
 
 constexpr uint32_t kRandomField = 0;
