@@ -201,3 +201,76 @@ def test_wide_canvas_three_radix_passes():
     flat = G.flat_from_specs(specs, 16384, 900, (1, 1, 1, 1))
     frame = check(flat, L.make_spec(32, 32, 4096, 127, 8))
     assert frame.stats["tiles"] >= 512 * 512
+
+
+def _random_flat(draw, st):
+    """A flattened scene with uneven structure: substances without shapes, shapes
+    without outlines, outlines of 0-12 pairs, points inside, outside and on the edges of
+    the canvas, repeated points, and the odd NaN or infinity."""
+    import dataclasses  # noqa: F401
+    w = draw(st.integers(1, 300))
+    h = draw(st.integers(1, 300))
+    n_sub = draw(st.integers(0, 8))
+    seed = draw(st.integers(0, 2 ** 32 - 1))
+    rng = np.random.default_rng(seed)
+    kinds, colors, pics, pxf, sub_start, compounds, outline_start, pair_start, chunks = [], [], [], [], [0], [], [0], [0], []
+    n_pairs = 0
+    special = np.array([np.nan, np.inf, -np.inf, 0.0, -0.0, w, h, -1e6, 1e6], np.float32)
+    for _ in range(n_sub):
+        kind = int(rng.integers(0, 3))
+        kinds.append(kind)
+        colors.append(rng.random(4, dtype=np.float32))
+        pics.append(int(rng.integers(0, 2)))
+        pxf.append(rng.random(3, dtype=np.float32))
+        for _ in range(int(rng.integers(0, 4))):
+            compounds.append(int(rng.integers(0, 2)))
+            for _ in range(int(rng.integers(0, 4))):
+                n = int(rng.integers(0, 13))
+                pts = (rng.random((n, 4), dtype=np.float32) * np.float32(1.4) - np.float32(0.2))
+                pts *= np.array([w, h, w, h], np.float32)
+                if n and rng.random() < 0.3:
+                    pts[int(rng.integers(0, n))] = pts[0]  # a repeated point
+                if n and rng.random() < 0.1:
+                    pts.reshape(-1)[int(rng.integers(0, 4 * n))] = special[int(rng.integers(0, special.size))]
+                chunks.append(pts)
+                n_pairs += n
+                pair_start.append(n_pairs)
+            outline_start.append(len(pair_start) - 1)
+        sub_start.append(len(compounds))
+    pictures = [G.noise_texture(seed=1, size=5), G.noise_texture(seed=2, size=9)]
+    offsets, sizes, off = [], [], 0
+    for p in pictures:
+        offsets.append(off)
+        sizes.append((p.shape[1], p.shape[0]))
+        off += p.size
+    rad = np.zeros(n_sub, dtype=L.RADIAL_DTYPE)
+    return S.FlatScene(
+        canvas_w=w, canvas_h=h, background=np.ones(4, np.float32),
+        substance_kind=np.asarray(kinds, np.int32), substance_color=np.asarray(colors, np.float32).reshape(-1, 4),
+        substance_picture=np.asarray(pics, np.int32), substance_picture_xform=np.asarray(pxf, np.float32).reshape(-1, 3),
+        substance_radial=rad, substance_shape_start=np.asarray(sub_start, np.int32),
+        shape_compound=np.asarray(compounds, np.int32), shape_outline_start=np.asarray(outline_start, np.int32),
+        outline_pair_start=np.asarray(pair_start, np.int32),
+        pairs=np.concatenate(chunks) if chunks else np.zeros((0, 4), np.float32),
+        pictures=np.concatenate([p.reshape(-1) for p in pictures]),
+        picture_size=np.asarray(sizes, np.int32), picture_offset=np.asarray(offsets, np.int32))
+
+
+def test_random_scenes_and_specs():
+    """Generated scenes and specs (tile 8-64, MAXSHAPE 1-127, strand limits down to 1,
+    one to many tiles per job): the device passes give the host serializer's bytes."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(st.data())
+    def run(data):
+        flat = _random_flat(data.draw, st)
+        tile = data.draw(st.sampled_from([8, 16, 32, 64]))
+        spec = L.make_spec(tile, tile * data.draw(st.sampled_from([1, 2, 4])), 512, 127, 8)
+        spec.max_shape = data.draw(st.sampled_from([1, 2, 3, 7, 127]))
+        spec.max_strands_per_tile = data.draw(st.sampled_from([1, 5, 40, 4094]))
+        spec.max_tiles_per_call = data.draw(st.sampled_from([1, 3, 1024]))
+        check(flat, spec, seeds=(data.draw(st.integers(0, 1000)),))
+
+    run()
