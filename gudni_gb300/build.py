@@ -2,9 +2,10 @@
 
   gudni_gb300/_build/libgudni_host.so   host serializer (g++)
   gudni_gb300/_build/libgudni_cuda.so   sm_103a raster kernels + C ABI (nvcc)
+  gudni_gb300/_build/gudni_render       native host program over both (render_main.cpp)
 
-Both are plain shared libraries with C entry points (include/*.h) loaded through
-ctypes; nothing is installed into site-packages.  Compilation runs in parallel and
+The two libraries are plain shared libraries with C entry points (include/*.h),
+loaded through ctypes; nothing is installed into site-packages.  Compilation runs in parallel and
 only when a source is newer than its library.
 """
 from __future__ import annotations
@@ -81,11 +82,25 @@ def build_cuda(force: bool = False) -> str:
     return CUDA_LIB
 
 
+RENDER_SOURCES = [os.path.join(CSRC, "render_main.cpp")]
+RENDER = os.path.join(BUILD, "gudni_render")
+
+
+def build_render(force: bool = False) -> str:
+    """gudni_render, the native host program (links both libraries and the CUDA runtime)."""
+    if force or _stale(RENDER, RENDER_SOURCES + [HOST_LIB, CUDA_LIB]):
+        _run([nvcc(), "-O2", "-std=c++17", "-I", INCLUDE] + RENDER_SOURCES +
+             ["-o", RENDER, "-L", BUILD, "-lgudni_cuda", "-lgudni_host", "-Xlinker", "-rpath," + BUILD])
+    return RENDER
+
+
 def build_all(force: bool = False) -> dict:
     with ThreadPoolExecutor(max_workers=2) as ex:
         h = ex.submit(build_host, force)
         c = ex.submit(build_cuda, force)
-        return {"host": h.result(), "cuda": c.result()}
+        out = {"host": h.result(), "cuda": c.result()}
+    out["render"] = build_render(force)
+    return out
 
 
 if __name__ == "__main__":

@@ -551,6 +551,36 @@ def serialize(scene: Scene, canvas_w: int, canvas_h: int, spec: L.Spec,
     return serialize_flat(flat, spec, random_field)
 
 
+def write_scene_file(path: str, flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndarray] = None) -> None:
+    """Write a flattened scene with its spec, picture pile and random field as the
+    scene file gudni_render reads: a list of named arrays (u32 name length, name, u64
+    byte count, bytes), the arrays of gudni_scene_desc under their field names."""
+    arrays = {
+        "header": np.array([flat.canvas_w, flat.canvas_h, flat.substance_kind.size, flat.picture_offset.size],
+                           np.int32),
+        "spec": np.frombuffer(bytes(spec), np.uint8),
+        "background": np.asarray(flat.background, np.float32),
+        "substance_kind": flat.substance_kind.astype(np.int32),
+        "substance_color": flat.substance_color.astype(np.float32),
+        "substance_picture": flat.substance_picture.astype(np.int32),
+        "substance_picture_xform": flat.substance_picture_xform.astype(np.float32),
+        "substance_radial": flat.substance_radial,
+        "substance_shape_start": flat.substance_shape_start.astype(np.int32),
+        "shape_compound": flat.shape_compound.astype(np.int32),
+        "shape_outline_start": flat.shape_outline_start.astype(np.int32),
+        "outline_pair_start": flat.outline_pair_start.astype(np.int32),
+        "pairs": flat.pairs.astype(np.float32),
+        "picture_size": flat.picture_size.astype(np.int32),
+        "picture_offset": flat.picture_offset.astype(np.int32),
+        "pictures": flat.pictures.astype(np.uint8),
+        "random_field": np.asarray(default_random_field() if random_field is None else random_field, np.float32),
+    }
+    with open(path, "wb") as f:
+        for name, a in arrays.items():
+            b = np.ascontiguousarray(a).tobytes()
+            f.write(np.uint32(len(name)).tobytes() + name.encode() + np.uint64(len(b)).tobytes() + b)
+
+
 def scene_desc(flat: FlatScene):
     """The gudni_scene_desc of a flattened scene, and the arrays it points into (keep
     them alive while the descriptor is in use)."""
