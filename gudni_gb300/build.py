@@ -25,6 +25,7 @@ HOST_LIB = os.path.join(BUILD, "libgudni_host.so")
 CUDA_LIB = os.path.join(BUILD, "libgudni_cuda.so")
 
 HOST_SOURCES = [os.path.join(CSRC, "serialize.cpp")]
+HOST_DEPS = [os.path.join(CSRC, "serialize_device.cuh")]
 CUDA_SOURCES = [os.path.join(CSRC, f) for f in ("raster.cu", "raster_counter.cu", "adjoint.cu", "capi.cu",
                                                   "noalloc.cu")]
 HEADERS = [os.path.join(INCLUDE, h) for h in ("gudni_cuda.h", "gudni_serialize.h")] + [
@@ -36,7 +37,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-ffp-contract=off"]
-GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing"]
+GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp"]
 
 
 def _stale(target: str, sources: list[str]) -> bool:
@@ -53,6 +54,11 @@ def nvcc() -> str:
     return path
 
 
+def cuda_include() -> str:
+    """The CUDA headers (vector types for the serializer's shared pass code)."""
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+
+
 def _run(cmd: list[str]) -> None:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -61,8 +67,9 @@ def _run(cmd: list[str]) -> None:
 
 def build_host(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    if force or _stale(HOST_LIB, HOST_SOURCES):
-        _run(["g++"] + GXX_FLAGS + ["-shared", "-I", INCLUDE] + HOST_SOURCES + ["-o", HOST_LIB])
+    if force or _stale(HOST_LIB, HOST_SOURCES + HOST_DEPS):
+        _run(["g++"] + GXX_FLAGS + ["-shared", "-I", INCLUDE, "-I", CSRC, "-I", cuda_include()] + HOST_SOURCES +
+             ["-o", HOST_LIB])
     return HOST_LIB
 
 

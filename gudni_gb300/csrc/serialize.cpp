@@ -6,17 +6,46 @@
 
 #include "gudni_serialize.h"
 
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <utility>
 #include <string>
 #include <vector>
+
+#include "serialize_device.cuh"
 
 namespace {
 
 thread_local std::string g_error;
+
+// An allocator whose resize leaves new elements uninitialized (default-initialized):
+// the parallel serializer writes every byte of the piles it sizes, so the zero fill a
+// std::vector resize performs would be a second, serial pass over them.
+template <class T>
+struct NoFill : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoFill<U>;
+  };
+  NoFill() = default;
+  template <class U>
+  NoFill(const NoFill<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <class U, class... Args>
+  void construct(U* p, Args&&... args) {
+    ::new (static_cast<void*>(p)) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using Pile = std::vector<T, NoFill<T>>;
 
 struct P2 { float x, y; };
 struct Bez { P2 a, c, b; };  // start, control, end (Figure/Bezier.hs Bez)
@@ -187,15 +216,15 @@ inline bool connectable(const Bez& a, const Bez& b) {  // Strand.hs:77-81
 }
 
 struct ProvSink {
-  std::vector<int32_t> src;     // 3 per serialized point
-  std::vector<float> w;         // 3 per serialized point
-  std::vector<uint32_t> where;  // float index of the point's x in the geometry pile
+  Pile<int32_t> src;     // 3 per serialized point
+  Pile<float> w;         // 3 per serialized point
+  Pile<uint32_t> where;  // float index of the point's x in the geometry pile
 };
 
 // Append the serialized strands of one outline (curve pairs) to `geo`; returns the
 // number of strands.  splitShape / outlineToStrands, Strand.hs:153-178.  With `prov`,
 // also records the provenance of every point written (pair indices from `pair0`).
-uint32_t outline_to_strands(const float* pairs, int n_pairs, std::vector<uint8_t>& geo, ProvSink* prov = nullptr,
+uint32_t outline_to_strands(const float* pairs, int n_pairs, Pile<uint8_t>& geo, ProvSink* prov = nullptr,
                             int32_t pair0 = 0) {
   if (n_pairs < 2) return 0;
   // pairsToBeziers (overNeighbors makeBezier), then replaceKnobs
@@ -473,7 +502,7 @@ class TileTree {
 
 struct gudni_frame {
   ProvSink prov;
-  std::vector<uint8_t> geometry;
+  Pile<uint8_t> geometry;
   std::vector<float> substances;
   std::vector<gudni_picture_use> picture_uses;
   std::vector<gudni_radial> radials;
@@ -644,6 +673,135 @@ gudni_frame* gudni_serialize(const gudni_scene_desc* s, const gudni_spec* spec) 
   f->stats[4] = tree.splits();
   // finalState ^. bsCurrentJob : finalState ^. bsJobs -- the last job first
   f->jobs.assign(built.rbegin(), built.rend());
+  return f.release();
+}
+
+}  // extern "C"
+
+namespace {
+
+// The serializer's data-parallel passes (serialize_device.cuh) on host threads: every
+// pass an OpenMP loop over its items (each item writes its own outputs), scans
+// sequential.  Pile results land in the frame's own vectors.
+struct ThreadExec {
+  gudni_frame* f;
+  int threads;
+  std::vector<Pile<uint8_t>> slot = std::vector<Pile<uint8_t>>(gudni::ser::kSlots);
+
+  template <class V>
+  void* grow(V& v, uint64_t bytes) {
+    v.resize((size_t)((bytes + sizeof(typename V::value_type) - 1) / sizeof(typename V::value_type)) + 1);
+    return v.data();
+  }
+  template <class T>
+  T* alloc(gudni::ser::Slot s, uint64_t n) {
+    const uint64_t bytes = n * sizeof(T);
+    switch (s) {
+      case gudni::ser::kGeometry: return static_cast<T*>(grow(f->geometry, bytes));
+      case gudni::ser::kPointSources: return static_cast<T*>(grow(f->prov.src, bytes));
+      case gudni::ser::kPointWeights: return static_cast<T*>(grow(f->prov.w, bytes));
+      case gudni::ser::kPointOffsets: return static_cast<T*>(grow(f->prov.where, bytes));
+      default: {
+        Pile<uint8_t>& v = slot[s];
+        // 16-byte units keep every record type aligned
+        if (v.size() < bytes + 16) v.resize((size_t)bytes + 16);
+        return reinterpret_cast<T*>(v.data());
+      }
+    }
+  }
+  template <class Pass>
+  int forEach(uint64_t n, const Pass& pass) {
+    if (n < 2048 || threads <= 1) {
+      for (uint64_t i = 0; i < n; ++i) pass(i);
+      return 0;
+    }
+    const long long count = (long long)n;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+    for (long long i = 0; i < count; ++i) pass((uint64_t)i);
+    return 0;
+  }
+  int scan(const uint64_t* in, uint64_t* out, uint64_t n) {
+    uint64_t acc = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint64_t v = in[i];
+      out[i] = acc;
+      acc += v;
+    }
+    out[n] = acc;
+    return 0;
+  }
+  int read(void* dst, const void* src, size_t bytes) {
+    std::memmove(dst, src, bytes);
+    return 0;
+  }
+  int copy(void* dst, const void* src, size_t bytes) {
+    std::memmove(dst, src, bytes);
+    return 0;
+  }
+  int upload(void* dst, const void* src, size_t bytes) {
+    std::memmove(dst, src, bytes);
+    return 0;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+gudni_frame* gudni_serialize_parallel(const gudni_scene_desc* s, const gudni_spec* spec, int threads) {
+  g_error.clear();
+  if (!validate(s, spec)) return nullptr;
+  gudni::ser::Scene sc;
+  int64_t n_pairs = 0;
+  std::unique_ptr<gudni_frame> f(new gudni_frame());
+  std::vector<float4> subs;
+  std::vector<uint64_t> tags;
+  const char* why = gudni::ser::checkScene(s, *spec, sc, n_pairs);
+  if (!why) why = gudni::ser::buildSubstances(s, subs, f->picture_uses, f->radials, tags);
+  if (why) {
+    g_error = why;
+    return nullptr;
+  }
+  f->substances.resize(subs.size() * 4);
+  if (!subs.empty()) std::memcpy(f->substances.data(), subs.data(), subs.size() * sizeof(float4));
+  sc.substance_shape_start = s->substance_shape_start;
+  sc.substance_tag = tags.data();
+  sc.shape_compound = s->shape_compound;
+  sc.shape_outline_start = s->shape_outline_start;
+  sc.outline_pair_start = s->outline_pair_start;
+  sc.pairs = s->pairs;
+  const gudni::ser::Limits lim{spec->max_tile_size, spec->threads_per_tile, spec->max_tiles_per_call,
+                               spec->max_shape, (int64_t)spec->max_strands_per_tile};
+  ThreadExec ex{f.get(), threads > 0 ? threads : omp_get_max_threads()};
+  gudni::ser::Result r;
+  const int rc = gudni::ser::serialize(ex, sc, lim, r, true);
+  if (rc) {
+    g_error = rc == -2 ? "scene too large" : "serializer failed";
+    return nullptr;
+  }
+  f->geometry.resize((size_t)r.geometry_bytes);
+  f->prov.src.resize((size_t)r.n_points * 3);
+  f->prov.w.resize((size_t)r.n_points * 3);
+  f->prov.where.resize((size_t)r.n_points);
+  // the concatenated piles back into jobs: each job's tiles and shapes are contiguous
+  f->jobs.resize((size_t)r.n_jobs);
+  size_t t = 0;
+  for (size_t j = 0; j < f->jobs.size(); ++j) {
+    gudni_frame::Job& job = f->jobs[j];
+    const size_t t0 = t;
+    while (t < r.n_tiles && r.tile_jobs[t] == (int32_t)j) ++t;
+    const uint32_t base = t0 < t ? r.tiles[t0].shapes.start : 0;
+    uint64_t n = 0;
+    for (size_t k = t0; k < t; ++k) {
+      gudni_tile_info ti = r.tiles[k];
+      ti.shapes.start -= base;
+      n += ti.shapes.length;
+      job.tiles.push_back(ti);
+    }
+    job.shapes.assign(r.shapes + base, r.shapes + base + n);
+    job.columns = (int32_t)((t - t0) * (size_t)spec->threads_per_tile);
+  }
+  std::memcpy(f->stats, r.stats, sizeof(f->stats));
   return f.release();
 }
 

@@ -898,9 +898,13 @@ struct LeafMaxPass {
 #if defined(__CUDA_ARCH__)
     atomicMax(&out[0], (unsigned long long)nodes[i].count);
     atomicMax(&out[1], (unsigned long long)nodes[i].strands);
-#else
-    out[0] = nodes[i].count > out[0] ? nodes[i].count : out[0];
-    out[1] = nodes[i].strands > out[1] ? nodes[i].strands : out[1];
+#else  // host threads may run items at once
+    for (int j = 0; j < 2; ++j) {
+      const unsigned long long v = j == 0 ? nodes[i].count : nodes[i].strands;
+      unsigned long long cur = __atomic_load_n(&out[j], __ATOMIC_RELAXED);
+      while (v > cur && !__atomic_compare_exchange_n(&out[j], &cur, v, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+      }
+    }
 #endif
   }
 };

@@ -97,6 +97,8 @@ def load_host():
         lib = C.CDLL(path)
         lib.gudni_serialize.restype = C.c_void_p
         lib.gudni_serialize.argtypes = [C.POINTER(SceneDesc), C.POINTER(Spec)]
+        lib.gudni_serialize_parallel.restype = C.c_void_p
+        lib.gudni_serialize_parallel.argtypes = [C.POINTER(SceneDesc), C.POINTER(Spec), C.c_int]
         lib.gudni_serialize_error.restype = C.c_char_p
         lib.gudni_frame_free.argtypes = [C.c_void_p]
         for name in ("geometry_bytes", "n_substances", "n_picture_uses", "n_radials", "n_jobs"):

@@ -612,10 +612,17 @@ def scene_desc(flat: FlatScene):
     return d, keep
 
 
-def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndarray] = None) -> Frame:
+def serialize_flat(flat: FlatScene, spec: L.Spec, random_field: Optional[np.ndarray] = None,
+                   threads: int = 0) -> Frame:
+    """Serialize a flattened scene.  threads == 1: the sequential restatement of the
+    reference's walk (gudni_serialize); otherwise the same piles from the serializer's
+    data-parallel passes on that many host threads, 0 for all (gudni_serialize_parallel)."""
     lib = L.load_host()
     d, keep = scene_desc(flat)
-    h = lib.gudni_serialize(C.byref(d), C.byref(spec))
+    if threads == 1:
+        h = lib.gudni_serialize(C.byref(d), C.byref(spec))
+    else:
+        h = lib.gudni_serialize_parallel(C.byref(d), C.byref(spec), int(threads))
     if not h:
         raise ValueError("serialize failed: " + lib.gudni_serialize_error().decode())
     try:

@@ -67,6 +67,12 @@ typedef struct gudni_frame gudni_frame;
  * gudni_serialize_error()). */
 gudni_frame* gudni_serialize(const gudni_scene_desc* scene, const gudni_spec* spec);
 const char* gudni_serialize_error(void);
+
+/* The same frame, byte for byte and with the same point provenance, computed by the
+ * serializer's data-parallel passes (the ones gudni_serialize_device runs as kernels)
+ * on `threads` host threads (0: all available).  gudni_serialize is the sequential
+ * restatement of the reference's walk; this is its fast form. */
+gudni_frame* gudni_serialize_parallel(const gudni_scene_desc* scene, const gudni_spec* spec, int threads);
 void gudni_frame_free(gudni_frame* frame);
 
 size_t gudni_frame_geometry_bytes(const gudni_frame* f);

@@ -274,3 +274,26 @@ def test_random_scenes_and_specs():
         check(flat, spec, seeds=(data.draw(st.integers(0, 1000)),))
 
     run()
+
+
+@pytest.mark.parametrize("threads", [2, 0])
+def test_parallel_host_serializer(threads):
+    """gudni_serialize_parallel (the passes on host threads) gives gudni_serialize's
+    frame: piles, jobs, counters and point provenance."""
+    cases = [(S.flatten(F.SCENES[n][0](), *F.SCENES[n][1:3]), F.SCENES[n][3]) for n in F.SCENES]
+    cases.append((G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25), L.make_spec(32, 32, 4096, 511, 8)))
+    spec = L.make_spec(16, 64, 4096, 7, 8)
+    spec.max_tiles_per_call = 5
+    cases.append((G.random_shapes(seed=21, width=150, height=97, n_shapes=30), spec))
+    for flat, spec in cases:
+        a = S.serialize_flat(flat, spec, threads=1)
+        b = S.serialize_flat(flat, spec, threads=threads)
+        assert a.geometry.tobytes() == b.geometry.tobytes()
+        assert a.substances.tobytes() == b.substances.tobytes()
+        assert a.picture_uses.tobytes() == b.picture_uses.tobytes() and a.radials.tobytes() == b.radials.tobytes()
+        assert [(j.shapes.tobytes(), j.tiles.tobytes(), j.columns) for j in a.jobs] == \
+               [(j.shapes.tobytes(), j.tiles.tobytes(), j.columns) for j in b.jobs]
+        assert a.stats == b.stats
+        assert a.point_offsets.tobytes() == b.point_offsets.tobytes()
+        assert a.point_sources.tobytes() == b.point_sources.tobytes()
+        assert a.point_weights.tobytes() == b.point_weights.tobytes()
