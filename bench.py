@@ -542,8 +542,8 @@ def run_adjoint(args):
 def run_scene(args):
     """Scene to pixels on the device: the page's flattened scene (host arrays, what a
     host hands over) serialized by kernels (gudni_serialize_device) and rendered from
-    the frame left on the device; the host serializer (gudni_serialize, one host core)
-    is timed beside it.  A step is one serialization plus one render.  The piles are
+    the frame left on the device; the host serializer is timed beside it, sequential
+    (gudni_serialize) and on all host threads (gudni_serialize_parallel).  A step is one serialization plus one render.  The piles are
     checked byte for byte against the host serializer's and the image against the
     render of the host-serialized frame."""
     import torch
@@ -558,11 +558,12 @@ def run_scene(args):
     spec = L.make_spec(max_tile_size=tile, threads_per_tile=tpt, max_thresholds=4096, max_shape=127,
                        stack_sections=8)
     flat = G.glyph_page(seed=1)
-    host_ms = []
-    for _ in range(max(1, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        host = S.serialize_flat(flat, spec)
-        host_ms.append(1000 * (time.perf_counter() - t0))
+    host_ms = {1: [], 0: []}  # the sequential restatement, and its passes on all host threads
+    for threads in (1, 0):
+        for _ in range(max(1, min(args.steps, 5))):
+            t0 = time.perf_counter()
+            host = S.serialize_flat(flat, spec, threads=threads)
+            host_ms[threads].append(1000 * (time.perf_counter() - t0))
     shapes, tiles, jobs = S.concatenated_piles(host)
     w, h = flat.canvas_w, flat.canvas_h
     r = Rasterizer(spec)
@@ -618,8 +619,9 @@ def run_scene(args):
                        "tiles": int(host.stats["tiles"]), "l2": "flushed between steps (256 MB write)",
                        "inputs": "flattened scene arrays in host memory, uploaded inside each step"},
             "device_serialize_ms": statistics.median(ser_ms), "render_ms": statistics.median(ren_ms),
-            "host_serialize_ms": statistics.median(host_ms),
-            "host_serializer_scene_to_pixels_ms": statistics.median(host_ms) + statistics.median(ren_ms),
+            "host_serialize_ms": {"sequential": statistics.median(host_ms[1]),
+                                  "parallel": statistics.median(host_ms[0]), "host_threads": os.cpu_count()},
+            "host_serializer_scene_to_pixels_ms": statistics.median(host_ms[0]) + statistics.median(ren_ms),
             "gpu_launches": int(launches), "clocks": clocks.summary(),
             "parity": {"piles_identical_to_host_serializer": piles, "image_vs_host_frame": lsb_parity(img, ref)}}
     print(json.dumps(line))
