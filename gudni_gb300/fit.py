@@ -84,7 +84,8 @@ class BatchFit:
         """One Adam step over every scene; returns the summed loss before the step."""
         torch = self.torch
         t0 = time.perf_counter()
-        frames = list(self.pool.map(lambda f: S.serialize_flat(f, self.spec), self.flats))
+        # one scene per pool thread: each serialized on its own thread (threads=1)
+        frames = list(self.pool.map(lambda f: S.serialize_flat(f, self.spec, threads=1), self.flats))
         batch = B.build_batch(frames)
         t1 = time.perf_counter()
         self.r.upload(batch)
