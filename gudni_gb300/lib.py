@@ -135,7 +135,7 @@ def _copy(ptr, count, dtype) -> np.ndarray:
     if count == 0 or not ptr:
         return np.zeros(0, dtype=dtype)
     buf = (C.c_uint8 * (count * dtype.itemsize)).from_address(ptr)
-    return np.frombuffer(bytes(buf), dtype=dtype).copy()
+    return np.frombuffer(buf, dtype=dtype).copy()  # one copy, out of the library's memory
 
 
 # ------------------------------------------------------------------ CUDA library
