@@ -146,6 +146,7 @@ struct gudni_ctx {
   int dense_min = 0;  // gudni_set_dense_columns (0: per-lane scan only)
   uint32_t random_mode = gudni::kRandomField;  // gudni_set_random_source
   uint64_t random_seed = 0;
+  bool device_strands = false;  // gudni_set_device_strand_table
 
   // adjoint scratch: slots x capacity thresholds, provenance and line records
   int adj_grid = 0;
@@ -411,6 +412,14 @@ int upload(gudni_ctx* ctx, DevBuf<T>& buf, const void* src, size_t count, const 
 }
 
 int build_strand_table(gudni_ctx* ctx, const uint8_t* geo, size_t bytes);
+int build_strand_table_device(gudni_ctx* ctx, size_t bytes);
+
+// The strand table of the pile just uploaded: on the host from the caller's copy, or
+// (gudni_set_device_strand_table) on the device from the uploaded one.
+int strand_table_of(gudni_ctx* ctx, const void* geometry, size_t bytes) {
+  if (ctx->device_strands) return build_strand_table_device(ctx, bytes);
+  return build_strand_table(ctx, static_cast<const uint8_t*>(geometry), bytes);
+}
 
 // Every picture usage must read inside a picture pile of `picture_bytes` bytes, from a
 // 4-byte aligned offset; *extent receives the furthest byte any of them reads.
@@ -448,7 +457,7 @@ int upload_common_buffers(gudni_ctx* ctx, const void* geometry, size_t geometry_
   ctx->has_random = random_field != nullptr;
   if (random_field && (rc = upload(ctx, ctx->random_field, random_field, GUDNI_RANDOM_FIELD_SIZE, "random field upload")))
     return rc;
-  if ((rc = build_strand_table(ctx, static_cast<const uint8_t*>(geometry), geometry_bytes))) return rc;
+  if ((rc = strand_table_of(ctx, geometry, geometry_bytes))) return rc;
   ctx->geometry_bytes = geometry_bytes;
   ctx->n_substances = n_substances;
   ctx->picture_bytes = picture_bytes;
@@ -652,6 +661,19 @@ struct SerExec {
   }
 };
 
+// The strand table of the uploaded pile by the device passes (serialize_device.cuh
+// strandTable) on the context's stream; one read of the strand count.
+int build_strand_table_device(gudni_ctx* ctx, size_t bytes) {
+  SerExec ex{ctx, ctx->stream};
+  gudni::ser::StrandTableOut t;
+  const int rc = gudni::ser::strandTable(ex, bytes ? ctx->geometry.ptr : nullptr, bytes, t);
+  if (rc == -2) return fail(ctx, GUDNI_ERR_BAD_INPUT, "too many strands");
+  if (rc) return cuda_fail(ctx, ex.err, "strand table");
+  ctx->n_strands = t.n_strands;
+  ctx->n_units = bytes / 16;
+  return GUDNI_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -804,7 +826,7 @@ int gudni_upload_frame(gudni_ctx* ctx, const void* geometry, size_t geometry_byt
   cudaError_t e;
   if (!ctx->pictures.ptr && (e = ctx->pictures.reserve(0)) != cudaSuccess)  // never hand the kernels a null pile
     return cuda_fail(ctx, e, "picture pile");
-  if ((rc = build_strand_table(ctx, static_cast<const uint8_t*>(geometry), geometry_bytes))) return rc;
+  if ((rc = strand_table_of(ctx, geometry, geometry_bytes))) return rc;
   ctx->geometry_bytes = geometry_bytes;
   ctx->n_substances = n_substances;
   ctx->n_uses = n_picture_uses;
@@ -1204,6 +1226,12 @@ int gudni_enable_counters(gudni_ctx* ctx, int enable) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "counters");
   ctx->counters_on = enable != 0;
+  return GUDNI_OK;
+}
+
+int gudni_set_device_strand_table(gudni_ctx* ctx, int enable) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  ctx->device_strands = enable != 0;
   return GUDNI_OK;
 }
 

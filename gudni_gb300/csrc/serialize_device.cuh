@@ -1042,7 +1042,7 @@ inline const char* buildSubstances(const gudni_scene_desc* s, std::vector<float4
   return nullptr;
 }
 
-// ------------------------------------------------------------ the whole serializer
+// Storage the passes ask their executor for.
 enum Slot {
   kGeometry, kStrandTable, kStrandY, kStrandFirst, kShapes, kTiles, kTileJobs,  // results
   kShapeSub, kBox, kKeep, kKeptAt, kOutlineShape, kOutlineBytes, kByteAt, kOutlineStrands, kStrandAt,
@@ -1051,6 +1051,148 @@ enum Slot {
   kRect, kPairCount, kPairAt, kKeysA, kKeysB, kHist, kHistAt, kTileFirst, kTileEnd,
   kSlots
 };
+
+// ------------------------------------------------------------ strand table of a pile
+// The strand table of an uploaded geometry pile (strand_table.h builds the same by one
+// walk on the host).  The walk follows a chain: the strand at byte 0, then each next
+// one right after it, stopping at the first header that is too short, odd, or runs past
+// the pile, or where fewer than 32 bytes remain.  Here every 16-byte unit reads the
+// header it would hold and points to the unit after that strand (or to a sink when the
+// header is not valid there); the chain from unit 0 is then found by pointer doubling
+// -- round k marks, from every unit already reached, the unit 2^k strands further --
+// so after ceil(log2(units)) + 1 rounds every strand start is marked.  A marked unit
+// with a valid header is a strand; a scan numbers them.
+struct StrandLinkPass {
+  const uint8_t* geo;
+  uint64_t bytes, units;
+  uint64_t* next;     // per unit: the unit after its strand, or `units` (the sink)
+  uint8_t* valid;
+  uint8_t* reached;
+  GUDNI_SHD void operator()(uint64_t u) const {
+    const uint64_t off = 16 * u;
+    bool ok = off + 32 <= bytes;
+    uint32_t size = 0;
+    if (ok) {
+      size = (uint32_t)geo[off] | ((uint32_t)geo[off + 1] << 8);
+      ok = size >= 4 && (size & 1u) == 0 && off + (uint64_t)size * 8 <= bytes && off / 8 <= 0xFFFFFFFFull;
+    }
+    valid[u] = ok ? 1 : 0;
+    next[u] = ok ? u + size / 2 : units;
+    reached[u] = u == 0 ? 1 : 0;
+  }
+};
+
+// one doubling round: reached' = reached plus the units `jump` leads to from reached
+// ones; jump' = jump applied twice
+struct StrandReachPass {
+  const uint64_t* jump;
+  const uint8_t* reached;
+  uint64_t units;
+  uint8_t* reached_next;  // a copy of `reached` beforehand
+  GUDNI_SHD void operator()(uint64_t u) const {
+    if (reached[u] && jump[u] < units) reached_next[jump[u]] = 1;
+  }
+};
+struct StrandJumpPass {
+  const uint64_t* jump;
+  uint64_t units;
+  uint64_t* jump_next;
+  GUDNI_SHD void operator()(uint64_t u) const { jump_next[u] = jump[u] < units ? jump[jump[u]] : units; }
+};
+struct ByteCopyPass {
+  const uint8_t* in;
+  uint8_t* out;
+  GUDNI_SHD void operator()(uint64_t i) const { out[i] = in[i]; }
+};
+struct StrandFlagPass {
+  const uint8_t* reached;
+  const uint8_t* valid;
+  uint64_t* is_start;
+  GUDNI_SHD void operator()(uint64_t u) const { is_start[u] = reached[u] && valid[u] ? 1 : 0; }
+};
+
+// per strand start: its table row, y range and unit mark (strand_table.h's entries)
+struct StrandRowPass {
+  const uint8_t* geo;
+  const uint64_t* is_start;
+  const uint64_t* index;  // exclusive scan of is_start
+  uint4* table;
+  float2* ys;
+  uint32_t* first;
+  GUDNI_SHD void operator()(uint64_t u) const {
+    if (!is_start[u]) {
+      first[u] = kNoStrand;
+      return;
+    }
+    const uint64_t off = 16 * u;
+    const uint32_t size = (uint32_t)geo[off] | ((uint32_t)geo[off + 1] << 8);
+    const float* p = reinterpret_cast<const float*>(geo + off + 8);
+    float lo = INFINITY, hi = -INFINITY;
+    bool nan = false;
+    for (uint32_t i = 0; i + 1 < size; ++i) {  // every point: (size - 1) 8-byte pairs
+      const float y = p[2 * i + 1];
+      if (y != y) nan = true;
+      lo = y < lo ? y : lo;
+      hi = hi < y ? y : hi;
+    }
+    const uint32_t k = (uint32_t)index[u];
+    table[k] = make_uint4((uint32_t)(off / 8), size, floatBits(p[2]), floatBits(p[0]));
+    ys[k] = nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+    first[u] = k;
+  }
+};
+
+struct StrandTableOut {
+  uint4* table;
+  float2* ys;
+  uint32_t* first;
+  uint64_t n_strands;
+};
+
+// The strand table of `bytes` bytes of pile at `geo` (on the executing side).  The
+// table and y ranges go to slots kStrandTable / kStrandY, the per-unit map to
+// kStrandFirst.  Returns 0, -1 (storage) or -2 (more strands than 32-bit indices).
+template <class Ex>
+int strandTable(Ex& ex, const uint8_t* geo, uint64_t bytes, StrandTableOut& out) {
+  int rc;
+  const uint64_t units = bytes / 16;
+  uint64_t* next = ex.template alloc<uint64_t>(kKeysA, units + 1);
+  uint64_t* next2 = ex.template alloc<uint64_t>(kKeysB, units + 1);
+  uint8_t* valid = ex.template alloc<uint8_t>(kRect, units + 1);
+  uint8_t* reached = ex.template alloc<uint8_t>(kPairCount, units + 1);
+  uint8_t* reached2 = ex.template alloc<uint8_t>(kPairAt, units + 1);
+  uint64_t* is_start = ex.template alloc<uint64_t>(kHist, units + 1);
+  uint64_t* index = ex.template alloc<uint64_t>(kHistAt, units + 1);
+  if (!next || !next2 || !valid || !reached || !reached2 || !is_start || !index) return -1;
+  if ((rc = ex.forEach(units, StrandLinkPass{geo, bytes, units, next, valid, reached}))) return rc;
+  int rounds = 1;
+  while (rounds < 64 && (1ull << (rounds - 1)) < units) ++rounds;
+  for (int k = 0; k < rounds; ++k) {
+    if ((rc = ex.forEach(units, ByteCopyPass{reached, reached2}))) return rc;
+    if ((rc = ex.forEach(units, StrandReachPass{next, reached, units, reached2}))) return rc;
+    if ((rc = ex.forEach(units, StrandJumpPass{next, units, next2}))) return rc;
+    uint8_t* tr = reached;
+    reached = reached2;
+    reached2 = tr;
+    uint64_t* tj = next;
+    next = next2;
+    next2 = tj;
+  }
+  if ((rc = ex.forEach(units, StrandFlagPass{reached, valid, is_start}))) return rc;
+  if ((rc = ex.scan(is_start, index, units))) return rc;
+  uint64_t n = 0;
+  if ((rc = ex.read(&n, index + units, 8))) return rc;
+  if (n >= 0xFFFFFFF0ull) return -2;
+  out.table = ex.template alloc<uint4>(kStrandTable, n);
+  out.ys = ex.template alloc<float2>(kStrandY, n);
+  out.first = ex.template alloc<uint32_t>(kStrandFirst, units);
+  if (!out.table || !out.ys || !out.first) return -1;
+  if ((rc = ex.forEach(units, StrandRowPass{geo, is_start, index, out.table, out.ys, out.first}))) return rc;
+  out.n_strands = n;
+  return 0;
+}
+
+// ------------------------------------------------------------ the whole serializer
 
 struct Result {
   uint64_t geometry_bytes = 0, n_strands = 0, n_shapes = 0, n_tiles = 0, n_jobs = 0;

@@ -188,6 +188,8 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_upload_random_field.argtypes = [vp, vp]
     lib.gudni_upload_frame.restype = C.c_int
     lib.gudni_upload_frame.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz]
+    lib.gudni_set_device_strand_table.restype = C.c_int
+    lib.gudni_set_device_strand_table.argtypes = [vp, C.c_int]
     lib.gudni_set_random_source.restype = C.c_int
     lib.gudni_set_random_source.argtypes = [vp, C.c_int, C.c_uint64]
     lib.gudni_serialize_device.restype = C.c_int

@@ -183,6 +183,11 @@ class Rasterizer:
     def enable_counters(self, on: bool = True) -> None:
         self._check(self.lib.gudni_enable_counters(self.ctx, 1 if on else 0))
 
+    def set_device_strand_table(self, on: bool = True) -> None:
+        """Build the strand table of later uploads on the device from the uploaded pile
+        (gudni_set_device_strand_table) instead of on the host; the table is the same."""
+        self._check(self.lib.gudni_set_device_strand_table(self.ctx, 1 if on else 0))
+
     def set_random_source(self, source: int, seed: int = 0) -> None:
         """Where the stochastic jitter comes from when the spec's stochastic_factor
         is not 0 (gudni_set_random_source): lib.RANDOM_FIELD (the reference's random

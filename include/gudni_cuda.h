@@ -324,6 +324,15 @@ int gudni_read_counters(gudni_ctx* ctx, int64_t out[4]);
  * sections, no sharing of values between neighbouring columns; a new seed per frame
  * gives independent jitter per frame.  No reference
  * counterpart.  Takes effect from the next launch. */
+/* Where the uploads (gudni_upload_common, gudni_upload_frame, gudni_batch_upload)
+ * build the strand table the raster kernels read (per strand its offset, size, x
+ * extent and y range, and per 16-byte unit of the pile the strand starting there):
+ * 0 (default) on the host, by one walk of the caller's pile, then uploaded; 1 on the
+ * device from the uploaded pile, by data-parallel passes (the walk's chain found by
+ * pointer doubling) -- the same table, no host walk and no table upload.  Takes effect
+ * from the next upload. */
+int gudni_set_device_strand_table(gudni_ctx* ctx, int enable);
+
 #define GUDNI_RANDOM_FIELD   0
 #define GUDNI_RANDOM_COUNTER 1
 int gudni_set_random_source(gudni_ctx* ctx, int source, uint64_t seed);

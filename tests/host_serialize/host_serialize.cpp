@@ -182,7 +182,42 @@ static const T* arr(Arrays& a, const char* name) {
   return reinterpret_cast<const T*>(it->second.data());
 }
 
+// host_serialize --strands <pile file> <result file> <seed>: the strand table of a
+// geometry pile by the device passes (strandTable).
+static int strands_main(char** argv) {
+  FILE* f = std::fopen(argv[2], "rb");
+  if (!f) return 2;
+  std::vector<uint8_t> pile;
+  uint8_t buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) pile.insert(pile.end(), buf, buf + got);
+  std::fclose(f);
+  Exec ex;
+  ex.rng = std::strtoull(argv[4], nullptr, 10);
+#if defined(__CUDACC__)
+  cudaDeviceGetAttribute(&ex.sm_count, cudaDevAttrMultiProcessorCount, 0);
+#endif
+  const uint8_t* geo = static_cast<const uint8_t*>(ex.place(pile.data(), pile.size()));
+  ser::StrandTableOut t;
+  const int rc = ser::strandTable(ex, pile.empty() ? nullptr : geo, pile.size(), t);
+  FILE* out = std::fopen(argv[3], "wb");
+  if (!out) return 2;
+  if (rc) {
+    put(out, "error", "strand table failed", 19);
+  } else {
+    const std::vector<uint8_t> tb = ex.fetch(t.table, t.n_strands * sizeof(uint4));
+    const std::vector<uint8_t> ys = ex.fetch(t.ys, t.n_strands * sizeof(float2));
+    const std::vector<uint8_t> fi = ex.fetch(t.first, pile.size() / 16 * 4);
+    put(out, "strand_table", tb.data(), tb.size());
+    put(out, "strand_y", ys.data(), ys.size());
+    put(out, "strand_first", fi.data(), fi.size());
+  }
+  std::fclose(out);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 5 && std::strcmp(argv[1], "--strands") == 0) return strands_main(argv);
   if (argc < 4) return 2;
   Arrays a;
   if (!load(argv[1], a)) return 2;

@@ -248,3 +248,36 @@ def test_stochastic_jitter_sources(source):
     want = O.render_frame(frame, random_source=source, random_seed=seed)
     assert not np.array_equal(want, plain)
     assert np.array_equal(got, want), f"{int((got != want).sum())} pixels differ"
+
+
+def test_device_strand_table():
+    """The strand table built on the device from the uploaded pile
+    (gudni_set_device_strand_table) renders the same images as the host-built one,
+    and a pile damaged in the middle gives the same result either way."""
+    flat = G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25)
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, 511, 8))
+
+    def both(fr):
+        outs = []
+        for on in (False, True):
+            with Rasterizer(fr.spec) as r:
+                r.set_device_strand_table(on)
+                try:
+                    outs.append(("image", r.queue_jobs(fr), r.raster_frame(fr)))
+                except RasterError as e:
+                    outs.append(("error", e.code, None))
+        return outs
+
+    (k0, a0, b0), (k1, a1, b1) = both(frame)
+    assert k0 == k1 == "image"
+    assert np.array_equal(a0, a1) and np.array_equal(b0, b1) and np.array_equal(a0, b0)
+    import dataclasses
+    geo = frame.geometry.copy()
+    at = (geo.size // 2) // 16 * 16
+    geo[at:at + 2] = np.frombuffer(np.uint16(7).tobytes(), np.uint8)  # an odd size mid-pile
+    (k0, a0, b0), (k1, a1, b1) = both(dataclasses.replace(frame, geometry=geo))
+    assert k0 == k1
+    if k0 == "image":
+        assert np.array_equal(a0, a1) and np.array_equal(b0, b1)
+    else:
+        assert a0 == a1

@@ -297,3 +297,55 @@ def test_parallel_host_serializer(threads):
         assert a.point_offsets.tobytes() == b.point_offsets.tobytes()
         assert a.point_sources.tobytes() == b.point_sources.tobytes()
         assert a.point_weights.tobytes() == b.point_weights.tobytes()
+
+
+def device_strand_table(geometry, seed=1):
+    """The strand table of a pile by the device passes (strandTable) on the CPU."""
+    from host_serialize.build import build
+    with tempfile.TemporaryDirectory() as d:
+        src, dst = os.path.join(d, "pile.bin"), os.path.join(d, "out.bin")
+        geometry.tofile(src)
+        r = subprocess.run([build(), "--strands", src, dst, str(seed)], capture_output=True, text=True,
+                           env=dict(os.environ, ASAN_OPTIONS="detect_leaks=0"))
+        assert r.returncode == 0, r.stderr[-4000:]
+        return _read(dst)
+
+
+def check_strands(geometry, seed=1):
+    got = device_strand_table(geometry, seed)
+    assert "error" not in got
+    table, ys, first = host_strand_table(geometry)
+    assert got["strand_table"] == table.tobytes()
+    assert got["strand_y"] == ys.tobytes()
+    assert got["strand_first"] == first.tobytes()
+    return len(table)
+
+
+def test_strand_table_of_piles():
+    """The pile walk (strand_table.h) and the pointer-doubling passes give the same
+    table on serialized piles, and stop at the same place on damaged ones: a
+    truncated pile, headers made odd, too small or too large, and a pile cut inside
+    its first strand."""
+    frame = S.serialize_flat(G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25),
+                             L.make_spec(32, 32, 4096, 511, 8))
+    geo = frame.geometry
+    n = check_strands(geo)
+    assert n == frame.stats["strands"]
+    table, _, _ = host_strand_table(geo)
+    rng = np.random.default_rng(5)
+    for trial in range(8):
+        g = geo.copy()
+        k = int(rng.integers(1, len(table)))
+        off = int(table[k][0]) * 8
+        if trial % 4 == 0:
+            g = g[:off + 24]  # cut inside strand k (16-byte multiple kept below)
+            g = g[:len(g) // 16 * 16]
+        elif trial % 4 == 1:
+            g[off:off + 2] = np.frombuffer(np.uint16(7).tobytes(), np.uint8)
+        elif trial % 4 == 2:
+            g[off:off + 2] = np.frombuffer(np.uint16(2).tobytes(), np.uint8)
+        else:
+            g[off:off + 2] = np.frombuffer(np.uint16(60000).tobytes(), np.uint8)
+        assert check_strands(g, seed=trial) == k
+    assert check_strands(geo[:16]) == 0
+    assert check_strands(np.zeros(0, np.uint8)) == 0
