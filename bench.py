@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-sample-frames", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="page4k", choices=sorted(WORKLOADS))
+    ap.add_argument("--device-strand-table", action="store_true",
+                    help="uploads build the strand table on the device (gudni_set_device_strand_table)")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--tile", type=int, default=None, help="tile size (default: the workload's)")
     ap.add_argument("--threads-per-tile", type=int, default=None, help="threads per tile (default: the workload's)")
@@ -728,6 +730,8 @@ def main():
     frame = make_frame(args.workload, False, *tile_override(args, *PLAIN_TILES[args.workload]))
     shapes, tiles, tile_jobs = S.concatenated_piles(frame)
     r = Rasterizer(frame.spec, device=local)
+    if args.device_strand_table:
+        r.set_device_strand_table(True)
     r.upload_common(frame)
     d_shapes = torch.from_numpy(shapes.view(np.uint8).copy()).to(dev)
     d_tiles = torch.from_numpy(tiles.view(np.uint8).copy()).to(dev)
@@ -818,7 +822,8 @@ def main():
            frame.radials.nbytes + frame.random_field.nbytes + shapes.nbytes + tiles.nbytes + tile_jobs.nbytes)
     e2e = {"value": world * pixels / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(pixels * 4), "ms_per_step": 1000 * e2e_s,
-           "call": "gudni_upload_common + gudni_raster_frame (host buffers)"}
+           "call": "gudni_upload_common + gudni_raster_frame (host buffers)",
+           "strand_table": "device" if args.device_strand_table else "host"}
 
     if rank != 0:
         r.close()
