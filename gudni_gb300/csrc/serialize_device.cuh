@@ -1048,9 +1048,58 @@ enum Slot {
   kShapeSub, kBox, kKeep, kKeptAt, kOutlineShape, kOutlineBytes, kByteAt, kOutlineStrands, kStrandAt,
   kKept, kNodesA, kNodesB, kPoolA, kPoolB, kOutNodes, kNodeAt, kOutList, kListAt, kChildSize,
   kChildStrands, kLeafCounts, kShapeAt, kReorder, kPointSources, kPointWeights, kPointOffsets,
-  kRect, kPairCount, kPairAt, kKeysA, kKeysB, kHist, kHistAt, kTileFirst, kTileEnd,
+  kRect, kPairCount, kPairAt, kKeysA, kKeysB, kHist, kHistAt, kTileFirst, kTileEnd, kScanSums, kScanStarts,
   kSlots
 };
+
+// ------------------------------------------------------------ long prefix sums
+// Exclusive prefix sum of n values (out[n] = the total) for any n: short arrays by the
+// executor's scan; long ones in three passes -- every block of kScanChunk values sums
+// itself, the block sums are scanned, and every block writes its prefixes from its
+// block's start -- so the work spreads over n / kScanChunk items.
+constexpr uint64_t kScanChunk = 1024;
+constexpr uint64_t kShortScan = 1 << 16;
+
+struct ChunkSumPass {
+  const uint64_t* in;
+  uint64_t n;
+  uint64_t* sums;
+  GUDNI_SHD void operator()(uint64_t b) const {
+    const uint64_t end = (b + 1) * kScanChunk < n ? (b + 1) * kScanChunk : n;
+    uint64_t acc = 0;
+    for (uint64_t i = b * kScanChunk; i < end; ++i) acc += in[i];
+    sums[b] = acc;
+  }
+};
+struct ChunkScanPass {
+  const uint64_t* in;
+  uint64_t n;
+  const uint64_t* starts;  // exclusive scan of the chunk sums
+  uint64_t* out;
+  GUDNI_SHD void operator()(uint64_t b) const {
+    const uint64_t end = (b + 1) * kScanChunk < n ? (b + 1) * kScanChunk : n;
+    uint64_t acc = starts[b];
+    for (uint64_t i = b * kScanChunk; i < end; ++i) {
+      const uint64_t v = in[i];
+      out[i] = acc;
+      acc += v;
+    }
+    if (end == n) out[n] = acc;
+  }
+};
+
+template <class Ex>
+int scanLong(Ex& ex, const uint64_t* in, uint64_t* out, uint64_t n, int sums_slot, int starts_slot) {
+  if (n <= kShortScan) return ex.scan(in, out, n);
+  const uint64_t chunks = (n + kScanChunk - 1) / kScanChunk;
+  uint64_t* sums = ex.template alloc<uint64_t>(Slot(sums_slot), chunks + 1);
+  uint64_t* starts = ex.template alloc<uint64_t>(Slot(starts_slot), chunks + 1);
+  if (!sums || !starts) return -1;
+  int rc;
+  if ((rc = ex.forEach(chunks, ChunkSumPass{in, n, sums}))) return rc;
+  if ((rc = ex.scan(sums, starts, chunks))) return rc;
+  return ex.forEach(chunks, ChunkScanPass{in, n, starts, out});
+}
 
 // ------------------------------------------------------------ strand table of a pile
 // The strand table of an uploaded geometry pile (strand_table.h builds the same by one
@@ -1179,7 +1228,7 @@ int strandTable(Ex& ex, const uint8_t* geo, uint64_t bytes, StrandTableOut& out)
     next2 = tj;
   }
   if ((rc = ex.forEach(units, StrandFlagPass{reached, valid, is_start}))) return rc;
-  if ((rc = ex.scan(is_start, index, units))) return rc;
+  if ((rc = scanLong(ex, is_start, index, units, kScanSums, kScanStarts))) return rc;
   uint64_t n = 0;
   if ((rc = ex.read(&n, index + units, 8))) return rc;
   if (n >= 0xFFFFFFF0ull) return -2;
@@ -1248,9 +1297,9 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
   GUDNI_SER_TRY(ex.forEach((uint64_t)s.n_substances, ShapeSubstancePass{s, shape_sub}));
   GUDNI_SER_TRY(ex.forEach(n_shapes, ShapeBoxPass{s, box, keep, outline_shape}));
   GUDNI_SER_TRY(ex.forEach(n_outlines, OutlineSizePass{s, outline_shape, keep, obytes, ostrands}));
-  GUDNI_SER_TRY(ex.scan(keep, kept_at, n_shapes));
-  GUDNI_SER_TRY(ex.scan(obytes, byte_at, n_outlines));
-  GUDNI_SER_TRY(ex.scan(ostrands, strand_at, n_outlines));
+  GUDNI_SER_TRY(scanLong(ex, keep, kept_at, n_shapes, kScanSums, kScanStarts));
+  GUDNI_SER_TRY(scanLong(ex, obytes, byte_at, n_outlines, kScanSums, kScanStarts));
+  GUDNI_SER_TRY(scanLong(ex, ostrands, strand_at, n_outlines, kScanSums, kScanStarts));
   uint64_t n_kept = 0, geo_bytes = 0, n_strands = 0;
   GUDNI_SER_TRY(ex.read(&n_kept, kept_at + n_shapes, 8));
   GUDNI_SER_TRY(ex.read(&geo_bytes, byte_at + n_outlines, 8));
@@ -1296,7 +1345,7 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
   uint64_t* pair_at = ex.template alloc<uint64_t>(kPairAt, n_kept + 1);
   if (!rect || !pair_count || !pair_at) return -1;
   GUDNI_SER_TRY(ex.forEach(n_kept, ReachPass{kept, grid_n, tile_side, rect, pair_count}));
-  GUDNI_SER_TRY(ex.scan(pair_count, pair_at, n_kept));
+  GUDNI_SER_TRY(scanLong(ex, pair_count, pair_at, n_kept, kScanSums, kScanStarts));
   uint64_t n_pairs = 0;
   GUDNI_SER_TRY(ex.read(&n_pairs, pair_at + n_kept, 8));
   if (n_pairs > 0xFFFFFFFFull) return -2;
@@ -1317,7 +1366,7 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
     uint32_t* pool_out = ex.template alloc<uint32_t>(Slot(other_pool), pool_cap);
     if (!hist || !hist_at || !keys_out || !pool_out) return -1;
     GUDNI_SER_TRY(ex.forEach(blocks, RadixCountPass{keys, n_pairs, blocks, shift, hist}));
-    GUDNI_SER_TRY(ex.scan(hist, hist_at, (uint64_t)kRadixDigits * blocks));
+    GUDNI_SER_TRY(scanLong(ex, hist, hist_at, (uint64_t)kRadixDigits * blocks, kScanSums, kScanStarts));
     GUDNI_SER_TRY(ex.forEach(blocks, RadixScatterPass{keys, pool, n_pairs, blocks, shift, hist_at, keys_out, pool_out}));
     keys = keys_out;
     pool = pool_out;
@@ -1347,8 +1396,8 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
     uint64_t* cstr = ex.template alloc<uint64_t>(kChildStrands, 2 * n_nodes);
     if (!out_nodes || !node_at || !out_list || !lat || !csize || !cstr) return -1;
     GUDNI_SER_TRY(ex.forEach(n_nodes, SplitCountPass{nodes, kept, pool, lim, out_nodes, out_list, csize, cstr}));
-    GUDNI_SER_TRY(ex.scan(out_nodes, node_at, n_nodes));
-    GUDNI_SER_TRY(ex.scan(out_list, lat, n_nodes));
+    GUDNI_SER_TRY(scanLong(ex, out_nodes, node_at, n_nodes, kScanSums, kScanStarts));
+    GUDNI_SER_TRY(scanLong(ex, out_list, lat, n_nodes, kScanSums, kScanStarts));
     uint64_t next_nodes = 0, new_entries = 0;
     GUDNI_SER_TRY(ex.read(&next_nodes, node_at + n_nodes, 8));
     GUDNI_SER_TRY(ex.read(&new_entries, lat + n_nodes, 8));
@@ -1382,7 +1431,7 @@ int serialize(Ex& ex, const Scene& s, const Limits& lim, Result& res, bool prove
   uint64_t* shape_at = ex.template alloc<uint64_t>(kShapeAt, n_nodes + 1);
   if (!leaf_counts || !shape_at) return -1;
   GUDNI_SER_TRY(ex.forEach(n_nodes, LeafCountPass{nodes, n_nodes, per_job, leaf_counts}));
-  GUDNI_SER_TRY(ex.scan(leaf_counts, shape_at, n_nodes));
+  GUDNI_SER_TRY(scanLong(ex, leaf_counts, shape_at, n_nodes, kScanSums, kScanStarts));
   uint64_t n_refs = 0;
   GUDNI_SER_TRY(ex.read(&n_refs, shape_at + n_nodes, 8));
   if (n_refs > 0xFFFFFFFFull) return -2;

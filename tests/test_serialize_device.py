@@ -349,3 +349,11 @@ def test_strand_table_of_piles():
         assert check_strands(g, seed=trial) == k
     assert check_strands(geo[:16]) == 0
     assert check_strands(np.zeros(0, np.uint8)) == 0
+
+
+def test_strand_table_of_the_page():
+    """The 4K page's pile (a million 16-byte units: the long prefix sums run in
+    chunks) through the pointer-doubling passes."""
+    frame = S.serialize_flat(G.glyph_page(), L.make_spec(32, 32, 4096, 127, 8))
+    assert frame.geometry.size // 16 > (1 << 16)
+    assert check_strands(frame.geometry) == frame.stats["strands"]
