@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--cpu-sample-frames", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="page4k", choices=sorted(WORKLOADS))
+    ap.add_argument("--dense-columns", type=int, default=0,
+                    help="scan columns with at least this many thresholds by the whole warp (0: off)")
     ap.add_argument("--device-strand-table", action="store_true",
                     help="uploads build the strand table on the device (gudni_set_device_strand_table)")
     ap.add_argument("--scenes", type=int, default=256)
@@ -340,6 +342,8 @@ def run_batch(args):
     t_ser = time.perf_counter() - t0
     spec = A.spec_for(32, 32, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
     r = B.BatchRasterizer(spec)
+    if args.dense_columns:
+        r.set_dense_columns(args.dense_columns)
     r.upload(batch)
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -406,7 +410,8 @@ def run_batch(args):
                        "tiles": int(len(batch.tiles)), "shapes": int(sum(f.stats["shapes"] for f in frames)),
                        "max_shape": BATCH_MAX_SHAPE, "max_thresholds": BATCH_MAX_THRESHOLDS,
                        "autotune": {str(k): list(v) for k, v in choice.items()},
-                       "l2": "flushed between steps (256 MB write)", "data": "synthetic, seeded"},
+                       "l2": "flushed between steps (256 MB write)", "data": "synthetic, seeded",
+                       "dense_columns": args.dense_columns},
             "mpixels_per_s": pixels / (batched_ms / 1000) / 1e6,
             "plain_per_scene": {"ms_per_batch": plain_ms, "frames_per_s": n / (plain_ms / 1000),
                                 "launches_per_scene": "3 ordering kernels + fast pass (+ full-capacity pass)",
@@ -732,6 +737,8 @@ def main():
     r = Rasterizer(frame.spec, device=local)
     if args.device_strand_table:
         r.set_device_strand_table(True)
+    if args.dense_columns:
+        r.set_dense_columns(args.dense_columns)
     r.upload_common(frame)
     d_shapes = torch.from_numpy(shapes.view(np.uint8).copy()).to(dev)
     d_tiles = torch.from_numpy(tiles.view(np.uint8).copy()).to(dev)
@@ -847,7 +854,7 @@ def main():
     line = {"metric": WORKLOADS[args.workload][1], "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(frame, args.workload),
+            "config": dict(config_dict(frame, args.workload), dense_columns=args.dense_columns),
             "frames_per_s": 1000.0 / ms * world, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clocks.summary(), "roofline": roofline,
             "work": {"thresholds": counters["thresholds"], "sections": counters["sections"],
