@@ -317,3 +317,25 @@ def test_warp_scan_capacity_and_mixed_columns():
     got, by_warp = host_render_warp(frame, dense_min=st["max_queue"] // 2, seed=8)
     assert 0 < by_warp < 1280
     assert np.array_equal(got, O.render_frame(frame))
+
+
+def test_warp_scan_generated_scenes():
+    """Generated dense scenes (canvas, shape count and sizes, tile shape, stack words,
+    the lanes' resume order) through the warp-cooperative scan: bit for bit the
+    oracle's image every time."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=12, deadline=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 10 ** 6), w=st.integers(8, 48), h=st.integers(8, 40),
+               n=st.integers(4, 90), seg_hi=st.integers(3, 16), tile=st.sampled_from([8, 16, 32]),
+               tpt_mul=st.sampled_from([1, 2, 4]), wide=st.booleans(), lanes=st.integers(0, 10 ** 6))
+    def run(seed, w, h, n, seg_hi, tile, tpt_mul, wide, lanes):
+        flat = G.random_shapes(seed=seed, width=w, height=h, n_shapes=n, seg_lo=2, seg_hi=seg_hi)
+        spec = L.make_spec(tile, tile * tpt_mul, 4096, 255 if wide else 127, 4 if wide else 2)
+        frame = S.serialize_flat(flat, spec)
+        got, _ = host_render_warp(frame, dense_min=0, seed=lanes)
+        want = O.render_frame(frame)
+        assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+
+    run()
