@@ -139,9 +139,34 @@ struct AdjQueue {
     }
   }
   // stable sort (the order the forward pass's sort produces): bottom-up merge sort
-  // through the free slab space below the queue when it has room, else insertion sort
+  // through the free slab space below the queue when it has room, else insertion sort;
+  // with a non-finite coordinate in the queue the reference's bubble sort, as
+  // sortQueue does
   __device__ __forceinline__ void sort() {
     const int n = cap - start;
+    bool ordered = true;
+    for (int i = start; i < cap && ordered; ++i) ordered = keysOrdered(thr[i]);
+    if (!ordered) {
+      bool done = false;
+      for (int k = n; !done; --k) {
+        done = true;
+        for (int i = start; i < start + k - 1; ++i) {
+          if (isBelow(hdr[i], thr[i], hdr[i + 1], thr[i + 1])) {
+            const float4 t = thr[i];
+            const uint32_t h = hdr[i];
+            const int4 p = prov[i];
+            thr[i] = thr[i + 1];
+            hdr[i] = hdr[i + 1];
+            prov[i] = prov[i + 1];
+            thr[i + 1] = t;
+            hdr[i + 1] = h;
+            prov[i + 1] = p;
+            done = false;
+          }
+        }
+      }
+      return;
+    }
     if (n >= 32 && start >= n) {
       int src = start, dst = start - n;
       for (int width = 1; width < n; width *= 2) {
@@ -380,7 +405,8 @@ __device__ __forceinline__ void strandP(const RasterInputs& in, AdjGen& g, size_
     const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
                            fmaxf(r.control.y, r.right.y));
     const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
-    const bool ordered = sum == sum;
+    const float sumX = l.left.x + l.control.x + l.right.x + r.left.x + r.control.x + r.right.x;
+    const bool ordered = fabsf(sum) <= FLT_MAX && fabsf(sumX) <= FLT_MAX;
     if (ordered && lo >= g.c->floatHeight + 1.0f) return;
     spawnP(g, bits, l, r, added, encStrand, status, above || (ordered && hi <= -1.0f));
   }

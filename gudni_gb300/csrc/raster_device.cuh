@@ -442,8 +442,11 @@ __device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* str
                            fminf(r.control.y, r.right.y));
     const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
                            fmaxf(r.control.y, r.right.y));
+    // the culling below needs every coordinate finite: a NaN or infinite one can make
+    // an intercept NaN or infinite, which need not lie in the hull
     const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
-    const bool ordered = sum == sum;  // no NaN among them: the culling below is safe
+    const float sumX = l.left.x + l.control.x + l.right.x + r.left.x + r.control.x + r.right.x;
+    const bool ordered = fabsf(sum) <= FLT_MAX && fabsf(sumX) <= FLT_MAX;
     if (ordered && lo >= g.c->floatHeight + 1.0f) return;  // all below the column: dropped, no enclosure
     spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status, above || (ordered && hi <= -1.0f));
   }
@@ -521,14 +524,46 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
 
 // sortThresholdArray K:1962-1976 replacement: the reference bubble-sorts the queue;
 // its comparator is a strict weak order, so any stable sort gives the same order.
+// isBelow is a strict weak order (lexicographic over top, top x and inverted slope)
+// unless a key is NaN.  A threshold whose width and height differences are finite has
+// no NaN key: top and top x are its own finite components, and the inverted slope is
+// FLT_MAX or a finite width over a non-zero finite height.
+__device__ __forceinline__ bool keysOrdered(float4 t) {
+  return fabsf(t.w - t.z) <= FLT_MAX && fabsf(t.y - t.x) <= FLT_MAX;
+}
+
 // Short queues: insertion sort in place.  Longer ones: bottom-up merge sort using the
 // free part of the column's slab below the queue as the second buffer (when it is
-// large enough), O(n log n) instead of O(n^2).
+// large enough), O(n log n) instead of O(n^2).  Both give the stable sorted order, the
+// order the reference's bubble sort gives, when the comparator is a strict weak order;
+// a queue holding a threshold with a non-finite coordinate takes the reference's
+// bubble sort itself (sortThresholdArray, K:1962-1976), since with a NaN key the
+// orders can differ.
 __device__ __forceinline__ void sortQueue(Queue& q) {
   const int n = q.length();
   const int s = q.start;
   float4* T = q.thr;
   uint32_t* H = q.hdr;
+  bool ordered = true;
+  for (int i = s; i < q.cap && ordered; ++i) ordered = keysOrdered(T[i]);
+  if (!ordered) {
+    bool done = false;
+    for (int k = n; !done; --k) {
+      done = true;
+      for (int i = s; i < s + k - 1; ++i) {
+        if (isBelow(H[i], T[i], H[i + 1], T[i + 1])) {
+          const float4 t = T[i];
+          const uint32_t h = H[i];
+          T[i] = T[i + 1];
+          H[i] = H[i + 1];
+          T[i + 1] = t;
+          H[i + 1] = h;
+          done = false;
+        }
+      }
+    }
+    return;
+  }
   if (n < 32 || s < n) {
     for (int i = s + 1; i < q.cap; ++i) {
       const float4 t = T[i];

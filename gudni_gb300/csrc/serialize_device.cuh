@@ -31,6 +31,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -345,18 +346,18 @@ GUDNI_SHD inline void writeStrand(const Bez* chunk, const BezProv* chunkp, int m
   hdr[1] = 0u;
   const int* row = o.rows + m * kMaxPoints;
   float lo = INFINITY, hi = -INFINITY;
-  bool nan = false;
+  bool bad = false;  // a non-finite coordinate: the range that disables culling (strand_table.h)
   float* p = reinterpret_cast<float*>(o.geo + off + 8);
   for (int i = 0; i < len; ++i) {
     const P2 q = pts[row[i]];
     p[2 * i] = q.x;
     p[2 * i + 1] = q.y;
-    if (q.y != q.y) nan = true;
+    if (!(fabsf(q.x) <= FLT_MAX) || !(fabsf(q.y) <= FLT_MAX)) bad = true;
     lo = q.y < lo ? q.y : lo;
     hi = hi < q.y ? q.y : hi;
   }
   o.table[index] = make_uint4((uint32_t)(off / 8), size, floatBits(p[2]), floatBits(p[0]));
-  o.ys[index] = nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+  o.ys[index] = bad ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
   o.first[off / 16] = index;
 }
 
@@ -1177,16 +1178,16 @@ struct StrandRowPass {
     const uint32_t size = (uint32_t)geo[off] | ((uint32_t)geo[off + 1] << 8);
     const float* p = reinterpret_cast<const float*>(geo + off + 8);
     float lo = INFINITY, hi = -INFINITY;
-    bool nan = false;
+    bool bad = false;
     for (uint32_t i = 0; i + 1 < size; ++i) {  // every point: (size - 1) 8-byte pairs
-      const float y = p[2 * i + 1];
-      if (y != y) nan = true;
+      const float x = p[2 * i], y = p[2 * i + 1];
+      if (!(fabsf(x) <= FLT_MAX) || !(fabsf(y) <= FLT_MAX)) bad = true;
       lo = y < lo ? y : lo;
       hi = hi < y ? y : hi;
     }
     const uint32_t k = (uint32_t)index[u];
     table[k] = make_uint4((uint32_t)(off / 8), size, floatBits(p[2]), floatBits(p[0]));
-    ys[k] = nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+    ys[k] = bad ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
     first[u] = k;
   }
 };

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -23,25 +24,28 @@ namespace gudni {
 constexpr uint32_t kNoStrandIndex = 0xFFFFFFFFu;  // no strand starts at this unit
 
 // y range of every point of one strand (right end, left end and its control, then
-// each tree node's point and control); NaN disables culling for the strand.
+// each tree node's point and control).  A strand with a non-finite coordinate (x or
+// y) gets (-inf, inf), which disables the kernels' culling for it: its curve
+// intercepts can be NaN or infinite, where the culling's reasoning does not hold.
 inline float2 strand_y_range(const uint8_t* strand, uint32_t size) {
   float lo = INFINITY, hi = -INFINITY;
-  bool nan = false;
-  auto take = [&](size_t at) {
-    float y;
-    std::memcpy(&y, strand + at, 4);
-    if (y != y) nan = true;
+  bool bad = false;
+  auto take = [&](size_t at) {  // the point whose x is at byte `at`
+    float x, y;
+    std::memcpy(&x, strand + at, 4);
+    std::memcpy(&y, strand + at + 4, 4);
+    if (!(std::fabs(x) <= FLT_MAX) || !(std::fabs(y) <= FLT_MAX)) bad = true;
     lo = std::min(lo, y);
     hi = std::max(hi, y);
   };
-  take(12);
-  take(20);
-  take(28);
+  take(8);
+  take(16);
+  take(24);
   for (size_t node = 32; node + 16 <= (size_t)size * 8; node += 16) {
-    take(node + 4);
-    take(node + 12);
+    take(node);
+    take(node + 8);
   }
-  return nan ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
+  return bad ? make_float2(-INFINITY, INFINITY) : make_float2(lo, hi);
 }
 
 // `threads` > 1: the y ranges (independent per strand, most of the time of a large

@@ -339,3 +339,69 @@ def test_warp_scan_generated_scenes():
         assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
 
     run()
+
+
+def _poked(flat, seed, value):
+    flat.pairs = flat.pairs.copy()
+    k = np.random.default_rng(seed).integers(0, flat.pairs.size)
+    flat.pairs.reshape(-1)[k] = value
+    return flat
+
+
+def non_finite_cases():
+    """Scenes where a single infinite control-point coordinate once made the product
+    differ from the reference kernels: +inf x on a 1x2 canvas (a NaN sort key, so the
+    queue order depends on the sort algorithm) and -inf y in a glyph scene (a strand
+    wholly above the column whose intercepts are NaN, so skipping them changed the
+    enclosure)."""
+    cases = []
+    for seg_hi in (5, 7, 10):
+        flat = G.random_shapes(seed=1558, width=1, height=2, n_shapes=29, seg_lo=2, seg_hi=seg_hi)
+        cases.append(S.serialize_flat(_poked(flat, 1558, np.inf), L.make_spec(8, 8, 4096, 127, 2)))
+    flat = G.glyph_page(seed=776117, width=40, height=30, n_glyphs=1, n_shapes=1)
+    cases.append(S.serialize_flat(_poked(flat, 776117, -np.inf), L.make_spec(8, 8, 4096, 127, 2)))
+    return cases
+
+
+def test_non_finite_coordinates_follow_the_reference():
+    for frame in non_finite_cases():
+        check(frame)
+        if O.ref_available(127, 2):
+            assert np.array_equal(O.render_frame(frame), O.ref_render_frame(frame, 4096))
+
+
+def test_generated_non_finite_scenes():
+    """Generated scenes with one NaN or infinite coordinate, at several tile shapes,
+    stack sizes and jitter sources: the product's column machine gives the oracle's
+    image.  (Inputs on which the reference's curve halving never ends are skipped:
+    there the kernels stop at their iteration cap and report it.)"""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    from host_column.build import load
+    lib = load()
+
+    @hyp.settings(max_examples=25, deadline=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 10 ** 6), w=st.integers(1, 48), h=st.integers(1, 40), n=st.integers(1, 60),
+               tile=st.sampled_from([8, 16, 32]), glyph=st.booleans(), counter=st.booleans(),
+               value=st.sampled_from([np.nan, np.inf, -np.inf]))
+    def run(seed, w, h, n, tile, glyph, counter, value):
+        if glyph:
+            flat = G.glyph_page(seed=seed, width=max(w, 40), height=max(h, 30), n_glyphs=max(n // 4, 1),
+                                n_shapes=max(n // 8, 1))
+        else:
+            flat = G.random_shapes(seed=seed, width=w, height=h, n_shapes=n, seg_lo=2, seg_hi=12)
+        frame = S.serialize_flat(_poked(flat, seed, value),
+                                 L.make_spec(tile, tile, 4096, 127, 2, stochastic_factor=0.25 if counter else 0.0))
+        lib.host_set_random_source(1 if counter else 0, seed)
+        try:
+            got = host_render(frame)
+        except AssertionError as e:
+            if "(2, 0)" in str(e):  # the iteration cap: the reference's halving would not end
+                return
+            raise
+        finally:
+            lib.host_set_random_source(0, 0)
+        want = O.render_frame(frame, random_source=1 if counter else 0, random_seed=seed)
+        assert np.array_equal(got, want), f"{int((got != want).sum())} of {got.size} pixels differ"
+
+    run()

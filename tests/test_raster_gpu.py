@@ -281,3 +281,12 @@ def test_device_strand_table():
         assert np.array_equal(a0, a1) and np.array_equal(b0, b1)
     else:
         assert a0 == a1
+
+
+def test_non_finite_coordinates_follow_the_oracle():
+    """Single infinite control-point coordinates (a NaN sort key; a strand above the
+    column with NaN intercepts): the kernels' image is the oracle's."""
+    sys.path.insert(0, HERE)
+    from test_host_column import non_finite_cases
+    for frame in non_finite_cases():
+        assert np.array_equal(render(frame), O.render_frame(frame))
