@@ -37,7 +37,12 @@ constexpr float kRight = 1.0f;              // RIGHTBORDER K:91
 constexpr float kFlatness = 0.25f;          // TAXICAB_FLATNESS K:250
 constexpr float kHalf = 0.5f;               // T K:249
 constexpr int kLargePrime = 7919;           // K:83
-constexpr int kBifurcateCap = 96;           // halvings of a quadratic before giving up
+// Halvings of a quadratic before giving up.  With finite coordinates the reference's
+// halving ends within ~131 steps (an x or y extent of at most 2^129 halved to the 0.25
+// flatness; coincident points end it sooner), so the cap changes no finite input; it
+// ends the loops the reference never leaves (an endpoint at +-inf the column position
+// never separates).
+constexpr int kBifurcateCap = 256;
 constexpr int kSectionCap = 1 << 22;        // sections per pixel before giving up
 
 constexpr uint32_t kPositive = 0x80000000u;

@@ -370,6 +370,42 @@ def test_non_finite_coordinates_follow_the_reference():
             assert np.array_equal(O.render_frame(frame), O.ref_render_frame(frame, 4096))
 
 
+def _extreme(seed, w, h, n, values):
+    """A random scene with three coordinates replaced by the given finite values."""
+    flat = G.random_shapes(seed=seed, width=w, height=h, n_shapes=n, seg_lo=2, seg_hi=10)
+    flat.pairs = flat.pairs.copy()
+    where = np.random.default_rng(seed).integers(0, flat.pairs.size, size=len(values))
+    for j, v in zip(where, values):
+        flat.pairs.reshape(-1)[j] = np.float32(v)
+    return flat
+
+
+def test_huge_finite_coordinates_halve_to_the_end():
+    """A curve spanning ~2^124 in x needs 102 halvings before it is flat; a halving cap
+    of 96 once stopped it with the iteration-limit status where the reference renders."""
+    frame = S.serialize_flat(_extreme(0, 1, 1, 1, [3e37, -3e37, 1e30]), L.make_spec(8, 8, 4096, 127, 2))
+    check(frame)
+    if O.ref_available(127, 2):
+        assert np.array_equal(O.render_frame(frame), O.ref_render_frame(frame, 4096))
+
+
+def test_generated_extreme_finite_scenes():
+    """Huge, tiny and subnormal coordinates: finite inputs never reach the halving cap
+    and the column machine gives the oracle's image."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=20, deadline=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 10 ** 6), w=st.integers(1, 40), h=st.integers(1, 30), n=st.integers(1, 40),
+               tile=st.sampled_from([8, 16, 32]),
+               values=st.sampled_from([(3e37, -3e37, 1e30), (1e-30, -1e-30, 1e-20), (1e-40, -1e-42, 1e-39),
+                                       (3e37, 1e-40, -1e30), (3.4e38, -3.4e38, 3.4e38)]))
+    def run(seed, w, h, n, tile, values):
+        check(S.serialize_flat(_extreme(seed, w, h, n, values), L.make_spec(tile, tile, 4096, 127, 2)))
+
+    run()
+
+
 def test_generated_non_finite_scenes():
     """Generated scenes with one NaN or infinite coordinate, at several tile shapes,
     stack sizes and jitter sources: the product's column machine gives the oracle's
