@@ -143,24 +143,28 @@ def build_batch(frames) -> Batch:
         frame_geo_offsets=np.asarray(frame_geo, np.int64), frame_sub_offsets=np.asarray(frame_sub, np.int64))
 
 
+def bind(lib) -> None:
+    """Declare the batch entry points' signatures on the CUDA library."""
+    vp, sz = C.c_void_p, C.c_size_t
+    lib.gudni_batch_upload.restype = C.c_int
+    lib.gudni_batch_upload.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, vp, vp, sz, vp,
+                                       sz, sz]
+    lib.gudni_batch_render.restype = C.c_int
+    lib.gudni_batch_render.argtypes = [vp, C.c_int, vp]
+    lib.gudni_batch_render_tiles.restype = C.c_int
+    lib.gudni_batch_render_tiles.argtypes = [vp, sz, sz, vp]
+    lib.gudni_batch_output.restype = vp
+    lib.gudni_batch_output.argtypes = [vp]
+    lib.gudni_batch_download.restype = C.c_int
+    lib.gudni_batch_download.argtypes = [vp, vp]
+
+
 class BatchRasterizer(Rasterizer):
     """A Rasterizer that holds one uploaded batch."""
 
     def __init__(self, spec: L.Spec, device: int = 0):
         super().__init__(spec, device)
-        lib = self.lib
-        vp, sz = C.c_void_p, C.c_size_t
-        lib.gudni_batch_upload.restype = C.c_int
-        lib.gudni_batch_upload.argtypes = [vp, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, vp, vp, sz, vp,
-                                           sz, sz]
-        lib.gudni_batch_render.restype = C.c_int
-        lib.gudni_batch_render.argtypes = [vp, C.c_int, vp]
-        lib.gudni_batch_render_tiles.restype = C.c_int
-        lib.gudni_batch_render_tiles.argtypes = [vp, sz, sz, vp]
-        lib.gudni_batch_output.restype = vp
-        lib.gudni_batch_output.argtypes = [vp]
-        lib.gudni_batch_download.restype = C.c_int
-        lib.gudni_batch_download.argtypes = [vp, vp]
+        bind(self.lib)
         self.batch = None
 
     def upload(self, batch: Batch, schedule: bool = True) -> None:
