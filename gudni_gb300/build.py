@@ -68,8 +68,12 @@ def _run(cmd: list[str]) -> None:
 def build_host(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     if force or _stale(HOST_LIB, HOST_SOURCES + HOST_DEPS):
-        _run(["g++"] + GXX_FLAGS + ["-shared", "-I", INCLUDE, "-I", CSRC, "-I", cuda_include()] + HOST_SOURCES +
-             ["-o", HOST_LIB])
+        cmd = ["g++"] + GXX_FLAGS + ["-shared", "-I", INCLUDE, "-I", CSRC, "-I", cuda_include()] + HOST_SOURCES + [
+            "-o", HOST_LIB]
+        try:
+            _run(cmd)
+        except RuntimeError:  # a toolchain without OpenMP: the parallel serializer runs on one thread
+            _run([a for a in cmd if a != "-fopenmp"])
     return HOST_LIB
 
 

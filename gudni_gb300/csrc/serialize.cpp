@@ -6,7 +6,9 @@
 
 #include "gudni_serialize.h"
 
+#if defined(_OPENMP)
 #include <omp.h>
+#endif
 
 #include <algorithm>
 #include <cmath>
@@ -772,7 +774,12 @@ gudni_frame* gudni_serialize_parallel(const gudni_scene_desc* s, const gudni_spe
   sc.pairs = s->pairs;
   const gudni::ser::Limits lim{spec->max_tile_size, spec->threads_per_tile, spec->max_tiles_per_call,
                                spec->max_shape, (int64_t)spec->max_strands_per_tile};
-  ThreadExec ex{f.get(), threads > 0 ? threads : omp_get_max_threads()};
+#if defined(_OPENMP)
+  const int all_threads = omp_get_max_threads();
+#else  // built without OpenMP: the passes' loops run on the calling thread
+  const int all_threads = 1;
+#endif
+  ThreadExec ex{f.get(), threads > 0 ? threads : all_threads};
   gudni::ser::Result r;
   const int rc = gudni::ser::serialize(ex, sc, lim, r, true);
   if (rc) {
