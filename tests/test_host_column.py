@@ -175,6 +175,43 @@ def test_adjoint_column_code_matches_fp64_reference(name):
         assert norm <= 1e-3 and worst <= 1e-3, (what, norm, worst)
 
 
+def test_adjoint_column_code_generated_scenes():
+    """Generated scenes, tile shapes and targets through the adjoint's column code: the
+    float image equals the FP64 reference's forward within 1e-6, and the gradients
+    agree with its gradients to a relative norm of 1e-3 and, element by element (those
+    above 1 % of the largest), to 1e-2; zero where the reference's are zero.  (Over 400
+    such scenes the worst seen were 7e-5 and 2.7e-3.)"""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 10 ** 6), w=st.integers(1, 96), h=st.integers(1, 80), n=st.integers(1, 40),
+               tile=st.sampled_from([8, 16, 32]), tpt_mul=st.sampled_from([1, 2, 4]), glyph=st.booleans(),
+               sigma=st.sampled_from([0.5, 2.0]))
+    def run(seed, w, h, n, tile, tpt_mul, glyph, sigma):
+        def make():
+            if glyph:
+                return G.glyph_page(seed=seed, width=max(w, 40), height=max(h, 30), n_glyphs=max(n // 2, 1),
+                                    n_shapes=max(n // 4, 1))
+            return G.random_shapes(seed=seed, width=w, height=h, n_shapes=n)
+        spec = L.make_spec(tile, tile * tpt_mul, 4096, 127, 8)
+        frame = S.serialize_flat(make(), spec)
+        t = make()
+        t.pairs = (t.pairs + np.random.default_rng(seed).normal(0, sigma, t.pairs.shape)).astype(np.float32)
+        target = O.render_float(S.serialize_flat(t, spec))
+        _, g_geo, g_sub, img_ref = O.loss_and_gradient(frame, target)
+        img, gg, gs = host_adjoint(frame, target, capacity=4096)
+        np.testing.assert_allclose(img, img_ref, rtol=1e-6, atol=1e-6)
+        for got, want, what in ((gg, g_geo, "geometry"), (gs, g_sub, "substances")):
+            if not np.any(want):
+                assert not np.any(got), what
+                continue
+            norm, worst = _rel(got, want)
+            assert norm <= 1e-3 and worst <= 1e-2, (what, norm, worst)
+
+    run()
+
+
 def test_strand_table_threads_give_the_same_table():
     """The C ABI builds the strand table's y ranges on several host threads; the table
     is the one-thread table, entry for entry."""
