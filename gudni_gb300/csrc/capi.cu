@@ -46,6 +46,7 @@ struct DevBuf {
     ptr = nullptr;
     cap = 0;
     size_t want = std::max<size_t>(n, 1);
+    if (want > SIZE_MAX / sizeof(T)) return cudaErrorMemoryAllocation;  // the byte count would wrap
     cudaError_t e = cudaMalloc(&ptr, want * sizeof(T));
     if (e == cudaSuccess) cap = want;
     return e;
@@ -615,6 +616,7 @@ struct SerExec {
   }
   template <class T>
   T* alloc(gudni::ser::Slot slot, uint64_t n) {
+    if (n > UINT64_MAX / sizeof(T)) return nullptr;  // the byte count would wrap: a storage error
     const uint64_t bytes = n * sizeof(T);
     void* p;
     switch (slot) {
