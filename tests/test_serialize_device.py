@@ -276,6 +276,30 @@ def test_random_scenes_and_specs():
     run()
 
 
+def test_extreme_finite_coordinates():
+    """Huge (up to 3.4e38), tiny and subnormal control-point coordinates: the passes'
+    piles equal the host serializer's byte for byte (their box, split and tile tests
+    compare floats and never convert them to integers)."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    values = {"huge": [3e37, -3e37, 1e30], "tiny": [1e-30, -1e-30, 1e-20], "subnormal": [1e-40, -1e-42, 1e-39],
+              "mixed": [3e37, 1e-40, -1e30], "max": [3.4e38, -3.4e38, 3.4e38]}
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(seed=st.integers(0, 10 ** 6), w=st.integers(1, 200), h=st.integers(1, 150), n=st.integers(1, 30),
+               tile=st.sampled_from([8, 16, 32]), mode=st.sampled_from(sorted(values)))
+    def run(seed, w, h, n, tile, mode):
+        flat = G.random_shapes(seed=seed, width=w, height=h, n_shapes=n, seg_lo=2, seg_hi=10)
+        flat.pairs = flat.pairs.copy()
+        for j, v in zip(np.random.default_rng(seed).integers(0, flat.pairs.size, size=3), values[mode]):
+            flat.pairs.reshape(-1)[j] = np.float32(v)
+        spec = L.make_spec(tile, tile, 4096, 127, 8)
+        spec.max_tiles_per_call = 64
+        check(flat, spec)
+
+    run()
+
+
 @pytest.mark.parametrize("threads", [2, 0])
 def test_parallel_host_serializer(threads):
     """gudni_serialize_parallel (the passes on host threads) gives gudni_serialize's
