@@ -170,3 +170,39 @@ def test_bindings_match_the_header_prototypes():
         want = c_kind(ret)
         if want not in (None, ("int", 4)):
             assert ctypes_kind(fn.restype) == want, (name, fn.restype, ret)
+
+
+HASKELL_KINDS = {"CInt": ("int", 4), "Int32": ("int", 4), "CUInt": ("int", 4), "Word32": ("int", 4),
+                 "CSize": ("int", 8), "Word64": ("int", 8), "Int64": ("int", 8), "CULong": ("int", 8),
+                 "CLong": ("int", 8), "CFloat": ("float", 4), "Float": ("float", 4), "CDouble": ("float", 8),
+                 "Double": ("float", 8), "CString": ("ptr", 8), "()": None}
+
+
+def haskell_kind(t):
+    t = " ".join(t.split())
+    while t.startswith("(") and t.endswith(")") and t != "()":
+        t = t[1:-1].strip()
+    if t.startswith("Ptr ") or t.startswith("FunPtr "):
+        return ("ptr", 8)
+    assert t in HASKELL_KINDS, f"unmapped Haskell type {t!r}"
+    return HASKELL_KINDS[t]
+
+
+def test_haskell_imports_match_the_header_prototypes():
+    """The foreign imports of the Haskell drop-in module written out for integration
+    take the arguments and return the result the header declares (number, and pointer,
+    integer or float of each, with its size)."""
+    import re
+    protos = header_prototypes()
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    imports = re.findall(r'foreign import ccall (?:safe|unsafe) "(gudni_[a-z0-9_]+)"\s+\w+\s*::\s*(.*?)'
+                         r'\bIO\s+(\(\s*\)|\([^)]*\)|\w+)', text, flags=re.S)
+    assert len(imports) >= 10
+    for name, args, result in imports:
+        assert name in protos, f"{name} is not declared in include/"
+        ret, params = protos[name]
+        types = [a for a in args.split("->") if a.strip()]
+        assert len(types) == len(params), (name, len(types), params)
+        for i, (t, p) in enumerate(zip(types, params)):
+            assert haskell_kind(t) == c_kind(p), (name, i, t, p)
+        assert haskell_kind(result) == c_kind(ret), (name, result, ret)
