@@ -404,9 +404,10 @@ __device__ __forceinline__ void strandP(const RasterInputs& in, AdjGen& g, size_
                            fminf(r.control.y, r.right.y));
     const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
                            fmaxf(r.control.y, r.right.y));
-    const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
-    const float sumX = l.left.x + l.control.x + l.right.x + r.left.x + r.control.x + r.right.x;
-    const bool ordered = fabsf(sum) <= FLT_MAX && fabsf(sumX) <= FLT_MAX;
+    const float extent = fabsf(l.left.y) + fabsf(l.control.y) + fabsf(l.right.y) + fabsf(r.left.y) +
+                       fabsf(r.control.y) + fabsf(r.right.y) + fabsf(l.left.x) + fabsf(l.control.x) +
+                       fabsf(l.right.x) + fabsf(r.left.x) + fabsf(r.control.x) + fabsf(r.right.x);
+    const bool ordered = extent <= kCullExtent;
     if (ordered && lo >= g.c->floatHeight + 1.0f) return;
     spawnP(g, bits, l, r, added, encStrand, status, above || (ordered && hi <= -1.0f));
   }

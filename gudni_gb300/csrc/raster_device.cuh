@@ -35,6 +35,10 @@ constexpr float kMinCrop = 0.2f;            // MINCROP K:47
 constexpr float kLeft = 0.0f;               // LEFTBORDER K:90
 constexpr float kRight = 1.0f;              // RIGHTBORDER K:91
 constexpr float kFlatness = 0.25f;          // TAXICAB_FLATNESS K:250
+// Hulls whose coordinates' magnitudes sum to more than this are not culled: below 2^21
+// per coordinate the intercept arithmetic stays finite and its rounding far inside
+// the one-pixel culling margin.
+constexpr float kCullExtent = 2097152.0f;
 constexpr float kHalf = 0.5f;               // T K:249
 constexpr int kLargePrime = 7919;           // K:83
 // Halvings of a quadratic before giving up.  With finite coordinates the reference's
@@ -447,11 +451,15 @@ __device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* str
                            fminf(r.control.y, r.right.y));
     const float hi = fmaxf(fmaxf(fmaxf(l.left.y, l.control.y), fmaxf(l.right.y, r.left.y)),
                            fmaxf(r.control.y, r.right.y));
-    // the culling below needs every coordinate finite: a NaN or infinite one can make
-    // an intercept NaN or infinite, which need not lie in the hull
-    const float sum = l.left.y + l.control.y + l.right.y + r.left.y + r.control.y + r.right.y;
-    const float sumX = l.left.x + l.control.x + l.right.x + r.left.x + r.control.x + r.right.x;
-    const bool ordered = fabsf(sum) <= FLT_MAX && fabsf(sumX) <= FLT_MAX;
+    // the culling below needs intercepts that are numbers inside the hull's y range
+    // (give or take rounding within the one-pixel margin): a NaN or infinite
+    // coordinate, or finite ones so large that a difference or product overflows, can
+    // make an intercept NaN or infinite.  The sum of the twelve magnitudes (NaN or
+    // infinite whenever one is) bounds every coordinate.
+    const float extent = fabsf(l.left.y) + fabsf(l.control.y) + fabsf(l.right.y) + fabsf(r.left.y) +
+                       fabsf(r.control.y) + fabsf(r.right.y) + fabsf(l.left.x) + fabsf(l.control.x) +
+                       fabsf(l.right.x) + fabsf(r.left.x) + fabsf(r.control.x) + fabsf(r.right.x);
+    const bool ordered = extent <= kCullExtent;
     if (ordered && lo >= g.c->floatHeight + 1.0f) return;  // all below the column: dropped, no enclosure
     spawnThresholds(g, shapeBit, l, r, added, enclosedByStrand, status, above || (ordered && hi <= -1.0f));
   }

@@ -49,6 +49,11 @@
 namespace gudni {
 namespace ser {
 
+// Magnitude beyond which a coordinate disables the kernels' y culling of its strand
+// (the strand table's y range becomes (-inf, inf)); the host strand table
+// (strand_table.h) uses the same bound.
+constexpr float kStrandCullExtent = 2097152.0f;  // 2^21
+
 constexpr int kMaxCurves = 16;                  // curves per strand (Strand.hs:178, mAXsECTIONsIZE/2)
 constexpr int kMaxPoints = 2 * kMaxCurves + 1;  // points of the largest strand
 constexpr int kRows = kMaxCurves + 1;           // reorder rows, by curve count
@@ -346,13 +351,13 @@ GUDNI_SHD inline void writeStrand(const Bez* chunk, const BezProv* chunkp, int m
   hdr[1] = 0u;
   const int* row = o.rows + m * kMaxPoints;
   float lo = INFINITY, hi = -INFINITY;
-  bool bad = false;  // a non-finite coordinate: the range that disables culling (strand_table.h)
+  bool bad = false;  // a coordinate beyond kStrandCullExtent: the range that disables culling
   float* p = reinterpret_cast<float*>(o.geo + off + 8);
   for (int i = 0; i < len; ++i) {
     const P2 q = pts[row[i]];
     p[2 * i] = q.x;
     p[2 * i + 1] = q.y;
-    if (!(fabsf(q.x) <= FLT_MAX) || !(fabsf(q.y) <= FLT_MAX)) bad = true;
+    if (!(fabsf(q.x) <= kStrandCullExtent) || !(fabsf(q.y) <= kStrandCullExtent)) bad = true;
     lo = q.y < lo ? q.y : lo;
     hi = hi < q.y ? q.y : hi;
   }
@@ -1181,7 +1186,7 @@ struct StrandRowPass {
     bool bad = false;
     for (uint32_t i = 0; i + 1 < size; ++i) {  // every point: (size - 1) 8-byte pairs
       const float x = p[2 * i], y = p[2 * i + 1];
-      if (!(fabsf(x) <= FLT_MAX) || !(fabsf(y) <= FLT_MAX)) bad = true;
+      if (!(fabsf(x) <= kStrandCullExtent) || !(fabsf(y) <= kStrandCullExtent)) bad = true;
       lo = y < lo ? y : lo;
       hi = hi < y ? y : hi;
     }

@@ -23,10 +23,17 @@ namespace gudni {
 
 constexpr uint32_t kNoStrandIndex = 0xFFFFFFFFu;  // no strand starts at this unit
 
+// Coordinates beyond this magnitude disable the kernels' y culling of their strand:
+// at and below it the curve intercepts stay finite and inside the strand's y range up
+// to rounding far below the culling's one-pixel margin; a NaN or infinite coordinate,
+// or finite ones so large that a difference or product overflows, can make an
+// intercept NaN or infinite, where the culling's reasoning does not hold.
+constexpr float kStrandCullExtent = 2097152.0f;  // 2^21
+
 // y range of every point of one strand (right end, left end and its control, then
-// each tree node's point and control).  A strand with a non-finite coordinate (x or
-// y) gets (-inf, inf), which disables the kernels' culling for it: its curve
-// intercepts can be NaN or infinite, where the culling's reasoning does not hold.
+// each tree node's point and control).  A strand with a coordinate (x or y) that is
+// NaN, infinite or beyond kStrandCullExtent in magnitude gets (-inf, inf), which
+// disables the kernels' culling for it.
 inline float2 strand_y_range(const uint8_t* strand, uint32_t size) {
   float lo = INFINITY, hi = -INFINITY;
   bool bad = false;
@@ -34,7 +41,7 @@ inline float2 strand_y_range(const uint8_t* strand, uint32_t size) {
     float x, y;
     std::memcpy(&x, strand + at, 4);
     std::memcpy(&y, strand + at + 4, 4);
-    if (!(std::fabs(x) <= FLT_MAX) || !(std::fabs(y) <= FLT_MAX)) bad = true;
+    if (!(std::fabs(x) <= kStrandCullExtent) || !(std::fabs(y) <= kStrandCullExtent)) bad = true;
     lo = std::min(lo, y);
     hi = std::max(hi, y);
   };

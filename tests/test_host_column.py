@@ -426,6 +426,19 @@ def test_huge_finite_coordinates_halve_to_the_end():
         assert np.array_equal(O.render_frame(frame), O.ref_render_frame(frame, 4096))
 
 
+def test_coordinates_near_float_max_are_not_culled():
+    """Finite coordinates near +-3.4e38: a curve difference overflows and its intercept
+    is infinite although every point is finite; y culling of such a strand once changed
+    two pixels of this 8x1 scene.  Strands and hulls with coordinates beyond 2^21 are no
+    longer culled (per lane and by the warp)."""
+    frame = S.serialize_flat(_extreme(16, 8, 1, 6, [3.4e38, -3.4e38, 3.4e38]), L.make_spec(8, 8, 4096, 127, 2))
+    check(frame)
+    got, _ = host_render_warp(frame, dense_min=0, seed=16)
+    assert np.array_equal(got, O.render_frame(frame))
+    if O.ref_available(127, 2):
+        assert np.array_equal(O.render_frame(frame), O.ref_render_frame(frame, 4096))
+
+
 def test_generated_extreme_finite_scenes():
     """Huge, tiny and subnormal coordinates: finite inputs never reach the halving cap
     and the column machine gives the oracle's image."""
