@@ -441,7 +441,7 @@ def test_coordinates_near_float_max_are_not_culled():
 
 def test_generated_extreme_finite_scenes():
     """Huge, tiny and subnormal coordinates: finite inputs never reach the halving cap
-    and the column machine gives the oracle's image."""
+    and the column machine, per lane and by the warp, gives the oracle's image."""
     hyp = pytest.importorskip("hypothesis")
     st = hyp.strategies
 
@@ -451,7 +451,10 @@ def test_generated_extreme_finite_scenes():
                values=st.sampled_from([(3e37, -3e37, 1e30), (1e-30, -1e-30, 1e-20), (1e-40, -1e-42, 1e-39),
                                        (3e37, 1e-40, -1e30), (3.4e38, -3.4e38, 3.4e38)]))
     def run(seed, w, h, n, tile, values):
-        check(S.serialize_flat(_extreme(seed, w, h, n, values), L.make_spec(tile, tile, 4096, 127, 2)))
+        frame = S.serialize_flat(_extreme(seed, w, h, n, values), L.make_spec(tile, tile, 4096, 127, 2))
+        check(frame)
+        got, _ = host_render_warp(frame, dense_min=0, seed=seed)  # every column by the warp
+        assert np.array_equal(got, O.render_frame(frame))
 
     run()
 
