@@ -285,8 +285,10 @@ def test_device_strand_table():
 
 def test_non_finite_coordinates_follow_the_oracle():
     """Single infinite control-point coordinates (a NaN sort key; a strand above the
-    column with NaN intercepts): the kernels' image is the oracle's."""
+    column with NaN intercepts) and finite ones near float max (an intercept that
+    overflows): the kernels' image is the oracle's."""
     sys.path.insert(0, HERE)
-    from test_host_column import non_finite_cases
-    for frame in non_finite_cases():
+    from test_host_column import _extreme, non_finite_cases
+    near_max = S.serialize_flat(_extreme(16, 8, 1, 6, [3.4e38, -3.4e38, 3.4e38]), L.make_spec(8, 8, 4096, 127, 2))
+    for frame in non_finite_cases() + [near_max]:
         assert np.array_equal(render(frame), O.render_frame(frame))
