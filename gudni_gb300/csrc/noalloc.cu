@@ -11,10 +11,18 @@
 // The array is a file-scope __device__ symbol.  In host code its name is only a
 // host-side stand-in, not a device address, so the first call on each device looks
 // the address up with cudaGetSymbolAddress (with that device current) and caches it;
-// that first call should come before any stream capture.  All calls share the array
-// and it keeps the previous call's contents: the status word and the work counter
-// are cleared at the start of every call, and calls whose launches overlap on the
-// GPU race on it.
+// that first call should come before any stream capture.  The cached address belongs
+// to the device's primary context: after cudaDeviceReset the module is loaded again
+// and the array may move, so a process that resets a device must not call this entry
+// point on it again.  All calls share the array and it keeps the previous call's
+// contents: the status word and the work counter are cleared at the start of every
+// call, and calls whose launches overlap on the GPU race on it.
+//
+// Width of the launch: at the default capacity of 512 thresholds per column and a
+// max_shape of 127 one slot takes 10,748 bytes, so the array holds 6,144 slots -- 48
+// blocks of 128 threads, fewer blocks than the GPU has SMs.  The array trades that
+// width for needing no allocation; the context entry points size their scratch to the
+// whole GPU.
 
 #include <cuda_runtime.h>
 
@@ -93,36 +101,17 @@ extern "C" int gudni_raster_job_noalloc(const gudni_spec* spec, const void* geom
       ((uint64_t)n_tiles << gudni::chunkLog2(compute_depth)) >= gudni::kMaxUnits || n_shapes > 0xFFFFFFFFull)
     return fail(GUDNI_ERR_BAD_INPUT, "too many tiles or shapes");
 
+  if (spec->stochastic_factor != 0.0f)
+    return fail(GUDNI_ERR_BAD_INPUT, "stochastic_factor must be 0 on this path (it takes no random field)");
+
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t e;
-  // Check the tile and picture-use records on the host, a few at a time through a
-  // stack buffer (the kernel bounds-checks every other record it reads).
-  {
-    gudni_tile_info buf[64];
-    for (size_t i = 0; i < n_tiles; i += 64) {
-      const size_t n = n_tiles - i < 64 ? n_tiles - i : 64;
-      if ((e = cudaMemcpy(buf, tiles + i, n * sizeof(gudni_tile_info), cudaMemcpyDeviceToHost)) != cudaSuccess)
-        return fail(GUDNI_ERR_CUDA, std::string("reading tiles: ") + cudaGetErrorString(e));
-      for (size_t k = 0; k < n; ++k) {
-        const gudni_tile_info& t = buf[k];
-        if ((uint64_t)t.shapes.start + t.shapes.length > n_shapes || t.hdepth < 0 || t.hdepth > 24 ||
-            t.vdepth < 0 || t.vdepth > 24 || t.left < 0 || t.top < 0)
-          return fail(GUDNI_ERR_BAD_INPUT, "tile " + std::to_string(i + k) + " is malformed");
-      }
-    }
-    gudni_picture_use ubuf[64];
-    for (size_t i = 0; i < n_picture_uses; i += 64) {
-      const size_t n = n_picture_uses - i < 64 ? n_picture_uses - i : 64;
-      if ((e = cudaMemcpy(ubuf, picture_uses + i, n * sizeof(gudni_picture_use), cudaMemcpyDeviceToHost)) != cudaSuccess)
-        return fail(GUDNI_ERR_CUDA, std::string("reading picture uses: ") + cudaGetErrorString(e));
-      for (size_t k = 0; k < n; ++k) {
-        const gudni_picture_use& u = ubuf[k];
-        if (u.size_x < 0 || u.size_y < 0 || u.mem_offset < 0 || (u.mem_offset & 3) != 0 ||
-            (uint64_t)u.mem_offset + 4ull * (uint64_t)u.size_x * (uint64_t)u.size_y > picture_bytes)
-          return fail(GUDNI_ERR_BAD_INPUT, "picture use " + std::to_string(i + k) + " points outside the picture pile");
-      }
-    }
-  }
+  // Nothing is read back before the launch: the records may still be in flight on
+  // `stream` (written there by the caller's asynchronous copies), and only work
+  // enqueued on that stream is ordered after them.  The kernel checks every record it
+  // reads -- each tile against the shape pile and canvas (tileOk), each picture use's
+  // offset and texel against the picture pile (readColor) -- and reports a bad one in
+  // the status word read below.
 
   // Carve the fixed scratch: header, then per-slot queues and shape-index tables.
   const int capacity = spec->max_thresholds < GUDNI_NOALLOC_CAPACITY ? spec->max_thresholds : GUDNI_NOALLOC_CAPACITY;

@@ -35,9 +35,10 @@ constexpr float kMinCrop = 0.2f;            // MINCROP K:47
 constexpr float kLeft = 0.0f;               // LEFTBORDER K:90
 constexpr float kRight = 1.0f;              // RIGHTBORDER K:91
 constexpr float kFlatness = 0.25f;          // TAXICAB_FLATNESS K:250
-// Hulls whose coordinates' magnitudes sum to more than this are not culled: below 2^21
-// per coordinate the intercept arithmetic stays finite and its rounding far inside
-// the one-pixel culling margin.
+// Hulls whose twelve coordinate magnitudes SUM to more than this are not culled (the
+// strand table bounds each coordinate by it instead, so the hull test is the stricter
+// of the two): below 2^21 per coordinate the intercept arithmetic stays finite and its
+// rounding far inside the one-pixel culling margin.
 constexpr float kCullExtent = 2097152.0f;
 constexpr float kHalf = 0.5f;               // T K:249
 constexpr int kLargePrime = 7919;           // K:83
@@ -678,6 +679,13 @@ __device__ __forceinline__ float4 readColor(const RasterInputs& in, int px, int 
     return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
   const gudni_picture_use u = in.uses[id];
+  // a texel is read as one aligned 4-byte word: the picture's offset must be a
+  // non-negative multiple of 4 (checked here as well as by the uploads, so that a
+  // record written straight into device memory cannot misalign the read)
+  if (u.mem_offset < 0 || (u.mem_offset & 3) != 0) {
+    status |= kStatusBadInput;
+    return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
   float scale = u.scale < 1e-7f ? 1e-7f : u.scale;
   int rx = (int)(((float)px / scale) - u.translate_x);  // cvt.rzi: saturating, NaN -> 0
   int ry = (int)(((float)py / scale) - u.translate_y);

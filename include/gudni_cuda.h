@@ -397,14 +397,20 @@ int gudni_batch_adjoint(gudni_ctx* ctx, const float* target, float* image,
  * thresholds per column (min with spec->max_thresholds); a column that needs more
  * returns GUDNI_ERR_THRESHOLD_OVERFLOW, and a max_shape too large for the scratch
  * returns GUDNI_ERR_BAD_INPUT.  No context is needed; the spec supplies max_shape
- * and threads per tile.
+ * and threads per tile.  The path takes no random field: a spec with a non-zero
+ * stochastic_factor is refused with GUDNI_ERR_BAD_INPUT.
  *
  * The first call on a device looks up the scratch's device address (with that device
- * current); make that first call before any stream capture.  Every call shares the
- * one scratch array, so calls whose launches overlap on the GPU race: issue them on
- * one stream, or serialise them.  The call enqueues on `stream` (NULL = the legacy
- * default stream) and waits for it to read the device status.  Error messages are
- * read with gudni_last_error(NULL). */
+ * current); make that first call before any stream capture.  The address is kept for
+ * the life of the process: do not call this entry point again on a device after
+ * cudaDeviceReset.  Every call shares the one scratch array, so calls whose launches
+ * overlap on the GPU race: issue them on one stream, or serialise them.  The call
+ * enqueues its work on `stream` (NULL = the legacy default stream) after whatever the
+ * caller enqueued there before -- it reads none of the records from the host, so
+ * records still being copied on `stream` are fine -- and then waits for `stream` to
+ * read the device status.  Malformed tiles and picture uses are found by the kernel
+ * and returned as GUDNI_ERR_BAD_INPUT.  Error messages are read with
+ * gudni_last_error(NULL). */
 int gudni_raster_job_noalloc(const gudni_spec* spec,
                              const void* geometry, size_t geometry_bytes,
                              const float* substances, size_t n_substances,

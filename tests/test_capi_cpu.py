@@ -70,3 +70,22 @@ def test_headers_compile_as_c_and_link(tmp_path):
                         str(exe), cuda_lib, host_lib, "-Wl,-rpath," + os.path.dirname(cuda_lib)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_no_alloc_refuses_a_stochastic_spec():
+    """The no-allocation entry point takes no random field: a spec with a non-zero
+    STOCHASTIC_FACTOR is refused before anything reaches a device (the pointers below
+    are never dereferenced)."""
+    lib = L.load_cuda()
+    fn = lib.gudni_raster_job_noalloc
+    fn.restype = C.c_int
+    vp, sz, i32 = C.c_void_p, C.c_size_t, C.c_int32
+    fn.argtypes = [C.POINTER(L.Spec), vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz,
+                   i32, i32, i32, i32, vp, vp, vp]
+    spec = L.make_spec(32, 32, 4096, 127, 2, stochastic_factor=0.25)
+    bg = (C.c_float * 4)(1, 1, 1, 1)
+    fake = 1 << 20  # 16-byte aligned, never read
+    rc = fn(C.byref(spec), fake, 16, fake, 1, None, 0, None, 0, None, 0, fake, 1, fake, 1, 32, 32, 5, 0, bg, fake,
+            None)
+    assert rc == -1
+    assert "stochastic" in lib.gudni_last_error(None).decode()

@@ -292,3 +292,45 @@ def test_non_finite_coordinates_follow_the_oracle():
     near_max = S.serialize_flat(_extreme(16, 8, 1, 6, [3.4e38, -3.4e38, 3.4e38]), L.make_spec(8, 8, 4096, 127, 2))
     for frame in non_finite_cases() + [near_max]:
         assert np.array_equal(render(frame), O.render_frame(frame))
+
+
+DENSE_CASES = {
+    # (width, height, shapes, seed, tile, threads per tile, max_shape, stack words)
+    "dense_160x120": (160, 120, 220, 91, 32, 32, 255, 4),
+    "dense_96x64_onepixel": (96, 64, 400, 7, 8, 64, 511, 8),
+    "dense_64x48_wide_stack": (64, 48, 600, 5, 8, 64, 1023, 16),
+}
+
+
+@pytest.mark.parametrize("dense_min", [32, 128])
+@pytest.mark.parametrize("case", sorted(DENSE_CASES))
+def test_dense_columns_by_a_warp(case, dense_min):
+    """The warp-cooperative scan of dense columns (gudni_set_dense_columns): canvas-wide
+    random shapes from the batched mix's generator, with hundreds of thresholds and
+    shape bits per column and tens of thousands of sections per pixel, scanned by all
+    32 lanes of a warp with real shuffles, ballots and __syncwarp; the image is the
+    oracle's and the per-lane kernel's, bit for bit."""
+    w, h, n, seed, tile, tpt, max_shape, sections = DENSE_CASES[case]
+    flat = G.random_shapes(seed=seed, width=w, height=h, n_shapes=n)
+    frame = S.serialize_flat(flat, L.make_spec(tile, tpt, 8192, max_shape, sections, max_strands_per_tile=1 << 24))
+    with Rasterizer(frame.spec) as r:
+        lane = r.queue_jobs(frame)
+        r.set_dense_columns(dense_min)
+        warp = r.queue_jobs(frame)
+        again = r.raster_frame(frame)
+    want = O.render_frame(frame)
+    assert np.array_equal(lane, want), f"per-lane: {int((lane != want).sum())} pixels differ"
+    assert np.array_equal(warp, want), f"warp: {int((warp != want).sum())} pixels differ"
+    assert np.array_equal(again, want)
+
+
+def test_dense_columns_on_the_512_golden():
+    """The 512x512 64-shape workload through the warp-cooperative scan matches the
+    image the reference kernels rendered (its digest in the golden index)."""
+    frame = F.build("random_512_cfg")
+    with Rasterizer(frame.spec) as r:
+        r.set_dense_columns(32)
+        got = r.queue_jobs(frame)
+    import hashlib
+    digest = hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest()
+    assert digest == INDEX["random_512_cfg"]["image_sha256"]

@@ -127,3 +127,71 @@ def test_no_alloc_rejects_columns_beyond_its_capacity():
             frame.compute_depth, 0, bg.ctypes.data, out.data_ptr(), None)
     assert rc == -2
     assert "512" in lib.gudni_last_error(None).decode()
+
+
+def test_no_alloc_orders_after_async_copies_on_its_stream():
+    """A caller that writes the records with asynchronous copies on its own
+    non-blocking stream and calls the entry point on that stream gets the image of
+    those records: the call reads nothing from the host before its launch, so the
+    kernel runs after the copies.  A sleep kernel ahead of the copies keeps them in
+    flight when the call is made.  A malformed tile and a misaligned picture use
+    written the same way are found by the kernel and returned as bad input."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    flat = G.glyph_page(seed=21, width=160, height=96, n_glyphs=40, n_shapes=8)
+    spec = L.make_spec(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+                       stack_sections=2)
+    frame = S.serialize_flat(flat, spec)
+    assert len(frame.jobs) == 1 and len(frame.picture_uses)
+    with Rasterizer(frame.spec) as r:
+        want = r.raster_frame(frame)
+    lib = L.load_cuda()
+    fn = _bind(lib)
+    stream = torch.cuda.Stream()  # torch's pool streams are non-blocking
+    job = frame.jobs[0]
+
+    def pinned(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).pin_memory()
+
+    host = {n: pinned(getattr(frame, n)) for n in ("geometry", "substances", "pictures", "picture_uses", "radials")}
+    host["shapes"], host["tiles"] = pinned(job.shapes), pinned(job.tiles)
+    dev = {n: torch.zeros(max(t.numel(), 16), dtype=torch.uint8, device="cuda") for n, t in host.items()}
+    out = torch.zeros(frame.canvas_w * frame.canvas_h, dtype=torch.int32, device="cuda")
+    bg = np.ascontiguousarray(frame.background, np.float32)
+    spec_c = L.Spec(*[getattr(frame.spec, f) for f, _ in L.Spec._fields_])
+    torch.cuda.synchronize()
+
+    def call(tiles_src, uses_src):
+        with torch.cuda.stream(stream):
+            torch.cuda._sleep(50_000_000)  # tens of milliseconds ahead of the copies
+            for n, t in host.items():
+                src = {"tiles": tiles_src, "picture_uses": uses_src}.get(n, t)
+                dev[n][:src.numel()].copy_(src, non_blocking=True)
+            out.fill_(0)
+        return fn(C.byref(spec_c), dev["geometry"].data_ptr(), frame.geometry.size, dev["substances"].data_ptr(),
+                  len(frame.substances), dev["pictures"].data_ptr(), frame.pictures.size,
+                  dev["picture_uses"].data_ptr(), len(frame.picture_uses), dev["radials"].data_ptr(),
+                  len(frame.radials), dev["shapes"].data_ptr(), len(job.shapes), dev["tiles"].data_ptr(),
+                  len(job.tiles), frame.canvas_w, frame.canvas_h, frame.compute_depth, 0, bg.ctypes.data,
+                  out.data_ptr(), C.c_void_p(stream.cuda_stream))
+
+    for _ in range(2):
+        assert call(host["tiles"], host["picture_uses"]) == 0, lib.gudni_last_error(None).decode()
+        stream.synchronize()
+        got = out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w)
+        assert_parity(got, want)
+        assert np.array_equal(got, want)
+
+    bad_tiles = job.tiles.copy()
+    bad_tiles["shape_length"][0] = len(job.shapes) + 5  # past the shape pile
+    assert call(pinned(bad_tiles), host["picture_uses"]) == -1
+    assert "outside" in lib.gudni_last_error(None).decode()
+    bad_uses = frame.picture_uses.copy()
+    bad_uses["mem_offset"] += 2  # not a multiple of 4
+    assert call(host["tiles"], pinned(bad_uses)) == -1
+    stream.synchronize()
+    # and the next good call renders the frame again
+    assert call(host["tiles"], host["picture_uses"]) == 0
+    stream.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32).reshape(frame.canvas_h, frame.canvas_w), want)
