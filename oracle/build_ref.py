@@ -28,7 +28,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
-DEFAULT_REFERENCE = "/root/reference"
+# Where the reference checkout lies: the GUDNI_REFERENCE environment variable, else the
+# build container's checkout (this recipe is the one file that reads it there).
+DEFAULT_REFERENCE = os.environ.get("GUDNI_REFERENCE") or "/root/reference"
 KERNELS_REL = os.path.join("src", "Graphics", "Gudni", "OpenCL", "Kernels.cl")
 SOURCE_PADDING = 40  # sOURCEfILEpADDING, Raster/Constants.hs:70
 

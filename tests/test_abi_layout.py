@@ -189,12 +189,15 @@ def haskell_kind(t):
 
 
 def test_haskell_imports_match_the_header_prototypes():
-    """The foreign imports of the Haskell drop-in module written out for integration
+    """The foreign imports of the Haskell drop-in modules (haskell/Graphics/Gudni/CUDA/)
     take the arguments and return the result the header declares (number, and pointer,
     integer or float of each, with its size)."""
+    import glob
     import re
     protos = header_prototypes()
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sources = sorted(glob.glob(os.path.join(ROOT, "haskell", "**", "*.hs"), recursive=True))
+    assert any(s.endswith(os.path.join("CUDA", "CallKernels.hs")) for s in sources)
+    text = "".join(open(s).read() for s in sources)
     imports = re.findall(r'foreign import ccall (?:safe|unsafe) "(gudni_[a-z0-9_]+)"\s+\w+\s*::\s*(.*?)'
                          r'\bIO\s+(\(\s*\)|\([^)]*\)|\w+)', text, flags=re.S)
     assert len(imports) >= 10
