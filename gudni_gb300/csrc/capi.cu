@@ -145,6 +145,7 @@ struct gudni_ctx {
   DevBuf<int64_t> counters;
   bool counters_on = false;
   int dense_min = 0;  // gudni_set_dense_columns (0: per-lane scan only)
+  bool coop = true;   // gudni_set_cooperative_units
   uint32_t random_mode = gudni::kRandomField;  // gudni_set_random_source
   uint64_t random_seed = 0;
   bool device_strands = false;  // gudni_set_device_strand_table
@@ -370,6 +371,7 @@ int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInf
   a.overflow_cap = (uint32_t)std::min<size_t>(max_items, 0xFFFFFFFFull);
   a.overflow_count = ctx->words.ptr;
   a.dense_min = ctx->dense_min;
+  a.coop = ctx->coop ? 1 : 0;
   a.status = ctx->status.ptr;
   const size_t warps_per_block = gudni::kRasterBlock / 32;
   const int grid = (int)std::min<size_t>((n_units + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
@@ -1252,6 +1254,13 @@ int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds) {
   if (min_thresholds < 0) return fail(ctx, GUDNI_ERR_BAD_INPUT, "min_thresholds must be >= 0");
   if (min_thresholds != ctx->dense_min) drop_graph(ctx);  // a captured launch holds the old setting
   ctx->dense_min = min_thresholds;
+  return GUDNI_OK;
+}
+
+int gudni_set_cooperative_units(gudni_ctx* ctx, int enable) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  if ((enable != 0) != ctx->coop) drop_graph(ctx);  // a captured launch holds the old setting
+  ctx->coop = enable != 0;
   return GUDNI_OK;
 }
 

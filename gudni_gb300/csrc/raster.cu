@@ -37,9 +37,73 @@
 #include "column_kernels.cuh"
 #include "raster_device.cuh"
 #include "raster_kernels.h"
+#include "tile_coop.cuh"
 #include "warp_column.cuh"
 
 namespace gudni {
+
+// The fast pass with warp-cooperative units (tile_coop.cuh): a unit's thresholds are
+// generated by all 32 lanes over (strand, column) pairs and binned to the columns by
+// ballots, the tile's shape records are staged by a bulk copy, each lane sorts and
+// scans its column as in raster_tiles_kernel, and the pixels leave through a
+// shared-memory tile by whole rows.  Units that do not qualify run the per-column code
+// on their lanes.  The image is raster_tiles_kernel's bit for bit.
+template <int SECTIONS>
+__global__ void __launch_bounds__(kRasterBlock) raster_tiles_coop_kernel(TileLaunch a) {
+  __shared__ __align__(16) CoopShared sh[kRasterBlock / 32];
+  const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  CoopShared& cs = sh[threadIdx.x >> 5];
+  const size_t cap = (size_t)a.scratch.capacity;
+  const size_t istride = (size_t)a.scratch.idx_stride;
+  float4* thr = a.scratch.thr + (size_t)slot * cap;
+  uint32_t* hdr = a.scratch.hdr + (size_t)slot * cap;
+  uint32_t* idx = a.scratch.idx + (size_t)slot * istride;
+  float4* thrWarp = thr - (size_t)lane * cap;
+  uint32_t* hdrWarp = hdr - (size_t)lane * cap;
+  uint32_t* idxWarp = idx - (size_t)lane * istride;
+  if (lane == 0) mbarInit(&cs.mbar);
+  __syncwarp();
+  uint32_t phase = 0u;
+  int status = 0;
+  for (;;) {
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(a.next_tile, 1u);
+    k = __shfl_sync(0xffffffffu, k, 0);
+    if (k >= a.n_units) break;
+    int tile, chunk;
+    unitOf(a.units, a.chunk_log2, k, tile, chunk);
+    bool ok;
+    const RasterInputs in = sceneInputs(a.in, a.scenes, a.tile_scene, a.n_scenes, tile, status, ok);
+    if (!ok) continue;
+    const gudni_tile_info ti = in.tiles[tile];
+    if (!tileOk(ti, in.n_shapes) || in.log2_tpt < 0 || in.log2_tpt > kMaxLog2Tpt) {
+      status |= kStatusBadInput;
+      continue;
+    }
+    const int tpt = 1 << in.log2_tpt;
+    const int column = chunk * 32 + lane;
+    const int flags = runUnitCoop(in, ti, chunk, lane, thrWarp, hdrWarp, idxWarp, (int)cap, (int)istride, status,
+                                  cs, phase);
+    bool overflow = (flags & kCoopOverflow) != 0;
+    if (flags & kCoopNotTaken)
+      overflow = column < tpt && runColumn<SECTIONS, false>(in, ti, column, thr, hdr, (int)cap, idx, status);
+    if (overflow) {
+      if (a.overflow_items) {
+        const uint32_t n = atomicAdd(a.overflow_count, 1u);
+        if (n < a.overflow_cap) {
+          a.overflow_items[n] = (k << kLaneBits) | (uint32_t)lane;
+        } else {
+          status |= kStatusOverflow;
+        }
+      } else {
+        status |= kStatusOverflow;
+      }
+    }
+  }
+  bulkStoreDrain();
+  if (status) atomicOr(a.status, status);
+}
 
 template <int SECTIONS>
 __global__ void __launch_bounds__(kRasterBlock) raster_tiles_warp_kernel(TileLaunch a) {
@@ -157,6 +221,8 @@ static cudaError_t launch_s(const TileLaunch& a, bool list, int grid, cudaStream
     raster_list_kernel<S, false><<<grid, kRasterBlock, 0, stream>>>(a);
   } else if (a.dense_min > 0) {
     raster_tiles_warp_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
+  } else if (a.coop) {
+    raster_tiles_coop_kernel<S><<<grid, kRasterBlock, 0, stream>>>(a);
   } else {
     raster_tiles_kernel<S, false><<<grid, kRasterBlock, 0, stream>>>(a);
   }

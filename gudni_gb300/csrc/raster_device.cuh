@@ -350,14 +350,20 @@ __device__ __forceinline__ float intersectCurve(Trav t, int& status) {
   return (((t.right.y - t.left.y) / (t.right.x - t.left.x)) * (t.xPos - t.left.x)) + t.left.y;
 }
 
-struct GenState {
-  Queue* q;
+// Where generated thresholds go: a column's Queue, or (the cooperative generation of a
+// tile, tile_coop.cuh) the few thresholds of one strand in one column.  Any sink with
+// push(header, threshold).
+template <class Sink>
+struct GenStateOf {
+  Sink* q;
   const ColumnState* c;
 };
+using GenState = GenStateOf<Queue>;
 
 // addLineSegment / addThreshold K:1155-1220 (lineToThreshold/lineToHeader K:1131-1150,
 // trimThresholdTop K:982-1005), inserting into sorted position.
-__device__ __forceinline__ void addLineSegment(GenState& g, float2 left, float2 right, uint32_t shapeBit,
+template <class G>
+__device__ __forceinline__ void addLineSegment(G& g, float2 left, float2 right, uint32_t shapeBit,
                                                bool& added, bool& enclosed) {
   float4 t = make_float4(cl_fmin(left.y, right.y), cl_fmax(left.y, right.y), left.x, right.x);
   bool positive = left.y <= right.y;
@@ -388,7 +394,8 @@ __device__ __forceinline__ void addLineSegment(GenState& g, float2 left, float2 
 // the column, so every line it spawns ends above the column top and only the
 // enclosure flag (set by any persistent line, whatever its y) can change; the border
 // intercepts are then not computed (any value above the column gives the same flags).
-__device__ __forceinline__ void spawnThresholds(GenState& g, uint32_t shapeBit, Trav& l, Trav& r, bool& added,
+template <class G>
+__device__ __forceinline__ void spawnThresholds(G& g, uint32_t shapeBit, Trav& l, Trav& r, bool& added,
                                                 bool& enclosed, int& status, bool above = false) {
   float yL = (l.left.x >= kLeft) ? l.left.y : (above ? -1.0f : intersectCurve(l, status));
   bool leftWing = false;
@@ -427,7 +434,8 @@ __device__ __forceinline__ void searchTree(Trav& t, const float4* tree, int tree
 }
 
 // traverseTree K:1378-1408 + spawnThresholds for one strand of `size` 8-byte units.
-__device__ __forceinline__ void strandThresholds(GenState& g, const uint8_t* strand, uint32_t size, float2 d,
+template <class G>
+__device__ __forceinline__ void strandThresholds(G& g, const uint8_t* strand, uint32_t size, float2 d,
                                                  uint32_t shapeBit, bool& added, bool& enclosedByStrand,
                                                  int& status, bool above = false) {
   const int treeSize = ((int)size - 4) / 2;
@@ -1039,12 +1047,14 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 // K:1826-1851, sectionColor K:1724-1742, writePixelGlobal K:1853-1862).
 // `image` (optional): instead of the BGRA word, write each pixel's colour before the
 // byte conversion and its section-area sum as a float4 (the adjoint's forward pass).
+// `stage` (optional): write the BGRA word of the column's row r to stage[32 * r]
+// instead of the output (the cooperative unit's shared-memory tile).
 // kCounterJitter: take the stochastic jitter from counterRandom (kRandomCounter) in
 // place of the random field; the default instantiation is the reference's scan.
 template <int SECTIONS, bool kCounterJitter = false>
 __device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
                                              ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
-                                             int shapeBits, float4* image = nullptr) {
+                                             int shapeBits, float4* image = nullptr, uint32_t* stage = nullptr) {
   Parse p;
   p.current = 0;
   p.numActive = 0;
@@ -1073,11 +1083,16 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
   WordCache words;
   words.clear();
   const bool oneWord = shapeBits <= 64;
-  for (p.pixelY = 1.0f; p.pixelY <= c.floatHeight; p.pixelY += 1.0f) {
-    if (colorPositional) colorOk = false;
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
-    int guard = 0;
-    while ((p.sEndX < kRight) || (p.sEndY < p.pixelY)) {
+  // The reference's two loops -- pixel rows (renderThresholdArray) and the sections of
+  // a row (calculatePixel) -- run as one loop whose step is either the next section of
+  // the row or, once the row is complete, its pixel.  Per column the operations and
+  // their order are the reference's; across the lanes of a warp a lane whose row is
+  // short goes on to its next row instead of waiting for the warp's longest row.
+  p.pixelY = 1.0f;
+  float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc4 = 0.0f;
+  int guard = 0;
+  while (p.pixelY <= c.floatHeight) {
+    if ((p.sEndX < kRight) || (p.sEndY < p.pixelY)) {
       if (++guard > kSectionCap) {
         status |= kStatusIterLimit;
         return;
@@ -1127,17 +1142,26 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
       if (p.current < p.numActive) stack.pass(q.getH(p.current));
       p.current += 1;
       ++sections;
-    }
-    const float r = acc0 / acc4, g = acc1 / acc4, b = acc2 / acc4;
-    if (image) {
-      image[(size_t)py * (size_t)in.bitmap_w + (size_t)px] = make_float4(r, g, b, acc4);
     } else {
-      *outp = toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
-      outp += in.bitmap_w;
+      // the row is complete: its pixel (writePixelGlobal K:1853-1862), then the next row
+      const float r = acc0 / acc4, g = acc1 / acc4, b = acc2 / acc4;
+      if (image) {
+        image[(size_t)py * (size_t)in.bitmap_w + (size_t)px] = make_float4(r, g, b, acc4);
+      } else if (stage) {
+        stage[32 * (py - c.deltaY)] =
+            toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
+      } else {
+        *outp = toByte(b * 255.0f) | (toByte(g * 255.0f) << 8) | (toByte(r * 255.0f) << 16) | (255u << 24);
+        outp += in.bitmap_w;
+      }
+      p.sStartX = kLeft;
+      p.sStartY = p.pixelY;
+      py += 1;
+      p.pixelY += 1.0f;
+      acc0 = acc1 = acc2 = acc4 = 0.0f;
+      guard = 0;
+      if (colorPositional) colorOk = false;
     }
-    p.sStartX = kLeft;
-    p.sStartY = p.pixelY;
-    py += 1;
   }
   if (in.counters) {
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[0]), (unsigned long long)sections);

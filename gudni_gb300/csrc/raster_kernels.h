@@ -46,6 +46,7 @@ struct TileLaunch {
   uint32_t* overflow_count;
   int dense_min;                // > 0: columns with at least this many thresholds are
                                 // scanned by the whole warp (raster_tiles_warp_kernel)
+  int coop;                     // != 0: warp-cooperative units (raster_tiles_coop_kernel)
   // full-capacity pass
   const uint32_t* list;         // overflowed columns
   const uint32_t* list_count;   // their number (device)

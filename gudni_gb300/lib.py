@@ -215,6 +215,8 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_read_counters.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.gudni_set_dense_columns.restype = C.c_int
     lib.gudni_set_dense_columns.argtypes = [vp, i32]
+    lib.gudni_set_cooperative_units.restype = C.c_int
+    lib.gudni_set_cooperative_units.argtypes = [vp, C.c_int]
     lib.gudni_launch_count.restype = C.c_uint64
     lib.gudni_launch_count.argtypes = [vp]
     lib.gudni_adjoint_tiles_device.restype = C.c_int

@@ -201,6 +201,11 @@ class Rasterizer:
         The image does not change."""
         self._check(self.lib.gudni_set_dense_columns(self.ctx, int(min_thresholds)))
 
+    def set_cooperative_units(self, on: bool = True) -> None:
+        """Warp-cooperative generation of each work unit (gudni_set_cooperative_units,
+        on by default); off runs every column's generation on its own lane."""
+        self._check(self.lib.gudni_set_cooperative_units(self.ctx, 1 if on else 0))
+
     def read_counters(self) -> dict:
         c = (C.c_int64 * 4)()
         self._check(self.lib.gudni_read_counters(self.ctx, c))

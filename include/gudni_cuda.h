@@ -342,8 +342,22 @@ int gudni_set_random_source(gudni_ctx* ctx, int source, uint64_t seed);
  * lanes of its warp together (sections dealt to the lanes, pixel sums taken in section
  * order), instead of by its own lane.  The output is the same bit for bit; the choice
  * is one of speed.  0 (the default) keeps every column on its own lane.  No
- * counterpart in the reference.  Not yet timed on a GPU. */
+ * counterpart in the reference. */
 int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds);
+
+/* Warp-cooperative work units (on by default): the 32 lanes of a warp generate a
+ * unit's thresholds together -- strands dealt to the lanes, their (strand, column)
+ * pairs dealt again, the thresholds binned to the columns by warp ballots in the
+ * order the per-column generation pushes them -- with the tile's shape records staged
+ * in shared memory by a bulk copy and the pixels written out by rows from a shared
+ * tile; each column is then sorted and scanned by its own lane.  Units of tiles with
+ * more than 64 shapes or more shapes than max_shape run the per-column generation.
+ * Replaces the per-column generation of generateThresholds (Kernels.cl:2030-2082,
+ * buildThresholdArray K:1540-1595); the output is the same bit for bit.  0 runs every
+ * unit through the per-column generation.  Not used by the warp-cooperative dense
+ * scan (gudni_set_dense_columns), by the counter-based jitter, or by
+ * gudni_raster_job_noalloc. */
+int gudni_set_cooperative_units(gudni_ctx* ctx, int enable);
 
 /* ------------------------------------------------------------------ adjoint */
 

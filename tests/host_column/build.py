@@ -9,7 +9,7 @@ SRC = os.path.join(HERE, "host_column.cpp")
 OUT = os.path.join(HERE, "_build", "libhost_column.so")
 DEPS = [SRC, os.path.join(HERE, "warp_emu.h")] + [
     os.path.join(ROOT, "gudni_gb300", "csrc", f)
-    for f in ("raster_device.cuh", "adjoint_device.cuh", "strand_table.h", "warp_column.cuh")] + [
+    for f in ("raster_device.cuh", "adjoint_device.cuh", "strand_table.h", "warp_column.cuh", "tile_coop.cuh")] + [
     os.path.join(ROOT, "include", "gudni_cuda.h")]
 CUDA_INCLUDE = "/usr/local/cuda/include"
 
@@ -35,6 +35,10 @@ def load():
     lib.host_column_raster_job_warp.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i,
                                                 vp, vp, C.c_float, i, i, i, i, C.c_uint64, vp,
                                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.host_column_raster_job_coop.restype = C.c_int
+    lib.host_column_raster_job_coop.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i,
+                                                vp, vp, C.c_float, i, i, i, C.c_uint64, vp, C.POINTER(C.c_int),
+                                                C.POINTER(C.c_int)]
     lib.host_warp_trace.restype = None
     lib.host_warp_trace.argtypes = [C.POINTER(C.c_longlong)]
     lib.host_set_random_source.restype = None

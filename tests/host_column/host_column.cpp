@@ -72,6 +72,30 @@ static inline int __shfl_xor_sync(unsigned, int v, int mask) {
   return (int)warp_emu::collective(warp_emu::kShflXor, (unsigned)v, mask);
 }
 static inline int __ffs(int x) { return __builtin_ffs(x); }
+static inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+static inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
+static inline unsigned __match_any_sync(unsigned, unsigned v) {
+  return warp_emu::collective(warp_emu::kMatch, v, 0);
+}
+static inline bool __all_sync(unsigned, int pred) {
+  return warp_emu::collective(warp_emu::kBallot, pred ? 1u : 0u, 0) == 0xffffffffu;
+}
+static inline bool __any_sync(unsigned, int pred) {
+  return warp_emu::collective(warp_emu::kBallot, pred ? 1u : 0u, 0) != 0u;
+}
+static inline unsigned __shfl_up_sync(unsigned, unsigned v, unsigned delta) {
+  return warp_emu::collective(warp_emu::kShflUp, v, (int)delta);
+}
+static inline unsigned long long atomicOr(unsigned long long* p, unsigned long long v) {
+  const unsigned long long o = *p;
+  *p = o | v;
+  return o;
+}
+static inline unsigned long long atomicXor(unsigned long long* p, unsigned long long v) {
+  const unsigned long long o = *p;
+  *p = o ^ v;
+  return o;
+}
 static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 // shared-memory atomics: lanes run one at a time between collectives
 static inline unsigned atomicXor(unsigned* p, unsigned v) {
@@ -84,6 +108,7 @@ static inline unsigned atomicXor(unsigned* p, unsigned v) {
 #include "../../gudni_gb300/csrc/adjoint_device.cuh"
 #include "../../gudni_gb300/csrc/strand_table.h"
 #include "../../gudni_gb300/csrc/warp_column.cuh"
+#include "../../gudni_gb300/csrc/tile_coop.cuh"
 
 namespace {
 
@@ -152,6 +177,61 @@ int run_all_warp(const gudni::RasterInputs& in, const gudni_tile_info* tiles, in
       }
     }
   }
+  return status;
+}
+
+// The warp-cooperative units (tile_coop.cuh): every work unit on an emulated warp,
+// the lanes resuming in a seeded random order at each collective; units that do not
+// qualify run the per-column code on their lanes, and columns that overflow the
+// working capacity `cap` are re-run by the per-column code with `full_cap`, as the
+// kernel and the full-capacity pass do.  *taken counts the units run cooperatively.
+template <int SECTIONS>
+int run_all_coop(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_tiles, int tpt, int cap,
+                 int full_cap, uint64_t seed, int* overflow, int* taken) {
+  const size_t idxStride = (size_t)in.max_shape + 1;
+  std::vector<float4> thr(32 * (size_t)cap, make_float4(-7.0f, -7.0f, -7.0f, -7.0f)), big((size_t)full_cap);
+  std::vector<uint32_t> hdr(32 * (size_t)cap, 0xDEADBEEFu), bigH((size_t)full_cap);
+  std::vector<uint32_t> idx(32 * idxStride);
+  gudni::CoopShared* sh = new gudni::CoopShared;
+  std::memset(sh, 0x5A, sizeof(*sh));
+  int status = 0;
+  for (int t = 0; t < n_tiles; ++t) {
+    for (int chunk = 0; chunk * 32 < tpt; ++chunk) {
+      int flags[32] = {0};
+      int laneStatus[32] = {0};
+      uint32_t phases[32] = {0};
+      const std::function<void(int)> body = [&](int lane) {
+        int st = 0;
+        flags[lane] = gudni::runUnitCoop(in, tiles[t], chunk, lane, thr.data(), hdr.data(), idx.data(), cap,
+                                         (int)idxStride, st, *sh, phases[lane]);
+        laneStatus[lane] = st;
+      };
+      if (!warp_emu::run(body, seed * 1000003ull + (uint64_t)t * 64u + (uint64_t)chunk)) {
+        delete sh;
+        return -100;
+      }
+      if (!(flags[0] & gudni::kCoopNotTaken)) *taken += 1;
+      for (int lane = 0; lane < 32; ++lane) {
+        status |= laneStatus[lane];
+        const int column = chunk * 32 + lane;
+        if (column >= tpt) continue;
+        if (flags[lane] & gudni::kCoopNotTaken) {
+          if (gudni::runColumn<SECTIONS>(in, tiles[t], column, thr.data() + (size_t)lane * cap,
+                                         hdr.data() + (size_t)lane * cap, cap, idx.data() + (size_t)lane * idxStride,
+                                         status)) {
+            if (gudni::runColumn<SECTIONS>(in, tiles[t], column, big.data(), bigH.data(), full_cap, idx.data(),
+                                           status))
+              *overflow = 1;
+          }
+        } else if (flags[lane] & gudni::kCoopOverflow) {
+          if (gudni::runColumn<SECTIONS>(in, tiles[t], column, big.data(), bigH.data(), full_cap, idx.data(),
+                                         status))
+            *overflow = 1;
+        }
+      }
+    }
+  }
+  delete sh;
   return status;
 }
 
@@ -415,4 +495,36 @@ extern "C" void host_warp_trace(long long out[gudni::kTraceEvents]) {
 extern "C" void host_set_random_source(int mode, uint64_t seed) {
   g_random_mode = mode == 1 ? gudni::kRandomCounter : gudni::kRandomField;
   g_random_seed = seed;
+}
+
+// One job through the warp-cooperative units on the host (see run_all_coop).
+extern "C" int host_column_raster_job_coop(const uint8_t* geometry, size_t geometry_bytes, const float* substances,
+                                           size_t n_substances, const uint8_t* pictures, size_t picture_bytes,
+                                           const gudni_picture_use* uses, size_t n_uses, const gudni_radial* radials,
+                                           size_t n_radials, const gudni_shape* shapes, size_t n_shapes,
+                                           const gudni_tile_info* tiles, int n_tiles, int compute_depth,
+                                           int bitmap_w, int bitmap_h, int job_index, const float* background,
+                                           const float* random_field, float stochastic, int capacity,
+                                           int max_thresholds, int max_shape, uint64_t seed, uint32_t* out,
+                                           int* overflow, int* taken) {
+  HostTables t;
+  gudni::RasterInputs in = host_inputs(t, geometry, geometry_bytes, substances, n_substances, pictures,
+                                       picture_bytes, uses, n_uses, radials, n_radials, shapes, n_shapes, tiles,
+                                       n_tiles, compute_depth, bitmap_w, bitmap_h, job_index, background, max_shape,
+                                       out);
+  in.random_field = random_field;
+  in.stochastic = stochastic;
+  in.random_mode = gudni::kRandomField;
+  *overflow = 0;
+  *taken = 0;
+  const int tpt = 1 << compute_depth;
+  switch (stack_words(max_shape)) {
+    case 1: return run_all_coop<1>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    case 2: return run_all_coop<2>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    case 4: return run_all_coop<4>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    case 8: return run_all_coop<8>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    case 16: return run_all_coop<16>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    case 32: return run_all_coop<32>(in, tiles, n_tiles, tpt, capacity, max_thresholds, seed, overflow, taken);
+    default: return -1;
+  }
 }

@@ -24,7 +24,7 @@
 
 namespace warp_emu {
 
-enum Kind { kSync = 1, kShfl = 2, kShflUp = 3, kBallot = 4, kShflXor = 5 };
+enum Kind { kSync = 1, kShfl = 2, kShflUp = 3, kBallot = 4, kShflXor = 5, kMatch = 6 };
 
 struct Warp {
   ucontext_t sched;
@@ -128,6 +128,13 @@ inline bool run(const std::function<void(int)>& body, uint64_t seed) {
         case kShflUp: w.result[l] = l - w.arg[l] >= 0 ? w.value[l - w.arg[l]] : w.value[l]; break;
         case kBallot: w.result[l] = ballot; break;
         case kShflXor: w.result[l] = w.value[(l ^ w.arg[l]) & 31]; break;
+        case kMatch: {
+          uint32_t m = 0;
+          for (int o = 0; o < 32; ++o)
+            if (w.value[o] == w.value[l]) m |= 1u << o;
+          w.result[l] = m;
+          break;
+        }
         default: w.result[l] = 0; break;
       }
     }

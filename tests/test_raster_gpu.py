@@ -334,3 +334,57 @@ def test_dense_columns_on_the_512_golden():
     import hashlib
     digest = hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest()
     assert digest == INDEX["random_512_cfg"]["image_sha256"]
+
+
+COOP_CASES = {
+    # name: (builder, spec)
+    "glyph_page_32x32": (lambda: G.glyph_page(seed=4, width=480, height=270, n_glyphs=150, n_shapes=25),
+                         dict(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+                              stack_sections=8)),
+    "split_leaves": (lambda: G.glyph_page(seed=7, width=200, height=120, n_glyphs=90, n_shapes=10),
+                     dict(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+                          stack_sections=8, max_strands_per_tile=60)),
+    "random_16x64": (lambda: G.random_shapes(seed=5, width=150, height=110, n_shapes=30),
+                     dict(max_tile_size=16, threads_per_tile=64, max_thresholds=4096, max_shape=127,
+                          stack_sections=8)),
+    "random_32x256": (lambda: G.random_shapes(seed=6, width=160, height=96, n_shapes=40),
+                      dict(max_tile_size=32, threads_per_tile=256, max_thresholds=4096, max_shape=127,
+                           stack_sections=8)),
+    "dense_one_word": (lambda: G.random_shapes(seed=13, width=96, height=80, n_shapes=60),
+                       dict(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=127,
+                            stack_sections=8)),
+    "beyond_64_shapes": (lambda: G.random_shapes(seed=9, width=96, height=64, n_shapes=90, seg_lo=4, seg_hi=8),
+                         dict(max_tile_size=32, threads_per_tile=32, max_thresholds=8192, max_shape=255,
+                              stack_sections=4)),
+}
+
+
+@pytest.mark.parametrize("case", sorted(COOP_CASES))
+def test_cooperative_units_match_per_column_generation(case):
+    """The warp-cooperative units (gudni_set_cooperative_units, the default): strands
+    and (strand, column) pairs dealt to the lanes, thresholds binned by ballots and
+    match masks, shape records staged by a bulk copy, pixels stored by rows from a
+    shared tile.  The image is the per-column kernel's and the oracle's bit for bit,
+    through the frame entry point and through a job at a time, twice in a row on one
+    context (the shared tile and the barrier phase carry over)."""
+    build, spec = COOP_CASES[case]
+    frame = S.serialize_flat(build(), L.make_spec(**spec))
+    want = O.render_frame(frame)
+    with Rasterizer(frame.spec) as r:
+        r.set_cooperative_units(False)
+        per_column = r.raster_frame(frame)
+        r.set_cooperative_units(True)
+        coop = [r.raster_frame(frame), r.queue_jobs(frame), r.raster_frame(frame)]
+    assert np.array_equal(per_column, want), f"per-column: {int((per_column != want).sum())} pixels differ"
+    for got in coop:
+        assert np.array_equal(got, want), f"cooperative: {int((got != want).sum())} pixels differ"
+
+
+def test_cooperative_units_overflow_to_the_full_pass(monkeypatch):
+    """A small working capacity sends long columns of cooperative units to the
+    full-capacity pass; the image does not change."""
+    monkeypatch.setenv("GUDNI_WORKING_CAPACITY", "24")
+    frame = F.build("random_128x96")
+    want = np.load(os.path.join(GOLDEN, INDEX["random_128x96"]["image_file"]))
+    with Rasterizer(frame.spec) as r:
+        assert np.array_equal(r.raster_frame(frame), want)
