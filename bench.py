@@ -67,6 +67,13 @@ def parse():
     ap.add_argument("--device-strand-table", action="store_true",
                     help="uploads build the strand table on the device (gudni_set_device_strand_table)")
     ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--plain-untimed-pass", type=int, default=1,
+                    help="batch256: one untimed pass of the per-scene path before timing it")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="page4k: leave out the batched, fwd+adjoint and fitting sub-records")
+    ap.add_argument("--form-dense-columns", type=int, default=32,
+                    help="page4k sub-records: the batched form's warp-cooperative dense columns threshold")
+    ap.add_argument("--fit-steps", type=int, default=5, help="page4k sub-records: timed fitting steps")
     ap.add_argument("--tile", type=int, default=None, help="tile size (default: the workload's)")
     ap.add_argument("--threads-per-tile", type=int, default=None, help="threads per tile (default: the workload's)")
     return ap.parse_args()
@@ -318,11 +325,12 @@ BATCH_MAX_THRESHOLDS = 32768
 BATCH_STRANDS_PER_TILE = 1 << 24  # no strand-count tile splitting
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     """The batched form: 256 scenes (sides log-uniform 64-1024 px, 10-2000 random shapes
     of 8-32 segments) in one persistent launch replayed from a CUDA graph, tile size and
     threads per tile per canvas-size bucket from the autotuner; against one launch pair
-    per scene over the same resident piles."""
+    per scene over the same resident piles.  Returns the result line (printed when
+    `emit`)."""
     import torch
     from gudni_gb300 import autotune as A
     from gudni_gb300 import batch as B
@@ -334,7 +342,7 @@ def run_batch(args):
     t_gen = time.perf_counter() - t0
     t0 = time.perf_counter()
     choice = A.autotune(flats, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE, samples=1, reps=2,
-                        log=lambda m: print(m, file=sys.stderr, flush=True))
+                        log=lambda m: print(m, file=sys.stderr, flush=True), dense_columns=args.dense_columns)
     t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     frames = A.serialize_tuned(flats, choice, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
@@ -376,9 +384,11 @@ def run_batch(args):
     r.sync_status()
     launches = r.launch_count() - launches0
     log(f"batched: {bt} ms")
-    # the plain path: one launch pair per scene, each timed on its own (after one
-    # untimed pass over every scene), summed
-    r.render_each_scene(stream=h)
+    # the plain path: one launch pair per scene, each timed on its own, summed (after
+    # one untimed pass over every scene, unless the batched warm-up already ran the
+    # kernels: --plain-untimed-pass 0)
+    if args.plain_untimed_pass:
+        r.render_each_scene(stream=h)
     r.sync_status()
     per_scene = []
     for i, (first, count) in enumerate(batch.frame_tiles):
@@ -420,9 +430,10 @@ def run_batch(args):
             "batched_over_plain": plain_ms / batched_ms,
             "gpu_launches": int(launches), "clocks": clocks.summary(), "parity_vs_oracle": parity,
             "host_s": {"generate": t_gen, "autotune": t_tune, "serialize": t_ser}}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     r.close()
-    return 0
+    return line
 
 
 ADJ_SPEC = dict(max_tile_size=32, threads_per_tile=32, max_thresholds=4096, max_shape=511, stack_sections=8,
@@ -440,7 +451,7 @@ def adjoint_scene(jitter_px: float = 0.0):
     return flat
 
 
-def run_adjoint(args):
+def run_adjoint(args, emit=True):
     """The differentiable form: forward raster vs one fwd+adjoint launch on the same
     frame; gradients checked against the FP64 reference adjoint and against central
     differences (h = 1e-2 px) of the loss on the largest point-gradient entries."""
@@ -541,9 +552,10 @@ def run_adjoint(args):
                        "data": "synthetic, seeded"},
             "forward_ms": fwd_ms, "fwd_adjoint_ms": adj_ms, "fwd_adjoint_over_forward": adj_ms / fwd_ms,
             "gpu_launches": int(launches), "clocks": clocks.summary(), "gradient_check": check}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     r.close()
-    return 0
+    return line
 
 
 def run_scene(args):
@@ -653,7 +665,7 @@ def fit_scenes(n=64, side=256, shapes=128, jitter_px=0.0, color_sigma=0.0, seed=
     return out
 
 
-def run_fit(args):
+def run_fit(args, emit=True):
     """Batched fitting: 64 independent 256x256 scenes of 128 shapes fitted by Adam (lr
     0.5 px on points, 0.01 on colours) to targets rendered from perturbed copies
     (points N(0, 4 px), colours N(0, 0.1)); each step serializes the scenes, runs every
@@ -701,9 +713,68 @@ def run_fit(args):
             "loss": {"first_timed": first, "final": final, "per_pixel_l2_first": first / (pixels * 3),
                      "per_pixel_l2_final": final / (pixels * 3)},
             "seconds": {k: v for k, v in fit.timings.items()}}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     fit.close()
-    return 0
+    return line
+
+
+def form_records(args) -> dict:
+    """The three systems forms beside the plain page, each run briefly (timed repeats
+    stated in each record), as sub-records of the page's line: the batched form on the
+    256-scene mix against the per-scene path over the same resident piles, fwd+adjoint
+    against forward on the 1024x1024 scene with gradients checked against the FP64
+    reference, and a few steps of the batched fitting.  A form that fails records its
+    error instead."""
+    import copy
+    out = {}
+
+    def guarded(name, fn):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:  # noqa: BLE001
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        out[name]["wall_s"] = time.perf_counter() - t0
+
+    def batched():
+        b = copy.copy(args)
+        b.steps, b.warmup, b.scenes, b.plain_untimed_pass = 1, 1, 256, 0
+        b.dense_columns = args.form_dense_columns
+        ln = run_batch(b, emit=False)
+        keys = ("metric", "value", "unit", "ms_per_step", "mpixels_per_s", "plain_per_scene", "batched_over_plain",
+                "parity_vs_oracle", "gpu_launches", "clocks", "host_s")
+        rec = {k: ln[k] for k in keys}
+        rec.update(steps=1, warmup=1, timing="one batched pass timed after one warm-up pass (the graph is captured "
+                   "in the warm-up); the per-scene path: every scene's launch pair timed alone, summed",
+                   autotune=ln["config"]["autotune"], dense_columns=b.dense_columns,
+                   scenes=ln["config"]["scenes"], pixels=ln["config"]["pixels"])
+        return rec
+
+    def adjoint():
+        a = copy.copy(args)
+        a.steps, a.warmup, a.tile, a.threads_per_tile = 3, 3, None, None
+        ln = run_adjoint(a, emit=False)
+        keys = ("metric", "value", "unit", "forward_ms", "fwd_adjoint_ms", "fwd_adjoint_over_forward",
+                "gradient_check", "gpu_launches", "clocks")
+        rec = {k: ln[k] for k in keys}
+        rec.update(steps=3, warmup=3, timing="median of 3 timed launches of each", config=ln["config"])
+        return rec
+
+    def fitting():
+        f = copy.copy(args)
+        f.steps, f.warmup = args.fit_steps, 1
+        ln = run_fit(f, emit=False)
+        keys = ("metric", "value", "unit", "ms_per_step", "loss", "steps_total", "seconds")
+        rec = {k: ln[k] for k in keys}
+        rec.update(steps=f.steps, warmup=1, note="a short run of --workload fit64 (the same step); the full "
+                   "2000-step fit is --workload fit64 --steps 2000")
+        return rec
+
+    guarded("batched", batched)
+    guarded("adjoint", adjoint)
+    guarded("fit", fitting)
+    return out
 
 
 def main():
@@ -711,11 +782,14 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch256":
-        return run_batch(args)
+        run_batch(args)
+        return 0
     if args.workload == "adjoint1024":
-        return run_adjoint(args)
+        run_adjoint(args)
+        return 0
     if args.workload == "fit64":
-        return run_fit(args)
+        run_fit(args)
+        return 0
     if args.workload == "scene4k":
         return run_scene(args)
 
@@ -869,8 +943,10 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
         line["parity_vs_oracle"] = lsb_parity(gpu_img, img)
         line["parity_reference_vs_oracle"] = ref_parity
-    print(json.dumps(line))
     r.close()
+    if world == 1 and args.workload == "page4k" and not args.no_forms:
+        line.update(form_records(args))
+    print(json.dumps(line))
     return 0
 
 

@@ -44,17 +44,21 @@ def scene_cost(f: S.FlatScene) -> float:
 
 def autotune(flats: Sequence[S.FlatScene], max_shape: int, max_thresholds: int, strands_per_tile: int,
              samples: int = 2, reps: int = 3, candidates=CANDIDATES, device: int = 0,
-             log=None) -> Dict[int, Tuple[int, int]]:
+             log=None, dense_columns: int = 0) -> Dict[int, Tuple[int, int]]:
     """Return {bucket: (tile, threads_per_tile)}.  Each candidate renders the bucket's
     sample scenes (its median and, with samples > 1, its most expensive scene by
     scene_cost) as one batch; the fastest mean over `reps` replays wins.  A candidate
-    whose first render is over three times the best so far is not replayed."""
+    whose first render is over three times the best so far is not replayed.  The
+    candidates are timed with the warp-cooperative dense-column threshold the batch
+    will render with (`dense_columns`, gudni_set_dense_columns)."""
     by_bucket: Dict[int, List[S.FlatScene]] = {}
     for f in flats:
         by_bucket.setdefault(bucket_of(f.canvas_w, f.canvas_h), []).append(f)
     choice: Dict[int, Tuple[int, int]] = {}
     base = spec_for(32, 32, max_shape, max_thresholds, strands_per_tile)
     with B.BatchRasterizer(base, device) as r:
+        if dense_columns:
+            r.set_dense_columns(dense_columns)
         for b, members in sorted(by_bucket.items()):
             ranked = sorted(members, key=scene_cost)
             picks = [ranked[len(ranked) // 2]] + ([ranked[-1]] if samples > 1 and len(ranked) > 1 else [])

@@ -706,10 +706,18 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
     }
     chainArea = 0.0f;
   };
-  for (float pixelY = 1.0f; pixelY <= c.floatHeight; pixelY += 1.0f) {
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, area = 0.0f;
+  // The rows and the sections of a row run as one loop (as in the forward scan,
+  // renderColumnT): a step is the next section of the row or, once the row is
+  // complete, its pixel's end and the next row's start.  Per column the operations
+  // and their order are unchanged; across a warp, a lane whose row is short goes on to
+  // its next row instead of waiting for the longest row.
+  float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, area = 0.0f;
+  size_t pix = 0;
+  int guard = 0;
+  auto rowStart = [&]() {
+    acc0 = acc1 = acc2 = area = 0.0f;
     if (colorPositional) colorOk = false;
-    const size_t pix = (size_t)py * (size_t)in.bitmap_w + (size_t)px;
+    pix = (size_t)py * (size_t)in.bitmap_w + (size_t)px;
     if (grad) {
       const float4 im = image[pix], tg = target[pix];
       I[0] = im.x;
@@ -720,8 +728,12 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       gI[1] = 2.0f * (im.y - tg.y);
       gI[2] = 2.0f * (im.z - tg.z);
     }
-    int guard = 0;
-    while ((sx1 < kRight) || (sy1 < pixelY)) {
+    guard = 0;
+  };
+  float pixelY = 1.0f;
+  if (pixelY <= c.floatHeight) rowStart();
+  while (pixelY <= c.floatHeight) {
+    if ((sx1 < kRight) || (sy1 < pixelY)) {
       if (++guard > kSectionCap) {
         status |= kStatusIterLimit;
         return;
@@ -867,19 +879,22 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       }
       if (current < numActive) stack.pass(q.hdr[q.start + current]);
       current += 1;
+    } else {
+      flushChain();  // dL/dI changes with the pixel
+      if (grad) {  // the row's last band
+        addY(s.lineGrad, srcY0, gY0);
+        addY(s.lineGrad, srcY1, gY1);
+        gY0 = gY1 = 0.0f;
+      }
+      if (!grad) image[pix] = make_float4(acc0 / area, acc1 / area, acc2 / area, area);
+      sx0 = kLeft;
+      srcX0 = kConst;
+      sy0 = pixelY;
+      srcY0 = kConst;
+      py += 1;
+      pixelY += 1.0f;
+      if (pixelY <= c.floatHeight) rowStart();
     }
-    flushChain();  // dL/dI changes with the pixel
-    if (grad) {  // the row's last band
-      addY(s.lineGrad, srcY0, gY0);
-      addY(s.lineGrad, srcY1, gY1);
-      gY0 = gY1 = 0.0f;
-    }
-    if (!grad) image[pix] = make_float4(acc0 / area, acc1 / area, acc2 / area, area);
-    sx0 = kLeft;
-    srcX0 = kConst;
-    sy0 = pixelY;
-    srcY0 = kConst;
-    py += 1;
   }
 }
 

@@ -61,7 +61,6 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_coop_kernel(TileLau
   uint32_t* idx = a.scratch.idx + (size_t)slot * istride;
   float4* thrWarp = thr - (size_t)lane * cap;
   uint32_t* hdrWarp = hdr - (size_t)lane * cap;
-  uint32_t* idxWarp = idx - (size_t)lane * istride;
   if (lane == 0) mbarInit(&cs.mbar);
   __syncwarp();
   uint32_t phase = 0u;
@@ -83,8 +82,7 @@ __global__ void __launch_bounds__(kRasterBlock) raster_tiles_coop_kernel(TileLau
     }
     const int tpt = 1 << in.log2_tpt;
     const int column = chunk * 32 + lane;
-    const int flags = runUnitCoop(in, ti, chunk, lane, thrWarp, hdrWarp, idxWarp, (int)cap, (int)istride, status,
-                                  cs, phase);
+    const int flags = runUnitCoop(in, ti, chunk, lane, thrWarp, hdrWarp, (int)cap, status, cs, phase);
     bool overflow = (flags & kCoopOverflow) != 0;
     if (flags & kCoopNotTaken)
       overflow = column < tpt && runColumn<SECTIONS, false>(in, ti, column, thr, hdr, (int)cap, idx, status);

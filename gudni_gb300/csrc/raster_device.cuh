@@ -721,9 +721,23 @@ __device__ __forceinline__ bool lastIsSetFor(uint64_t comp) {
 // `stopBit` receives the lowest bit position the walk read: the colour is a function
 // of the stack bits at and above it only (below it the walk had reached an opaque
 // composite and stopped), or of every bit (-1) when it reached the background.
-template <int SECTIONS>
-__device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
-                                                 const uint32_t* shapeIdx, int px, int py, int& status,
+// How the colour walk finds the tag of a shape bit: through the column's table of
+// shape indices (bit -> index into the job's shape pile, the per-column generation's
+// numbering), or directly when the bits are the tile's own shape numbers (the
+// warp-cooperative unit, whose tile records are staged in shared memory).
+struct IndexedTags {
+  const uint32_t* idx;
+  const gudni_shape* shapes;
+  __device__ __forceinline__ uint64_t tag(int bit) const { return shapes[idx[bit]].tag; }
+};
+struct DirectTags {
+  const gudni_shape* shapes;  // the tile's shape records: bit n is record n
+  __device__ __forceinline__ uint64_t tag(int bit) const { return shapes[bit].tag; }
+};
+
+template <int SECTIONS, class Tags>
+__device__ __forceinline__ float4 determineColorT(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
+                                                  const Tags& tags, int px, int py, int& status,
                                                  int64_t& texels, int topStart, bool& positional, int& stopBit) {
   // The reference starts at MAXSHAPE (K:1453); no bit at or above the column's
   // assigned shape-bit count is ever set, so starting there finds the same bits.
@@ -743,8 +757,7 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
       done = true;
       lastIsSet = true;
     } else {
-      const uint32_t ref = shapeIdx[topBit];
-      const uint64_t tag = in.shapes[ref].tag;
+      const uint64_t tag = tags.tag(topBit);
       const uint64_t sid = tag & GUDNI_TAG_ID_MASK;
       const uint64_t comp = tag & GUDNI_TAG_COMPOUND_MASK;
       if (sid == lastId) {
@@ -772,6 +785,14 @@ __device__ __forceinline__ float4 determineColor(const RasterInputs& in, const S
   }
   stopBit = topBit;
   return base;
+}
+
+template <int SECTIONS>
+__device__ __forceinline__ float4 determineColor(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
+                                                 const uint32_t* shapeIdx, int px, int py, int& status,
+                                                 int64_t& texels, int topStart, bool& positional, int& stopBit) {
+  return determineColorT<SECTIONS>(in, stack, IndexedTags{shapeIdx, in.shapes}, px, py, status, texels, topStart,
+                                   positional, stopBit);
 }
 
 // Second-level memo for columns whose shape bits fit in one stack word: the last few
@@ -1051,10 +1072,10 @@ __device__ __forceinline__ uint32_t toByte(float v) {
 // instead of the output (the cooperative unit's shared-memory tile).
 // kCounterJitter: take the stochastic jitter from counterRandom (kRandomCounter) in
 // place of the random field; the default instantiation is the reference's scan.
-template <int SECTIONS, bool kCounterJitter = false>
-__device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
-                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
-                                             int shapeBits, float4* image = nullptr, uint32_t* stage = nullptr) {
+template <int SECTIONS, bool kCounterJitter, class Tags>
+__device__ __forceinline__ void renderColumnT(const RasterInputs& in, const ColumnState& c, Queue& q,
+                                              ShapeStack<SECTIONS>& stack, const Tags& tags, int& status,
+                                              int shapeBits, float4* image, uint32_t* stage) {
   Parse p;
   p.current = 0;
   p.numActive = 0;
@@ -1117,7 +1138,8 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
           colorStop = words.stop[e];
           colorPositional = words.row[e] >= 0;
         } else {
-          color = determineColor(in, stack, shapeIdx, px, py, status, texels, shapeBits, colorPositional, colorStop);
+          color = determineColorT<SECTIONS>(in, stack, tags, px, py, status, texels, shapeBits, colorPositional,
+                                            colorStop);
           if (oneWord) words.put(stack.word(0), py, colorPositional, color, colorStop);
         }
         colorOk = true;
@@ -1167,6 +1189,14 @@ __device__ __forceinline__ void renderColumn(const RasterInputs& in, const Colum
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[0]), (unsigned long long)sections);
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[1]), (unsigned long long)texels);
   }
+}
+
+template <int SECTIONS, bool kCounterJitter = false>
+__device__ __forceinline__ void renderColumn(const RasterInputs& in, const ColumnState& c, Queue& q,
+                                             ShapeStack<SECTIONS>& stack, const uint32_t* shapeIdx, int& status,
+                                             int shapeBits, float4* image = nullptr, uint32_t* stage = nullptr) {
+  renderColumnT<SECTIONS, kCounterJitter>(in, c, q, stack, IndexedTags{shapeIdx, in.shapes}, status, shapeBits,
+                                          image, stage);
 }
 
 // One column, start to finish.  Returns true when the queue overflowed `cap`.

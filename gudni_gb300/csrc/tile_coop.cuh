@@ -25,11 +25,12 @@
 //    strand order, so that order is the per-column code's order of pushes, and each
 //    column's slab ends up holding, entry for entry, the queue the per-column
 //    generation builds (newest push first, K:1096-1103);
-//  * per column, the enclosure parity of each shape and whether a shape pushed a
-//    threshold are gathered with shared-memory atomics; the column's lane then turns
-//    tile shape indices into the column's shape bits (the per-column code numbers the
-//    shapes that touch the column in order, K:1586-1593) and sorts and scans its
-//    queue with the per-column code;
+//  * per column, the enclosure parity of each shape is gathered with shared-memory
+//    atomics; the column's shape bits are the tile's shape numbers (the per-column
+//    code numbers only the shapes that touch the column, K:1586-1593, in the same
+//    order, and the scan depends on the bits only through their order), so the
+//    colour walk reads each layer's tag straight from the staged shape records; the
+//    lane sorts and scans its queue with the per-column code;
 //  * the unit's pixels go to a shared-memory tile and leave as whole rows: one bulk
 //    copy per 128-byte row (cp.async.bulk shared -> global) where the row is complete
 //    and aligned, else plain stores.
@@ -265,14 +266,14 @@ __device__ __forceinline__ void storeStagedUnit(const RasterInputs& in, const Co
 }
 
 // The columns of unit `chunk` of tile `ti` (column = chunk * 32 + lane), generated by
-// the whole warp, then each sorted and scanned by its lane.  thrWarp / hdrWarp /
-// idxWarp are the warp's 32 scratch slots (lane L's slot at L * cap, L * idxStride).
+// the whole warp, then each sorted and scanned by its lane.  thrWarp / hdrWarp are
+// the warp's 32 scratch slots (lane L's queue at L * cap).
 // `stage`: write the pixels into sh.stage and store them by rows (single-slab units
 // of at most 32 rows).  Returns kCoop* flags for this lane; with kCoopNotTaken
 // nothing was written.
 __device__ __forceinline__ int runUnitCoop(const RasterInputs& in, const gudni_tile_info& ti, int chunk, int lane,
-                                           float4* thrWarp, uint32_t* hdrWarp, uint32_t* idxWarp, int cap,
-                                           int idxStride, int& status, CoopShared& sh, uint32_t& phase) {
+                                           float4* thrWarp, uint32_t* hdrWarp, int cap, int& status,
+                                           CoopShared& sh, uint32_t& phase) {
   const unsigned full = 0xffffffffu;
   const int numShapes = (int)ti.shapes.length;
   const int tpt = 1 << in.log2_tpt;
@@ -453,24 +454,16 @@ __device__ __forceinline__ int runUnitCoop(const RasterInputs& in, const gudni_t
     } else {
       float4* thr = thrWarp + (size_t)lane * (size_t)cap;
       uint32_t* hdr = hdrWarp + (size_t)lane * (size_t)cap;
-      uint32_t* idx = idxWarp + (size_t)lane * (size_t)idxStride;
+      // The column's shape bits are the tile's shape numbers n (the headers already
+      // carry them): the per-column generation numbers only the shapes that touch
+      // the column, in the same order, and the scan depends on the bits only
+      // through their order (findTop walks them top down, the colour memo compares
+      // positions), so the image is the same.  The initial stack is the enclosure
+      // parity of each shape.
       const unsigned long long encl = sh.encl[lane];
       const unsigned long long touched = encl | sh.added[lane];
-      // the column's shape bits: the touching shapes numbered in order
-      for (int i = cap - count; i < cap; ++i) {
-        const uint32_t h = hdr[i];
-        const uint32_t nn = h & kShapeBitMask;
-        const uint32_t bit = (uint32_t)__popcll(touched & ((1ull << nn) - 1ull));
-        hdr[i] = (h & ~kShapeBitMask) | bit;
-      }
-      uint64_t word = 0ull;
-      int bits = 0;
-      for (unsigned long long m = touched; m; m &= m - 1ull) {
-        const int nn = __ffsll((long long)m) - 1;
-        if ((encl >> nn) & 1ull) word |= 1ull << bits;
-        idx[bits] = ti.shapes.start + (uint32_t)nn;
-        ++bits;
-      }
+      const uint64_t word = encl;
+      const int bits = __popcll(touched);
       Queue q{thr, hdr, cap - count, cap, false};
       sortQueue(q);
       if (in.counters) {
@@ -481,7 +474,9 @@ __device__ __forceinline__ int runUnitCoop(const RasterInputs& in, const gudni_t
       one.clear();
       one.w[0] = word;
       one.nz = word ? 1u : 0u;
-      renderColumn<1>(in, c, q, one, idx, status, bits, nullptr, stageUnit ? sh.stage + lane : nullptr);
+      // tags of bit n: the staged record n (or the tile's records in the shape pile)
+      const DirectTags tags{staged ? sh.shapes : src};
+      renderColumnT<1, false>(in, c, q, one, tags, status, numShapes, nullptr, stageUnit ? sh.stage + lane : nullptr);
       if (q.overflow) {
         flags |= kCoopOverflow;
       } else {

@@ -202,8 +202,8 @@ int run_all_coop(const gudni::RasterInputs& in, const gudni_tile_info* tiles, in
       uint32_t phases[32] = {0};
       const std::function<void(int)> body = [&](int lane) {
         int st = 0;
-        flags[lane] = gudni::runUnitCoop(in, tiles[t], chunk, lane, thr.data(), hdr.data(), idx.data(), cap,
-                                         (int)idxStride, st, *sh, phases[lane]);
+        flags[lane] = gudni::runUnitCoop(in, tiles[t], chunk, lane, thr.data(), hdr.data(), cap, st, *sh,
+                                         phases[lane]);
         laneStatus[lane] = st;
       };
       if (!warp_emu::run(body, seed * 1000003ull + (uint64_t)t * 64u + (uint64_t)chunk)) {
