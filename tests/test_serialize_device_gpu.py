@@ -82,3 +82,61 @@ def test_device_serializer_rejects_bad_scenes():
         with pytest.raises(RasterError) as err:  # no picture pile uploaded: usages fall outside
             r.serialize_device(pic)
         assert err.value.code == -1
+
+
+def test_device_serializer_gives_the_known_piles():
+    """The known-answer piles derived from the reference's Haskell host
+    (tests/golden/known_piles.py): the device serializer through the C ABI writes the
+    same geometry pile and the same jobs, concatenated."""
+    import json
+    import known_piles as K
+    with open(os.path.join(HERE, "golden", "known_piles.json")) as f:
+        known = json.load(f)
+    for name, (shapes, w, h, tile, tpt, per_job, max_strands) in K.scenes().items():
+        spec = L.make_spec(tile, tpt, 4096, 127, 2, max_tiles_per_call=per_job, max_strands_per_tile=max_strands)
+        flat = K.flat_scene(shapes, w, h)
+        with Rasterizer(spec) as r:
+            got = r.download_device_frame(r.serialize_device(flat))
+        want = known[name]
+        assert got["geometry"].tobytes().hex() == want["geometry"], name
+        assert got["shapes"].tobytes() == b"".join(bytes.fromhex(j["shapes"]) for j in want["jobs"]), name
+        base, tiles = 0, []
+        for j in want["jobs"]:
+            t = np.frombuffer(bytes.fromhex(j["tiles"]), dtype=L.TILE_DTYPE).copy()
+            t["shape_start"] += base
+            tiles.append(t)
+            base += len(bytes.fromhex(j["shapes"])) // 16
+        assert got["tiles"].tobytes() == np.concatenate(tiles).tobytes(), name
+
+
+def test_device_serializer_on_the_4k_page():
+    """The 3840x2160 page (5000 glyph-like outlines, 2000 shapes, subtract, gradients,
+    textures: 12,145 shapes after the combinators) serialized by the device passes is
+    the host serializer's frame byte for byte, provenance included, and renders the
+    host frame's image."""
+    import torch
+    flat = G.glyph_page(seed=1)
+    spec = L.make_spec(32, 32, 4096, 127, 8)
+    frame = S.serialize_flat(flat, spec)
+    shapes, tiles, jobs = S.concatenated_piles(frame)
+    dev = torch.device("cuda:0")
+    out = torch.zeros(flat.canvas_h * flat.canvas_w, dtype=torch.int32, device=dev)
+    with Rasterizer(spec) as r:
+        r.upload_pictures(flat.pictures)
+        r.upload_random_field(frame.random_field)
+        df = r.serialize_device(flat, provenance=True)
+        got = r.download_device_frame(df)
+        assert got["geometry"].tobytes() == frame.geometry.tobytes()
+        assert got["shapes"].tobytes() == shapes.tobytes()
+        assert got["tiles"].tobytes() == tiles.tobytes()
+        assert np.array_equal(got["tile_jobs"], jobs)
+        assert list(df.stats) == [frame.stats[k] for k in STATS]
+        assert np.array_equal(got["point_offsets"], frame.point_offsets)
+        assert got["point_weights"].tobytes() == frame.point_weights.tobytes()
+        r.raster_device_frame(df, flat.canvas_w, flat.canvas_h, flat.background, out.data_ptr(),
+                              stream=L.current_stream_handle())
+        r.sync_status()
+        torch.cuda.synchronize()
+        host_img = r.raster_frame(frame)
+    img = out.cpu().numpy().view(np.uint32).reshape(flat.canvas_h, flat.canvas_w)
+    assert np.array_equal(img, host_img)
