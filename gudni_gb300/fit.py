@@ -4,17 +4,19 @@ one persistent launch per step (gudni_batch_adjoint).  No counterpart in the
 reference, which only renders.
 
 Each step serializes the current scenes (the serializer's point provenance maps the
-geometry pile back to the scene's curve points), uploads them as one batch, runs the
-adjoint of all scenes at once, carries the pile gradient to the points
-(scene.pair_gradient) and updates points and colours with Adam on the host.  The
-loss is the per-pixel L2 of the adjoint module over every scene.
+geometry pile back to the scene's curve points), uploads them as one batch and runs
+the adjoint of all scenes at once; on the device it then carries the pile gradient to
+the curve points (the provenance as gather and scatter-add, scene.pair_gradient's
+arithmetic) and updates every scene's points and colours with one Adam over their
+concatenation (Adam is elementwise, so this is each scene's own optimiser), and only
+the updated points and colours come back for the next serialization.  The loss is the
+per-pixel L2 of the adjoint module over every scene.
 """
 from __future__ import annotations
 
 import os
 import time
 from concurrent.futures import ThreadPoolExecutor
-from dataclasses import dataclass
 from typing import Sequence
 
 import numpy as np
@@ -25,26 +27,51 @@ from . import lib as L
 from . import scene as S
 
 
-@dataclass
-class Adam:
-    lr: float
-    beta1: float = 0.9
-    beta2: float = 0.999
-    eps: float = 1e-8
-    m: np.ndarray = None
-    v: np.ndarray = None
-    t: int = 0
+class DeviceAdam:
+    """Adam (Kingma and Ba 2015) over one float64 device tensor of parameters."""
 
-    def step(self, x: np.ndarray, g: np.ndarray) -> np.ndarray:
+    def __init__(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
+        self.lr, self.beta1, self.beta2, self.eps = lr, beta1, beta2, eps
+        self.m = self.v = None
+        self.t = 0
+
+    def step(self, x, g):
         if self.m is None:
-            self.m = np.zeros_like(g, dtype=np.float64)
-            self.v = np.zeros_like(g, dtype=np.float64)
+            self.m = g.new_zeros(g.shape)
+            self.v = g.new_zeros(g.shape)
         self.t += 1
-        self.m = self.beta1 * self.m + (1 - self.beta1) * g
-        self.v = self.beta2 * self.v + (1 - self.beta2) * g * g
+        self.m.mul_(self.beta1).add_(g, alpha=1 - self.beta1)
+        self.v.mul_(self.beta2).addcmul_(g, g, value=1 - self.beta2)
         mh = self.m / (1 - self.beta1 ** self.t)
         vh = self.v / (1 - self.beta2 ** self.t)
-        return x - self.lr * mh / (np.sqrt(vh) + self.eps)
+        return x - self.lr * mh / (vh.sqrt() + self.eps)
+
+
+def pair_gradients(frames, frame_geo_offsets, pair_start, grad_geometry):
+    """dL/d(curve pairs) of every scene of a batch at once, on grad_geometry's device:
+    scene.pair_gradient's gather of each pile point's x and y and scatter-add through
+    its provenance (up to three weighted source points), with every frame's pile
+    offsets shifted to its place in the batch (frame_geo_offsets, bytes) and its pair
+    indices to its place in the concatenated pairs (pair_start).  Returns a float64
+    (total pairs, 4) tensor."""
+    import torch
+    offs, srcs, wts = [], [], []
+    for i, fr in enumerate(frames):
+        offs.append(fr.point_offsets.astype(np.int64) + int(frame_geo_offsets[i]) // 4)
+        src = fr.point_sources.astype(np.int64)
+        srcs.append(np.where(src >= 0, src + 2 * int(pair_start[i]), -1))
+        wts.append(fr.point_weights.astype(np.float64))
+    dev = grad_geometry.device
+    off = torch.from_numpy(np.concatenate(offs)).to(dev)
+    src = torch.from_numpy(np.concatenate(srcs).reshape(-1, 3)).to(dev)
+    wt = torch.from_numpy(np.concatenate(wts).reshape(-1, 3)).to(dev)
+    g64 = grad_geometry.double()
+    gxy = torch.stack([g64[off], g64[off + 1]], 1)
+    gp = torch.zeros((2 * int(pair_start[-1]), 2), dtype=torch.float64, device=dev)
+    for j in range(3):
+        m = src[:, j] >= 0
+        gp.index_add_(0, src[m, j], wt[m, j, None] * gxy[m])
+    return gp.reshape(-1, 4)
 
 
 class BatchFit:
@@ -57,8 +84,11 @@ class BatchFit:
         self.spec = spec
         self.flats = list(flats)
         self.targets = [A.target_from(t[..., :3]) for t in targets]
-        self.point_opt = [Adam(lr_points) for _ in self.flats]
-        self.color_opt = [Adam(lr_colors) for _ in self.flats]
+        self.point_opt = DeviceAdam(lr_points)
+        self.color_opt = DeviceAdam(lr_colors)
+        # every scene's curve pairs and colours, concatenated, in float64 on the device
+        self.pair_start = np.cumsum([0] + [len(f.pairs) for f in self.flats])
+        self.sub_start = np.cumsum([0] + [len(f.substance_color) for f in self.flats])
         self.r = B.BatchRasterizer(spec, device)
         self.dev = torch.device("cuda", device)
         self.timings = {"serialize": 0.0, "upload": 0.0, "device": 0.0, "update": 0.0}
@@ -70,6 +100,11 @@ class BatchFit:
     def close(self):
         self.pool.shutdown()
         self.r.close()
+
+    def _sub_slice(self, i: int):
+        """(start, stop) of scene i's substances in the batch's substance pile."""
+        _, ss = self.r.frame_slices(i)
+        return ss.start, ss.stop
 
     def _target_tensor(self, batch: B.Batch):
         if self._target is None:
@@ -98,17 +133,21 @@ class BatchFit:
         self.r.sync_status()
         d = image[:, :3] - target[:, :3]
         loss = float((d.double() * d.double()).sum())
-        gg, gs = gg.cpu().numpy(), gs.cpu().numpy()
         t3 = time.perf_counter()
-        for i, (f, fr) in enumerate(zip(self.flats, frames)):
-            sg, ss = self.r.frame_slices(i)
-            gp = S.pair_gradient(fr, gg[sg]).reshape(f.pairs.shape)
-            f.pairs = self.point_opt[i].step(f.pairs.astype(np.float64), gp).astype(np.float32)
-            gc = gs[ss].astype(np.float64)
-            solid = f.substance_kind == 0
-            col = f.substance_color.astype(np.float64)
-            new = self.color_opt[i].step(col, np.where(solid[:, None], gc, 0.0))
-            f.substance_color = np.clip(new, 0.0, 1.0).astype(np.float32)
+        dev = self.dev
+        gp = pair_gradients(frames, batch.frame_geo_offsets, self.pair_start, gg)
+        pairs = torch.from_numpy(np.concatenate([f.pairs for f in self.flats]).astype(np.float64)).to(dev)
+        pairs = self.point_opt.step(pairs, gp)
+        # colours: solid substances only (a texture's colour slot holds no colour)
+        subs = torch.cat([gs[slice(*self._sub_slice(i))] for i in range(len(self.flats))]).double()
+        solid = torch.from_numpy(np.concatenate([f.substance_kind == 0 for f in self.flats])).to(dev)
+        cols = torch.from_numpy(np.concatenate([f.substance_color for f in self.flats]).astype(np.float64)).to(dev)
+        cols = self.color_opt.step(cols, torch.where(solid[:, None], subs, torch.zeros_like(subs)))
+        cols = cols.clamp_(0.0, 1.0).float().cpu().numpy()
+        pairs = pairs.float().cpu().numpy()
+        for i, f in enumerate(self.flats):
+            f.pairs = pairs[self.pair_start[i]:self.pair_start[i + 1]].copy()
+            f.substance_color = cols[self.sub_start[i]:self.sub_start[i + 1]].copy()
         t4 = time.perf_counter()
         self.timings["serialize"] += t1 - t0
         self.timings["upload"] += t2 - t1

@@ -136,14 +136,37 @@ def test_pair_gradient_sums_knob_splits():
 
 
 def test_adam_step_matches_the_textbook_update():
-    """fit.Adam: bias-corrected first and second moments (Kingma & Ba, Algorithm 1)."""
-    from gudni_gb300.fit import Adam
-    opt = Adam(lr=0.1)
+    """fit.DeviceAdam: bias-corrected first and second moments (Kingma & Ba,
+    Algorithm 1), on torch tensors (here on the CPU)."""
+    import torch
+    from gudni_gb300.fit import DeviceAdam
+    opt = DeviceAdam(lr=0.1)
     x = np.array([1.0, -2.0])
     g1, g2 = np.array([0.5, -1.0]), np.array([0.25, 2.0])
-    x1 = opt.step(x, g1)
+    t = lambda a: torch.from_numpy(a.copy())  # noqa: E731
+    x1 = opt.step(t(x), t(g1)).numpy()
     np.testing.assert_allclose(x1, x - 0.1 * np.sign(g1), rtol=1e-6)  # first step: lr * g / |g|
     m = 0.9 * 0.1 * g1 + 0.1 * g2
     v = 0.999 * 0.001 * g1 ** 2 + 0.001 * g2 ** 2
     mh, vh = m / (1 - 0.9 ** 2), v / (1 - 0.999 ** 2)
-    np.testing.assert_allclose(opt.step(x1, g2), x1 - 0.1 * mh / (np.sqrt(vh) + 1e-8), rtol=1e-9)
+    np.testing.assert_allclose(opt.step(t(x1), t(g2)).numpy(), x1 - 0.1 * mh / (np.sqrt(vh) + 1e-8), rtol=1e-9)
+
+
+def test_batch_pair_gradients_equal_each_frames_pair_gradient():
+    """fit.pair_gradients (every scene of a batch at once, as the fitting step runs it
+    on the device) gives scene.pair_gradient of each frame, on the frame's slice of a
+    batch pile gradient (here random, on the CPU)."""
+    import torch
+    from gudni_gb300 import batch as B
+    from gudni_gb300.fit import pair_gradients
+    flats = [G.random_shapes(seed=s, width=64, height=48, n_shapes=5) for s in range(3)]
+    frames = [S.serialize_flat(f, L.make_spec(16, 16, 1024, 127, 2)) for f in flats]
+    batch = B.build_batch(frames)
+    rng = np.random.default_rng(1)
+    gg = rng.standard_normal(batch.geometry.size // 4).astype(np.float32)
+    pair_start = np.cumsum([0] + [len(f.pairs) for f in flats])
+    got = pair_gradients(frames, batch.frame_geo_offsets, pair_start, torch.from_numpy(gg)).numpy()
+    for i, fr in enumerate(frames):
+        g0 = int(batch.frame_geo_offsets[i]) // 4
+        want = S.pair_gradient(fr, gg[g0:g0 + fr.geometry.size // 4])
+        np.testing.assert_allclose(got[pair_start[i]:pair_start[i + 1]], want, rtol=1e-12, atol=1e-12)
