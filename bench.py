@@ -66,6 +66,8 @@ def parse():
                     help="scan columns with at least this many thresholds by the whole warp (0: off)")
     ap.add_argument("--device-strand-table", action="store_true",
                     help="uploads build the strand table on the device (gudni_set_device_strand_table)")
+    ap.add_argument("--cooperative-units", default="off", choices=["off", "on", "auto"],
+                    help="warp-cooperative work units (gudni_set_cooperative_units) in every rasterizer")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--plain-untimed-pass", type=int, default=1,
                     help="batch256: one untimed pass of the per-scene path before timing it")
@@ -156,6 +158,17 @@ def reference_runner(workload: str, frame):
             print(f"reference kernels unavailable ({e}); timing the oracle", file=sys.stderr)
             fn, kind, img = (lambda: O.render_frame(frame)), "port", want  # noqa: E731
     return fn, kind, img, want
+
+
+def apply_coop(r, args):
+    """The --cooperative-units choice on a rasterizer (gudni_set_cooperative_units)."""
+    mode = getattr(args, "cooperative_units", "off")
+    r.set_cooperative_units({"on": True, "off": False, "auto": None}[mode])
+
+
+def ref_build_flags():
+    from oracle import build_ref
+    return build_ref.compile_flags()
 
 
 def lsb_parity(a, b):
@@ -313,7 +326,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": config_dict(frame, args.workload),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                             "build": " ".join(ref_build_flags()) if kind == "reference" else None},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "parity_reference_vs_oracle": lsb_parity(img, want)}
     print(json.dumps(line))
@@ -350,6 +364,7 @@ def run_batch(args, emit=True):
     t_ser = time.perf_counter() - t0
     spec = A.spec_for(32, 32, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
     r = B.BatchRasterizer(spec)
+    apply_coop(r, args)
     if args.dense_columns:
         r.set_dense_columns(args.dense_columns)
     r.upload(batch)
@@ -471,6 +486,7 @@ def run_adjoint(args, emit=True):
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     r = Rasterizer(spec)
+    apply_coop(r, args)
     with torch.cuda.stream(stream):
         tr = A.FrameAdjoint(r, tframe)
         _, timg, _, _ = tr.loss_and_gradient(np.zeros((1024, 1024, 4), np.float32))
@@ -586,6 +602,7 @@ def run_scene(args):
     shapes, tiles, jobs = S.concatenated_piles(host)
     w, h = flat.canvas_w, flat.canvas_h
     r = Rasterizer(spec)
+    apply_coop(r, args)
     r.upload_pictures(flat.pictures)
     r.upload_random_field(host.random_field)
     out = torch.zeros(w * h, dtype=torch.int32, device=dev)
@@ -719,6 +736,52 @@ def run_fit(args, emit=True):
     return line
 
 
+def time_plain(workload: str, coop: str, steps: int) -> float:
+    """Median ms of the workload's frame launch (gudni_raster_tiles_device, resident
+    piles) with the given --cooperative-units choice; the image is checked against the
+    per-column kernel's."""
+    import torch
+    from gudni_gb300 import scene as S
+    from gudni_gb300.raster import Rasterizer
+    frame = make_frame(workload, False, *PLAIN_TILES[workload])
+    shapes, tiles, tile_jobs = S.concatenated_piles(frame)
+    dev = torch.device("cuda", 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    d_shapes = torch.from_numpy(shapes.view(np.uint8).copy()).to(dev)
+    d_tiles = torch.from_numpy(tiles.view(np.uint8).copy()).to(dev)
+    d_jobs = torch.from_numpy(tile_jobs.copy()).to(dev)
+    d_out = torch.zeros(frame.canvas_w * frame.canvas_h, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    with Rasterizer(frame.spec) as r:
+        r.set_cooperative_units({"on": True, "off": False, "auto": None}[coop])
+        r.upload_common(frame)
+        torch.cuda.synchronize()
+
+        def step():
+            r.raster_tiles_device(frame, d_shapes.data_ptr(), len(shapes), d_tiles.data_ptr(), d_jobs.data_ptr(),
+                                  len(tiles), d_out.data_ptr(), stream=stream.cuda_stream)
+
+        for _ in range(3):
+            step()
+        ts = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        r.sync_status()
+        img = d_out.cpu().numpy()
+        r.set_cooperative_units(False)
+        ref = r.raster_frame(frame).reshape(-1)
+    if not np.array_equal(img.view(np.uint32), ref):
+        raise RuntimeError(f"{workload}: the {coop} image differs from the per-column kernel's")
+    return statistics.median(ts)
+
+
 def form_records(args) -> dict:
     """The three systems forms beside the plain page, each run briefly (timed repeats
     stated in each record), as sub-records of the page's line: the batched form on the
@@ -771,6 +834,17 @@ def form_records(args) -> dict:
                    "2000-step fit is --workload fit64 --steps 2000")
         return rec
 
+    def cooperative():
+        """The warp-cooperative units against the per-column kernel on the page and on
+        the quarter page (device-resident piles, CUDA events, median of 5 launches)."""
+        rec = {"timing": "median of 5 launches each after 3 warm-up launches, L2 flushed between launches"}
+        for wl in ("page4k", "page1080"):
+            ms = {m: time_plain(wl, m, 5) for m in ("off", "on")}
+            rec[wl] = {"per_column_ms": ms["off"], "cooperative_ms": ms["on"],
+                       "cooperative_over_per_column": ms["on"] / ms["off"]}
+        return rec
+
+    guarded("cooperative_units", cooperative)
     guarded("batched", batched)
     guarded("adjoint", adjoint)
     guarded("fit", fitting)
@@ -809,6 +883,7 @@ def main():
     frame = make_frame(args.workload, False, *tile_override(args, *PLAIN_TILES[args.workload]))
     shapes, tiles, tile_jobs = S.concatenated_piles(frame)
     r = Rasterizer(frame.spec, device=local)
+    apply_coop(r, args)
     if args.device_strand_table:
         r.set_device_strand_table(True)
     if args.dense_columns:
@@ -928,7 +1003,8 @@ def main():
     line = {"metric": WORKLOADS[args.workload][1], "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(config_dict(frame, args.workload), dense_columns=args.dense_columns),
+            "config": dict(config_dict(frame, args.workload), dense_columns=args.dense_columns,
+                           cooperative_units=args.cooperative_units),
             "frames_per_s": 1000.0 / ms * world, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clocks.summary(), "roofline": roofline,
             "work": {"thresholds": counters["thresholds"], "sections": counters["sections"],
@@ -940,7 +1016,8 @@ def main():
         sample = f"{args.cpu_sample_frames} full frame(s), {dt:.2f} s each"
         if kind == "reference" and len(frame.radials):
             sample += "; radial gradients baked into pictures (the reference has no radial substance)"
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample}
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+                                "build": " ".join(ref_build_flags()) if kind == "reference" else None}
         line["parity_vs_oracle"] = lsb_parity(gpu_img, img)
         line["parity_reference_vs_oracle"] = ref_parity
     r.close()

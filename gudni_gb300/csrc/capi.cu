@@ -31,6 +31,10 @@
 
 using gudni::TileLaunch;
 
+// Work units per resident cooperative warp below which a launch takes the cooperative
+// units when the choice is automatic (gudni_set_cooperative_units(ctx, -1)).
+#define GUDNI_COOP_UNITS_PER_WARP 2
+
 namespace {
 
 std::mutex g_create_mutex;
@@ -74,6 +78,7 @@ struct gudni_ctx {
   int sm_count = 0;
   int sections = 1;
   int blocks_per_sm = 1;
+  int coop_blocks_per_sm = 1;  // resident blocks of the cooperative-unit kernel
   int grid = 1;
   int working_capacity = 256;
   cudaStream_t stream = nullptr;
@@ -145,7 +150,7 @@ struct gudni_ctx {
   DevBuf<int64_t> counters;
   bool counters_on = false;
   int dense_min = 0;  // gudni_set_dense_columns (0: per-lane scan only)
-  bool coop = true;   // gudni_set_cooperative_units
+  int coop = 0;       // gudni_set_cooperative_units: 1 on, 0 off (default), -1 chosen per launch
   uint32_t random_mode = gudni::kRandomField;  // gudni_set_random_source
   uint64_t random_seed = 0;
   bool device_strands = false;  // gudni_set_device_strand_table
@@ -371,7 +376,14 @@ int enqueue(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::SceneInf
   a.overflow_cap = (uint32_t)std::min<size_t>(max_items, 0xFFFFFFFFull);
   a.overflow_count = ctx->words.ptr;
   a.dense_min = ctx->dense_min;
-  a.coop = ctx->coop ? 1 : 0;
+  // Cooperative units shorten each unit (its generation is shared by the warp) but
+  // hold more registers per thread, so fewer warps are resident.  A launch with few
+  // units per resident warp is bound by its longest units and takes them; one with
+  // many is bound by throughput and runs the per-column kernel, which keeps more warps
+  // in flight (GUDNI_COOP_UNITS_PER_WARP units per resident cooperative warp is the
+  // crossover measured on GB300).
+  const size_t coop_warps = (size_t)ctx->sm_count * (size_t)ctx->coop_blocks_per_sm * (gudni::kRasterBlock / 32);
+  a.coop = ctx->coop > 0 || (ctx->coop < 0 && n_units <= coop_warps * GUDNI_COOP_UNITS_PER_WARP) ? 1 : 0;
   a.status = ctx->status.ptr;
   const size_t warps_per_block = gudni::kRasterBlock / 32;
   const int grid = (int)std::min<size_t>((n_units + warps_per_block - 1) / warps_per_block, (size_t)ctx->grid);
@@ -712,6 +724,9 @@ gudni_ctx* gudni_create(const gudni_spec* spec, int device) {
   ctx->sections = gudni::sections_for(spec->max_shape);
   if ((e = gudni::raster_occupancy(ctx->sections, &ctx->blocks_per_sm)) != cudaSuccess || ctx->blocks_per_sm < 1)
     ctx->blocks_per_sm = 1;
+  if ((e = gudni::raster_coop_occupancy(ctx->sections, &ctx->coop_blocks_per_sm)) != cudaSuccess ||
+      ctx->coop_blocks_per_sm < 1)
+    ctx->coop_blocks_per_sm = 1;
   ctx->grid = ctx->sm_count * ctx->blocks_per_sm;
   // fast-pass capacity: as much of max_thresholds as ~8 GB of slots allow (at most
   // 4096); only columns that need more go through the full-capacity pass
@@ -1257,10 +1272,11 @@ int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds) {
   return GUDNI_OK;
 }
 
-int gudni_set_cooperative_units(gudni_ctx* ctx, int enable) {
+int gudni_set_cooperative_units(gudni_ctx* ctx, int mode) {
   if (!ctx) return GUDNI_ERR_BAD_INPUT;
-  if ((enable != 0) != ctx->coop) drop_graph(ctx);  // a captured launch holds the old setting
-  ctx->coop = enable != 0;
+  const int m = mode > 0 ? 1 : (mode == 0 ? 0 : -1);
+  if (m != ctx->coop) drop_graph(ctx);  // a captured launch holds the old setting
+  ctx->coop = m;
   return GUDNI_OK;
 }
 

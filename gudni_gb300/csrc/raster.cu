@@ -243,6 +243,20 @@ cudaError_t launch_raster(const TileLaunch& a, bool list, int sections, int grid
   }
 }
 
+cudaError_t raster_coop_occupancy(int sections, int* blocks_per_sm) {
+  const void* fn = nullptr;
+  switch (sections) {
+    case 1: fn = (const void*)raster_tiles_coop_kernel<1>; break;
+    case 2: fn = (const void*)raster_tiles_coop_kernel<2>; break;
+    case 4: fn = (const void*)raster_tiles_coop_kernel<4>; break;
+    case 8: fn = (const void*)raster_tiles_coop_kernel<8>; break;
+    case 16: fn = (const void*)raster_tiles_coop_kernel<16>; break;
+    case 32: fn = (const void*)raster_tiles_coop_kernel<32>; break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, kRasterBlock, 0);
+}
+
 cudaError_t raster_occupancy(int sections, int* blocks_per_sm) {
   const void* fn = nullptr;
   switch (sections) {

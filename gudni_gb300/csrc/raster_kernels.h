@@ -112,5 +112,6 @@ cudaError_t launch_tile_order(const gudni_tile_info* tiles, uint32_t n_tiles, co
                               uint32_t n_shapes, int chunk_log2, uint32_t* words128, uint32_t* units,
                               cudaStream_t stream);
 cudaError_t raster_occupancy(int sections, int* blocks_per_sm);
+cudaError_t raster_coop_occupancy(int sections, int* blocks_per_sm);
 
 }  // namespace gudni

@@ -201,10 +201,10 @@ class Rasterizer:
         The image does not change."""
         self._check(self.lib.gudni_set_dense_columns(self.ctx, int(min_thresholds)))
 
-    def set_cooperative_units(self, on: bool = True) -> None:
-        """Warp-cooperative generation of each work unit (gudni_set_cooperative_units,
-        on by default); off runs every column's generation on its own lane."""
-        self._check(self.lib.gudni_set_cooperative_units(self.ctx, 1 if on else 0))
+    def set_cooperative_units(self, on: Optional[bool] = True) -> None:
+        """Warp-cooperative work units (gudni_set_cooperative_units): True for every
+        launch, False for none, None to let each launch choose (the default)."""
+        self._check(self.lib.gudni_set_cooperative_units(self.ctx, -1 if on is None else (1 if on else 0)))
 
     def read_counters(self) -> dict:
         c = (C.c_int64 * 4)()

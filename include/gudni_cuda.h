@@ -345,19 +345,27 @@ int gudni_set_random_source(gudni_ctx* ctx, int source, uint64_t seed);
  * counterpart in the reference. */
 int gudni_set_dense_columns(gudni_ctx* ctx, int32_t min_thresholds);
 
-/* Warp-cooperative work units (on by default): the 32 lanes of a warp generate a
- * unit's thresholds together -- strands dealt to the lanes, their (strand, column)
- * pairs dealt again, the thresholds binned to the columns by warp ballots in the
- * order the per-column generation pushes them -- with the tile's shape records staged
- * in shared memory by a bulk copy and the pixels written out by rows from a shared
- * tile; each column is then sorted and scanned by its own lane.  Units of tiles with
- * more than 64 shapes or more shapes than max_shape run the per-column generation.
+/* Warp-cooperative work units: the 32 lanes of a warp generate a unit's thresholds
+ * together -- strands dealt to the lanes, their (strand, column) pairs dealt again,
+ * the thresholds binned to the columns by warp ballots in the order the per-column
+ * generation pushes them -- with the tile's shape records staged in shared memory by
+ * a bulk copy (the colour walk reads their tags there) and the pixels written out by
+ * rows from a shared tile; each column is then sorted and scanned by its own lane.
  * Replaces the per-column generation of generateThresholds (Kernels.cl:2030-2082,
- * buildThresholdArray K:1540-1595); the output is the same bit for bit.  0 runs every
- * unit through the per-column generation.  Not used by the warp-cooperative dense
- * scan (gudni_set_dense_columns), by the counter-based jitter, or by
+ * buildThresholdArray K:1540-1595); the output is the same bit for bit.  Units of
+ * tiles with more than 64 shapes or more shapes than max_shape run the per-column
+ * generation.  mode 1: every launch uses them; 0 (the default): none does; -1: a
+ * launch uses them when it has at most two work units per warp the cooperative
+ * kernel keeps resident (few, long units: the kernel is bound by its longest units,
+ * which the shared generation shortens), and the per-column kernel otherwise (many
+ * units: throughput, where the per-column kernel's smaller register footprint keeps
+ * more warps in flight).  On GB300 the cooperative kernel renders the 1920x1080 page
+ * in 12.3 ms against 13.5 ms, and the 3840x2160 page in 27.1 ms against 23.3 ms; tiles
+ * it does not take (more than 64 shapes) run slower inside it than in the per-column
+ * kernel.  Not used by the warp-cooperative dense scan
+ * (gudni_set_dense_columns), by the counter-based jitter, or by
  * gudni_raster_job_noalloc. */
-int gudni_set_cooperative_units(gudni_ctx* ctx, int enable);
+int gudni_set_cooperative_units(gudni_ctx* ctx, int mode);
 
 /* ------------------------------------------------------------------ adjoint */
 

@@ -33,6 +33,10 @@ OUT_DIR = os.path.join(HERE, "_ref")
 DEFAULT_REFERENCE = os.environ.get("GUDNI_REFERENCE") or "/root/reference"
 KERNELS_REL = os.path.join("src", "Graphics", "Gudni", "OpenCL", "Kernels.cl")
 SOURCE_PADDING = 40  # sOURCEfILEpADDING, Raster/Constants.hs:70
+# Optimisation level of the CPU build (GUDNI_REF_OPT, default -O2: one recipe that
+# builds the same on the x86 build machine and the Arm GPU host; -O3 is there to
+# compare the two once).
+OPT = os.environ.get("GUDNI_REF_OPT") or "-O2"
 
 VECTOR_LITERAL = re.compile(
     r"\(\s*(float2|float4|float8|int2|int4|uchar4|COLOR|SPACE2|SPACE4|THRESHOLD)\s*\)\s*\(")
@@ -67,7 +71,13 @@ def variant(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
 
 
 def library_name(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
-    return os.path.join(OUT_DIR, f"libgudni_ref_{variant(max_shape, sections, stochastic)}.so")
+    opt = "" if OPT == "-O2" else "_" + OPT.lstrip("-")
+    return os.path.join(OUT_DIR, f"libgudni_ref_{variant(max_shape, sections, stochastic)}{opt}.so")
+
+
+def compile_flags() -> list[str]:
+    """The g++ flags of the CPU build (no -march=native: the same recipe on both hosts)."""
+    return ["-std=c++17", OPT, "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp"]
 
 
 def source_name(max_shape: int, sections: int, stochastic: float = 0.0) -> str:
@@ -105,8 +115,7 @@ def build(reference: str = DEFAULT_REFERENCE, max_shape: int = 127, sections: in
     elif not os.path.isfile(cpp):
         # neither the reference checkout nor a translation unit generated from it
         return None
-    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fopenmp",
-           "-fPIC", "-shared", "-w", "-Wno-psabi", "-I", HERE, cpp, "-o", lib]
+    cmd = ["g++"] + compile_flags() + ["-fPIC", "-shared", "-w", "-Wno-psabi", "-I", HERE, cpp, "-o", lib]
     subprocess.run(cmd, check=True)
     return lib
 
