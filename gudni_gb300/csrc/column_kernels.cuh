@@ -12,11 +12,13 @@
 
 namespace gudni {
 
-// Up to 8 stack words the kernel is held to 72 registers (7 blocks of 128 threads per
-// SM): the scan is latency-bound, and on the 4K page the extra resident warps outweigh
-// the few spills (23.3 ms a frame against 24.8 ms at the 80 registers ptxas picks).
+// With a stack of at most two words the kernel is held to 72 registers (7 blocks of
+// 128 threads per SM): the scan is latency-bound, and on the 4K page the extra resident
+// warps outweigh the few spills (23.3 ms a frame against 24.8 ms at the 80 registers
+// ptxas picks).  Wider stacks (hundreds of shapes per column) spill heavily at that
+// bound (4x slower on 500 canvas-wide shapes) and keep ptxas's choice.
 template <int SECTIONS>
-constexpr int rasterMinBlocks() { return SECTIONS <= 8 ? 7 : 1; }
+constexpr int rasterMinBlocks() { return SECTIONS <= 2 ? 7 : 1; }
 
 template <int SECTIONS, bool kCounterJitter>
 __global__ void __launch_bounds__(kRasterBlock, rasterMinBlocks<SECTIONS>()) raster_tiles_kernel(TileLaunch a) {
