@@ -112,6 +112,9 @@ WORKLOADS = {
                     "Mpixels/s (fwd+adjoint, 1024x1024 500 shapes, grads vs FP64 reference)"),
     # batched fitting (run_fit): 64 scenes of 256x256, 128 shapes each, Adam on points and colours
     "fit64": ("fit_64x256x256_shapes128", "steps/s (batched fwd+adjoint fitting, 64 scenes 256x256)"),
+    # the 256-scene mix's densest scene alone (run_dense): 87x75, 1817 canvas-wide shapes
+    "densest": ("batch_mix_scene25_87x75_shapes1817",
+                "Mpixels/s (the batched mix's densest scene, 87x75 with 1817 shapes, <=1 LSB RGBA8)"),
     # scene to pixels on the device (run_scene): the page serialized by kernels, then rendered
     "scene4k": ("scene_page_3840x2160_glyphs5000_shapes2000",
                 "Mpixels/s (scene to pixels: device serializer + raster, 3840x2160 page, <=1 LSB RGBA8)"),
@@ -578,6 +581,48 @@ def run_adjoint(args, emit=True):
     return line
 
 
+def run_dense(args):
+    """The batched mix's densest scene (scene 25 of batch_mix(seed=2): 87x75 canvas,
+    1817 canvas-wide random shapes, ~97,000 sections per pixel) rendered alone at the
+    spec the autotuner picks for its bucket (8-pixel tiles, 64 threads: one-pixel
+    columns), with or without the warp-cooperative scan of dense columns
+    (--dense-columns).  Timed on the host clock around each blocking frame call (one
+    launch is seconds long); the image is checked against the per-lane scan's."""
+    from gudni_gb300 import autotune as A
+    from gudni_gb300 import scene as S
+    from gudni_gb300 import scenes as G
+    from gudni_gb300.raster import Rasterizer
+    flat = G.batch_mix(seed=2, n_scenes=26)[25]
+    spec = A.spec_for(8, 64, BATCH_MAX_SHAPE, BATCH_MAX_THRESHOLDS, BATCH_STRANDS_PER_TILE)
+    frame = S.serialize_flat(flat, spec)
+    times, img = [], None
+    with Rasterizer(spec) as r:
+        apply_coop(r, args)
+        if args.dense_columns:
+            r.set_dense_columns(args.dense_columns)
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            img = r.raster_frame(frame)
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        launches = r.launch_count()
+    parity = None
+    if args.dense_columns and not args.no_cpu_baseline:
+        with Rasterizer(spec) as r:
+            parity = lsb_parity(img, r.raster_frame(frame))
+    s_frame = statistics.median(times)
+    line = {"metric": WORKLOADS["densest"][1], "value": frame.canvas_w * frame.canvas_h / s_frame / 1e6, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * s_frame,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS["densest"][0], "canvas": [frame.canvas_w, frame.canvas_h],
+                       "shapes": int(frame.stats["shapes"]), "tile_size": 8, "threads_per_tile": 64,
+                       "max_shape": BATCH_MAX_SHAPE, "dense_columns": args.dense_columns,
+                       "timing": "host clock around gudni_raster_frame (blocking), median"},
+            "gpu_launches": int(launches), "parity_vs_per_lane_scan": parity}
+    print(json.dumps(line))
+    return 0
+
+
 def run_scene(args):
     """Scene to pixels on the device: the page's flattened scene (host arrays, what a
     host hands over) serialized by kernels (gudni_serialize_device) and rendered from
@@ -884,6 +929,8 @@ def main():
         return 0
     if args.workload == "scene4k":
         return run_scene(args)
+    if args.workload == "densest":
+        return run_dense(args)
 
     import torch
 
