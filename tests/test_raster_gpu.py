@@ -388,3 +388,18 @@ def test_cooperative_units_overflow_to_the_full_pass(monkeypatch):
     want = np.load(os.path.join(GOLDEN, INDEX["random_128x96"]["image_file"]))
     with Rasterizer(frame.spec) as r:
         assert np.array_equal(r.raster_frame(frame), want)
+
+
+def test_cooperative_units_chosen_per_launch():
+    """gudni_set_cooperative_units(ctx, -1): each launch picks the cooperative units
+    or the per-column kernel by its number of work units; whichever it picks, the
+    image is the per-column kernel's (job by job and as one frame launch)."""
+    small = F.build("random_128x96")
+    big = S.serialize_flat(G.random_shapes(seed=0, width=512, height=512, n_shapes=64),
+                           L.make_spec(32, 256, 4096, 127, 8))
+    for frame in (small, big):
+        with Rasterizer(frame.spec) as r:
+            want = r.raster_frame(frame)
+            r.set_cooperative_units(None)
+            assert np.array_equal(r.raster_frame(frame), want)
+            assert np.array_equal(r.queue_jobs(frame), want)
