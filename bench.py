@@ -78,6 +78,10 @@ def parse():
     ap.add_argument("--form-dense-columns", type=int, default=32,
                     help="page4k sub-records: the batched form's warp-cooperative dense columns threshold")
     ap.add_argument("--fit-steps", type=int, default=5, help="page4k sub-records: timed fitting steps")
+    ap.add_argument("--fit-resume", default=None,
+                    help="fit64: continue from a state written by --fit-checkpoint (BatchFit.load)")
+    ap.add_argument("--fit-checkpoint", default=None,
+                    help="fit64: write the fit's state here at the end (BatchFit.save)")
     ap.add_argument("--tile", type=int, default=None, help="tile size (default: the workload's)")
     ap.add_argument("--threads-per-tile", type=int, default=None, help="threads per tile (default: the workload's)")
     return ap.parse_args()
@@ -735,7 +739,9 @@ def run_fit(args, emit=True):
     """Batched fitting: 64 independent 256x256 scenes of 128 shapes fitted by Adam (lr
     0.5 px on points, 0.01 on colours) to targets rendered from perturbed copies
     (points N(0, 4 px), colours N(0, 0.1)); each step serializes the scenes, runs every
-    scene's forward and adjoint in one launch and updates on the host."""
+    scene's forward and adjoint in one launch and updates every scene's points and
+    colours by Adam on the device.  --fit-checkpoint / --fit-resume split a long fit
+    over several processes (BatchFit.save / load)."""
     import torch
     from gudni_gb300 import adjoint as A
     from gudni_gb300 import fit as F
@@ -753,6 +759,10 @@ def run_fit(args, emit=True):
             _, img, _, _ = fa.loss_and_gradient(np.zeros((f.canvas_h, f.canvas_w, 4), np.float32))
             targets.append(img.cpu().numpy())
     fit = F.BatchFit(fit_scenes(), targets, spec, lr_points=0.5, lr_colors=0.01)
+    resume = getattr(args, "fit_resume", None)
+    if resume:
+        fit.load(resume)
+    resumed_steps = fit.steps
     pixels = 64 * 256 * 256
     for _ in range(args.warmup):  # warm-up steps are fitting steps too; they are counted in `steps_total`
         fit.step()
@@ -776,10 +786,14 @@ def run_fit(args, emit=True):
                        **FIT_SPEC, "lr_points_px": 0.5, "lr_colors": 0.01,
                        "targets": "perturbed copies: points N(0, 4 px), colours N(0, 0.1)",
                        "data": "synthetic, seeded"},
-            "steps_total": args.warmup + args.steps,
+            "steps_total": fit.steps,
+            "resumed_from_step": resumed_steps,
             "loss": {"first_timed": first, "final": final, "per_pixel_l2_first": first / (pixels * 3),
                      "per_pixel_l2_final": final / (pixels * 3)},
             "seconds": {k: v for k, v in fit.timings.items()}}
+    checkpoint = getattr(args, "fit_checkpoint", None)
+    if checkpoint:
+        fit.save(checkpoint)
     if emit:
         print(json.dumps(line))
     fit.close()

@@ -96,10 +96,46 @@ class BatchFit:
         # serialize in parallel
         self.pool = ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1))
         self._target = None
+        self.steps = 0  # Adam steps taken, including those before a `load`
 
     def close(self):
         self.pool.shutdown()
         self.r.close()
+
+    def save(self, path: str) -> None:
+        """Write the fit's state (every scene's curve pairs and colours, both Adam
+        moments and step counts, the steps taken) to an .npz file, so that a long fit
+        can continue in another process with `load`."""
+        def moments(opt):
+            if opt.m is None:
+                return np.zeros(0), np.zeros(0)
+            return opt.m.cpu().numpy(), opt.v.cpu().numpy()
+        pm, pv = moments(self.point_opt)
+        cm, cv = moments(self.color_opt)
+        np.savez(path, pairs=np.concatenate([f.pairs for f in self.flats]),
+                 colors=np.concatenate([f.substance_color for f in self.flats]),
+                 pair_start=self.pair_start, sub_start=self.sub_start,
+                 point_m=pm, point_v=pv, point_t=self.point_opt.t,
+                 color_m=cm, color_v=cv, color_t=self.color_opt.t, steps=self.steps)
+
+    def load(self, path: str) -> None:
+        """Continue from a state written by `save` for the same scenes (same curve and
+        substance counts per scene); raises ValueError for another set of scenes."""
+        z = np.load(path)
+        if not (np.array_equal(z["pair_start"], self.pair_start) and np.array_equal(z["sub_start"], self.sub_start)):
+            raise ValueError("checkpoint was written for other scenes")
+        for i, f in enumerate(self.flats):
+            f.pairs = z["pairs"][self.pair_start[i]:self.pair_start[i + 1]].astype(np.float32)
+            f.substance_color = z["colors"][self.sub_start[i]:self.sub_start[i + 1]].astype(np.float32)
+        for opt, key in ((self.point_opt, "point"), (self.color_opt, "color")):
+            opt.t = int(z[key + "_t"])
+            m = z[key + "_m"]
+            if m.size:
+                opt.m = self.torch.from_numpy(m).to(self.dev)
+                opt.v = self.torch.from_numpy(z[key + "_v"]).to(self.dev)
+            else:
+                opt.m = opt.v = None
+        self.steps = int(z["steps"])
 
     def _sub_slice(self, i: int):
         """(start, stop) of scene i's substances in the batch's substance pile."""
@@ -153,4 +189,5 @@ class BatchFit:
         self.timings["upload"] += t2 - t1
         self.timings["device"] += t3 - t2
         self.timings["update"] += t4 - t3
+        self.steps += 1
         return loss

@@ -170,3 +170,40 @@ def test_batch_pair_gradients_equal_each_frames_pair_gradient():
         g0 = int(batch.frame_geo_offsets[i]) // 4
         want = S.pair_gradient(fr, gg[g0:g0 + fr.geometry.size // 4])
         np.testing.assert_allclose(got[pair_start[i]:pair_start[i + 1]], want, rtol=1e-12, atol=1e-12)
+
+
+def test_fit_checkpoint_round_trip(tmp_path):
+    """BatchFit.save / load: a fit continued from a checkpoint has the same curve
+    pairs, colours, Adam moments and step counts as the one that wrote it (the state
+    here on the CPU, without a rasterizer), and a checkpoint of other scenes is refused."""
+    import torch
+    from gudni_gb300.fit import BatchFit, DeviceAdam
+
+    def fake_fit(flats):
+        f = BatchFit.__new__(BatchFit)
+        f.torch, f.dev, f.flats, f.steps = torch, torch.device("cpu"), flats, 0
+        f.pair_start = np.cumsum([0] + [len(x.pairs) for x in flats])
+        f.sub_start = np.cumsum([0] + [len(x.substance_color) for x in flats])
+        f.point_opt, f.color_opt = DeviceAdam(0.5), DeviceAdam(0.01)
+        return f
+
+    flats = [G.random_shapes(seed=s, width=64, height=48, n_shapes=4) for s in range(3)]
+    a = fake_fit(flats)
+    pairs = torch.from_numpy(np.concatenate([x.pairs for x in flats]).astype(np.float64))
+    for k in range(3):  # three Adam steps on made-up gradients
+        pairs = a.point_opt.step(pairs, torch.full_like(pairs, 0.1 * (k + 1)))
+        a.steps += 1
+    for i, x in enumerate(a.flats):
+        x.pairs = pairs[a.pair_start[i]:a.pair_start[i + 1]].float().numpy()
+    path = str(tmp_path / "fit.npz")
+    a.save(path)
+    b = fake_fit([G.random_shapes(seed=s, width=64, height=48, n_shapes=4) for s in range(3)])
+    b.load(path)
+    assert b.steps == 3 and b.point_opt.t == 3 and b.color_opt.t == 0 and b.color_opt.m is None
+    for x, y in zip(a.flats, b.flats):
+        np.testing.assert_array_equal(x.pairs, y.pairs)
+        np.testing.assert_array_equal(x.substance_color, y.substance_color)
+    assert torch.equal(a.point_opt.m, b.point_opt.m) and torch.equal(a.point_opt.v, b.point_opt.v)
+    other = fake_fit([G.random_shapes(seed=9, width=64, height=48, n_shapes=5)])
+    with pytest.raises(ValueError):
+        other.load(path)
