@@ -536,6 +536,12 @@ def run_adjoint(args, emit=True):
         r.sync_status()
         launches = r.launch_count() - launches0
         fwd_ms, adj_ms = statistics.median(ft), statistics.median(at)
+        # the other mode: the backward regenerates the thresholds (same image and gradients)
+        r.set_adjoint_regenerate(True)
+        fwd_adjoint()
+        regen_ms = statistics.median(timed(fwd_adjoint, args.steps))
+        r.set_adjoint_regenerate(False)
+        r.sync_status()
         loss, img, gg, gs = fa.loss_and_gradient(target)
         gg, gs = gg.cpu().numpy().astype(np.float64), gs.cpu().numpy().astype(np.float64)
         img = img.cpu().numpy()
@@ -578,6 +584,11 @@ def run_adjoint(args, emit=True):
                        "tiles": int(frame.n_tiles), **adj_spec, "l2": "flushed between steps (256 MB write)",
                        "data": "synthetic, seeded"},
             "forward_ms": fwd_ms, "fwd_adjoint_ms": adj_ms, "fwd_adjoint_over_forward": adj_ms / fwd_ms,
+            "thresholds": "generated once per work unit: the forward scans a copy of the sorted queue, the "
+                          "backward the queue itself",
+            "regenerate": {"fwd_adjoint_ms": regen_ms, "fwd_adjoint_over_forward": regen_ms / fwd_ms,
+                           "thresholds": "the forward generates its own, the backward generates them again "
+                                         "(gudni_set_adjoint_regenerate)", "steps": args.steps},
             "gpu_launches": int(launches), "clocks": clocks.summary(), "gradient_check": check}
     if emit:
         print(json.dumps(line))
@@ -750,7 +761,9 @@ def run_fit(args, emit=True):
     from gudni_gb300.raster import Rasterizer
 
     torch.cuda.set_device(0)
-    spec = L.make_spec(**FIT_SPEC)
+    tile, tpt = tile_override(args, FIT_SPEC["max_tile_size"], FIT_SPEC["threads_per_tile"])
+    fit_spec = {**FIT_SPEC, "max_tile_size": tile, "threads_per_tile": tpt}
+    spec = L.make_spec(**fit_spec)
     log = lambda m: print(m, file=sys.stderr, flush=True)  # noqa: E731
     targets = []
     with Rasterizer(spec) as r:
@@ -783,7 +796,7 @@ def run_fit(args, emit=True):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS["fit64"][0], "scenes": 64, "canvas": [256, 256], "shapes": 128,
-                       **FIT_SPEC, "lr_points_px": 0.5, "lr_colors": 0.01,
+                       **fit_spec, "lr_points_px": 0.5, "lr_colors": 0.01,
                        "targets": "perturbed copies: points N(0, 4 px), colours N(0, 0.1)",
                        "data": "synthetic, seeded"},
             "steps_total": fit.steps,
@@ -890,20 +903,22 @@ def form_records(args) -> dict:
             specs.append(run_adjoint(a, emit=False))
         best = min(specs, key=lambda ln: ln["forward_ms"])
         keys = ("metric", "value", "unit", "forward_ms", "fwd_adjoint_ms", "fwd_adjoint_over_forward",
-                "gpu_launches", "clocks")
+                "thresholds", "regenerate", "gpu_launches", "clocks")
         rec = {k: best[k] for k in keys}
         rec.update(steps=3, warmup=3, timing="median of 3 timed launches of each", config=best["config"],
                    gradient_check=specs[0]["gradient_check"],
                    gradient_check_spec=[specs[0]["config"]["max_tile_size"], specs[0]["config"]["threads_per_tile"]],
                    by_spec=[{"tile": ln["config"]["max_tile_size"], "threads_per_tile": ln["config"]["threads_per_tile"],
                              "forward_ms": ln["forward_ms"], "fwd_adjoint_ms": ln["fwd_adjoint_ms"],
-                             "fwd_adjoint_over_forward": ln["fwd_adjoint_over_forward"]} for ln in specs],
+                             "fwd_adjoint_over_forward": ln["fwd_adjoint_over_forward"],
+                             "regenerate_fwd_adjoint_ms": ln["regenerate"]["fwd_adjoint_ms"]} for ln in specs],
                    headline="the spec with the fastest forward")
         return rec
 
     def fitting():
         f = copy.copy(args)
         f.steps, f.warmup = args.fit_steps, 1
+        f.tile = f.threads_per_tile = f.fit_resume = f.fit_checkpoint = None  # the fit's own spec, from step 0
         ln = run_fit(f, emit=False)
         keys = ("metric", "value", "unit", "ms_per_step", "loss", "steps_total", "seconds")
         rec = {k: ln[k] for k in keys}

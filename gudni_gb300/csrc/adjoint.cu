@@ -96,6 +96,8 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
   s.cap = a.capacity;
   s.thr = a.thr + slot * cap;
   s.hdr = a.hdr + slot * cap;
+  s.thrFwd = a.thr_fwd + slot * cap;
+  s.hdrFwd = a.hdr_fwd + slot * cap;
   s.prov = a.prov + slot * cap;
   s.lines = reinterpret_cast<LineRec*>(a.lines) + slot * cap;
   s.lineGrad = a.line_grad + slot * cap;
@@ -128,8 +130,8 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
     int nLines = 0, nBits = 0;
     float2 delta = make_float2(0.0f, 0.0f);
     if (column < tpt) {
-      if (adjointColumn<SECTIONS>(in, ti, column, s, a.image + base, a.target + base, nLines, nBits, delta,
-                                  status))
+      if (adjointColumn<SECTIONS>(in, ti, column, s, a.image + base, a.target + base, a.regenerate != 0, nLines,
+                                  nBits, delta, status))
         status |= kStatusOverflow;
     }
     warpChain(in, s, nLines, nBits, delta, a.grad_geometry, a.grad_substances);  // all 32 lanes

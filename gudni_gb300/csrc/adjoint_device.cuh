@@ -649,6 +649,8 @@ __device__ __forceinline__ void epTargets(const EP& e, float gx, float gy, const
 struct AdjSlot {
   float4* thr;
   uint32_t* hdr;
+  float4* thrFwd;  // the forward scan's copy of the sorted queue
+  uint32_t* hdrFwd;
   int4* prov;
   LineRec* lines;
   float4* lineGrad;
@@ -681,7 +683,9 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   bool colorOk = false, colorPositional = false;
   int colorStop = 0, K = 0;
   float chainArea = 0.0f;
-  float gI[3] = {0.0f, 0.0f, 0.0f}, I[3] = {0.0f, 0.0f, 0.0f}, A = 1.0f;
+  // invA: 1 / the pixel's section-area sum, taken once per pixel (the gradients need
+  // no bit-exact match, only the forward image does)
+  float gI[3] = {0.0f, 0.0f, 0.0f}, I[3] = {0.0f, 0.0f, 0.0f}, invA = 1.0f;
   // Geometry gradients are gathered per band: every section of a band shares its y
   // sources, and a threshold line is the right edge of one section and the left edge
   // of the next at the same mid-height, so its two contributions are summed
@@ -689,7 +693,8 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   float gY0 = 0.0f, gY1 = 0.0f, pendCoef = 0.0f;
   auto flushChain = [&]() {
     if (grad && chainArea != 0.0f && K > 0) {
-      float4 d = make_float4(gI[0] * chainArea / A, gI[1] * chainArea / A, gI[2] * chainArea / A, 0.0f);
+      const float w = chainArea * invA;
+      float4 d = make_float4(gI[0] * w, gI[1] * w, gI[2] * w, 0.0f);
       for (int k = K - 1; k >= 0; --k) {
         float4 df, db;
         compositeAdjoint(s.front[k], s.layer[k], d, df, db);
@@ -723,7 +728,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       I[0] = im.x;
       I[1] = im.y;
       I[2] = im.z;
-      A = im.w;
+      invA = 1.0f / im.w;
       gI[0] = 2.0f * (im.x - tg.x);
       gI[1] = 2.0f * (im.y - tg.y);
       gI[2] = 2.0f * (im.z - tg.z);
@@ -857,7 +862,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       area += a;
       if (grad) {
         // a = (x1 - x0)(y1 - y0): d/dx1 = w, d/dx0 = -w, d/dy1 = h, d/dy0 = -h
-        const float dA = (gI[0] * (col.x - I[0]) + gI[1] * (col.y - I[1]) + gI[2] * (col.z - I[2])) / A;
+        const float dA = (gI[0] * (col.x - I[0]) + gI[1] * (col.y - I[1]) + gI[2] * (col.z - I[2])) * invA;
         const float w = sy1 - sy0, hgt = sx1 - sx0;
         gY0 -= dA * hgt;
         gY1 += dA * hgt;
@@ -898,46 +903,85 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   }
 }
 
+// The forward scan (renderColumn, writing the float image) of a sorted queue.
+template <int SECTIONS>
+__device__ __forceinline__ void forwardScan(const RasterInputs& in, const ColumnState& c, Queue& q,
+                                            ShapeStack<SECTIONS>& stack, const AdjSlot& s, uint32_t bits,
+                                            float4* image, int& status) {
+  if (SECTIONS > 1 && bits <= 64) {
+    ShapeStack<1> one;
+    one.clear();
+    one.w[0] = stack.word(0);
+    one.nz = one.w[0] ? 1u : 0u;
+    renderColumn<1>(in, c, q, one, s.idx, status, (int)bits, image);
+  } else {
+    renderColumn<SECTIONS>(in, c, q, stack, s.idx, status, (int)bits, image);
+  }
+}
+
 // one column: float image, then gradients
 // The column's lines and their gradients stay in the slot (nLines, nBits, delta out);
 // the kernel carries them to the pile and the substances for the whole warp at once.
+//
+// By default the thresholds are generated once, with provenance: the forward scan
+// runs on a copy of the sorted queue (the scan consumes its queue) and the gradient
+// scan on the queue itself, so nothing outlives the work unit.  generateP makes the
+// same thresholds in the same order as buildThresholds (the same decisions and
+// arithmetic, with sources recorded beside them) and both sorts are stable under the
+// same order, so the forward image is the raster kernel's.  With `regenerate` the
+// forward pass generates its own thresholds (buildThresholds) and the gradient pass
+// generates them again.
 template <int SECTIONS>
 __device__ bool adjointColumn(const RasterInputs& in, const gudni_tile_info& ti, int column, const AdjSlot& s,
-                              float4* image, const float4* target, int& nLines, int& nBits, float2& delta,
-                              int& status) {
+                              float4* image, const float4* target, bool regenerate, int& nLines, int& nBits,
+                              float2& delta, int& status) {
   nLines = 0;
   nBits = 0;
   const ColumnState c = initColumn(in, ti, column, in.job_index);
   if (!c.active) return false;
-  {
-    // pass 1: the raster kernel's own generate / order / render, writing the float
-    // image (I rgb, section-area sum) instead of bytes
-    Queue q{s.thr, s.hdr, s.cap, s.cap, false};
-    ShapeStack<SECTIONS> stack;
-    stack.clear();
-    const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, s.idx, status);
-    if (q.overflow) return true;
-    sortQueue(q);
-    if (SECTIONS > 1 && bits <= 64) {
-      ShapeStack<1> one;
-      one.clear();
-      one.w[0] = stack.word(0);
-      one.nz = one.w[0] ? 1u : 0u;
-      renderColumn<1>(in, c, q, one, s.idx, status, (int)bits, image);
-    } else {
-      renderColumn<SECTIONS>(in, c, q, stack, s.idx, status, (int)bits, image);
-    }
-    if (q.overflow) return true;
-  }
-  // pass 2: the thresholds again, now with provenance, and the gradients
   AdjQueue q{s.thr, s.hdr, s.prov, s.cap, s.cap, false};
-  ShapeStack<SECTIONS> stack;
-  stack.clear();
   int n_lines = 0;
   AdjGen g{&q, s.lines, &n_lines, s.cap, &c};
-  const uint32_t bits = generateP<SECTIONS>(in, c, g, stack, s.idx, status);
-  if (q.overflow) return true;
-  q.sort();
+  ShapeStack<SECTIONS> stack;
+  stack.clear();
+  uint32_t bits = 0, fbits;
+  Queue f{s.thrFwd, s.hdrFwd, s.cap, s.cap, false};  // the forward scan's queue
+  if (regenerate) {  // the raster kernel's own generate and order
+    fbits = buildThresholds<SECTIONS>(in, c, f, stack, s.idx, status);
+    if (f.overflow) return true;
+    sortQueue(f);
+  } else {  // the thresholds with provenance, once; the forward scans a copy
+    bits = fbits = generateP<SECTIONS>(in, c, g, stack, s.idx, status);
+    if (q.overflow) return true;
+    q.sort();
+    for (int i = q.start; i < q.cap; ++i) {
+      s.thrFwd[i] = s.thr[i];
+      s.hdrFwd[i] = s.hdr[i];
+    }
+    f.start = q.start;
+  }
+  // The stack the generation left, for the gradient scan: kept in local memory while
+  // the forward scan runs (a second stack in registers would spill in the scans).
+  volatile uint64_t w0[SECTIONS];
+#pragma unroll
+  for (int k = 0; k < SECTIONS; ++k) w0[k] = stack.w[k];
+  const uint32_t nz0 = stack.nz;
+  const int hi0 = stack.hiFlip;
+  // the forward: the float image (I rgb, section-area sum) instead of bytes
+  forwardScan<SECTIONS>(in, c, f, stack, s, fbits, image, status);
+  if (f.overflow) return true;
+  if (regenerate) {  // the thresholds again, now with provenance
+    stack.clear();
+    bits = generateP<SECTIONS>(in, c, g, stack, s.idx, status);
+    if (q.overflow) return true;
+    q.sort();
+  } else {
+#pragma unroll
+    for (int k = 0; k < SECTIONS; ++k) stack.w[k] = w0[k];
+    stack.nz = nz0;
+    stack.hiFlip = hi0;
+  }
+  // the gradients
   for (int i = 0; i < n_lines; ++i) s.lineGrad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   for (uint32_t b = 0; b < bits; ++b) s.bitGrad[b] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (SECTIONS > 1 && bits <= 64) {  // as the forward scan: a one-word stack

@@ -21,6 +21,9 @@ struct AdjointLaunch {
   int capacity;           // thresholds (and lines) per column
   float4* thr;            // slots * capacity
   uint32_t* hdr;          // slots * capacity
+  float4* thr_fwd;        // slots * capacity: the forward scan's copy of the sorted queue
+  uint32_t* hdr_fwd;      // slots * capacity
+  int regenerate;         // 1: the forward generates its own thresholds, the backward regenerates them
   int4* prov;             // slots * capacity
   void* lines;            // slots * capacity line records
   float4* line_grad;      // slots * capacity

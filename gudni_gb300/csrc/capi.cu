@@ -160,6 +160,9 @@ struct gudni_ctx {
   int adj_capacity = 0;
   DevBuf<float4> a_thr;
   DevBuf<uint32_t> a_hdr;
+  DevBuf<float4> a_thr_fwd;  // the forward scan's copy of each column's sorted queue
+  DevBuf<uint32_t> a_hdr_fwd;
+  int adj_regenerate = 0;  // gudni_set_adjoint_regenerate
   DevBuf<int4> a_prov;
   DevBuf<uint8_t> a_lines;
   DevBuf<float4> a_line_grad;
@@ -523,7 +526,7 @@ int ensure_adjoint_scratch(gudni_ctx* ctx) {
   }
   int bps = 1;
   if (gudni::adjoint_occupancy(ctx->sections, &bps) != cudaSuccess || bps < 1) bps = 1;
-  const size_t per_slot = (size_t)cap * (sizeof(float4) + 4 + sizeof(int4) + gudni::adjoint_line_bytes() +
+  const size_t per_slot = (size_t)cap * (2 * (sizeof(float4) + 4) + sizeof(int4) + gudni::adjoint_line_bytes() +
                                          sizeof(float4)) +
                           (size_t)ctx->spec.max_shape * (4 + sizeof(float4)) +
                           (size_t)(ctx->spec.max_shape + 1) * (2 * sizeof(float4) + 4);
@@ -533,6 +536,8 @@ int ensure_adjoint_scratch(gudni_ctx* ctx) {
   cudaError_t e;
   if ((e = ctx->a_thr.reserve(slots * cap)) != cudaSuccess ||
       (e = ctx->a_hdr.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_thr_fwd.reserve(slots * cap)) != cudaSuccess ||
+      (e = ctx->a_hdr_fwd.reserve(slots * cap)) != cudaSuccess ||
       (e = ctx->a_prov.reserve(slots * cap)) != cudaSuccess ||
       (e = ctx->a_lines.reserve(slots * cap * gudni::adjoint_line_bytes())) != cudaSuccess ||
       (e = ctx->a_line_grad.reserve(slots * cap)) != cudaSuccess ||
@@ -582,6 +587,9 @@ int enqueue_adjoint(gudni_ctx* ctx, const gudni::RasterInputs& in, const gudni::
   a.next_tile = ctx->words.ptr + 1;
   a.capacity = ctx->adj_capacity;
   a.thr = ctx->a_thr.ptr;
+  a.thr_fwd = ctx->a_thr_fwd.ptr;
+  a.hdr_fwd = ctx->a_hdr_fwd.ptr;
+  a.regenerate = ctx->adj_regenerate;
   a.hdr = ctx->a_hdr.ptr;
   a.prov = ctx->a_prov.ptr;
   a.lines = ctx->a_lines.ptr;
@@ -1277,6 +1285,12 @@ int gudni_set_cooperative_units(gudni_ctx* ctx, int mode) {
   const int m = mode > 0 ? 1 : (mode == 0 ? 0 : -1);
   if (m != ctx->coop) drop_graph(ctx);  // a captured launch holds the old setting
   ctx->coop = m;
+  return GUDNI_OK;
+}
+
+int gudni_set_adjoint_regenerate(gudni_ctx* ctx, int on) {
+  if (!ctx) return GUDNI_ERR_BAD_INPUT;
+  ctx->adj_regenerate = on ? 1 : 0;
   return GUDNI_OK;
 }
 

@@ -217,6 +217,8 @@ def load_cuda(build_if_missing: bool = True):
     lib.gudni_set_dense_columns.argtypes = [vp, i32]
     lib.gudni_set_cooperative_units.restype = C.c_int
     lib.gudni_set_cooperative_units.argtypes = [vp, C.c_int]
+    lib.gudni_set_adjoint_regenerate.restype = C.c_int
+    lib.gudni_set_adjoint_regenerate.argtypes = [vp, C.c_int]
     lib.gudni_launch_count.restype = C.c_uint64
     lib.gudni_launch_count.argtypes = [vp]
     lib.gudni_adjoint_tiles_device.restype = C.c_int

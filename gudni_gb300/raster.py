@@ -203,8 +203,14 @@ class Rasterizer:
 
     def set_cooperative_units(self, on: Optional[bool] = True) -> None:
         """Warp-cooperative work units (gudni_set_cooperative_units): True for every
-        launch, False for none, None to let each launch choose (the default)."""
+        launch, False for none, None to let each launch choose.  A context starts with
+        False."""
         self._check(self.lib.gudni_set_cooperative_units(self.ctx, -1 if on is None else (1 if on else 0)))
+
+    def set_adjoint_regenerate(self, on: bool = True) -> None:
+        """The adjoint's backward pass regenerates each column's thresholds
+        (gudni_set_adjoint_regenerate) instead of scanning the forward pass's queue."""
+        self._check(self.lib.gudni_set_adjoint_regenerate(self.ctx, 1 if on else 0))
 
     def read_counters(self) -> dict:
         c = (C.c_int64 * 4)()

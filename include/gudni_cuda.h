@@ -378,7 +378,12 @@ int gudni_set_cooperative_units(gudni_ctx* ctx, int mode);
  * as for gudni_raster_tiles_device; `target` and `image` are bitmap_w*bitmap_h float4
  * (image receives I rgb and the pixel's section-area sum in .w); `grad_geometry`
  * (geometry_bytes/4 floats) and `grad_substances` (4 floats per substance) are ADDED
- * to.  Thresholds are recomputed in the backward pass, not stored.  A column that
+ * to.  Forward and backward run in one launch, one work unit (a tile's 32 columns) at
+ * a time, and no threshold outlives its work unit: by default each column's
+ * thresholds are generated once, with their sources in the pile, the forward scan
+ * runs on a copy of the sorted queue and the gradient scan on the queue itself; with
+ * gudni_set_adjoint_regenerate(ctx, 1) the forward generates its own and the
+ * backward generates them again.  The image is the same either way.  A column that
  * needs more than the adjoint's working capacity (min(max_thresholds, 1024), or
  * GUDNI_ADJOINT_CAPACITY) raises GUDNI_ERR_THRESHOLD_OVERFLOW.  The stochastic area
  * jitter (STOCHASTIC_FACTOR) is off in the adjoint: the loss is defined on the
@@ -390,6 +395,10 @@ int gudni_adjoint_tiles_device(gudni_ctx* ctx,
                                const float background[4],
                                const float* target, float* image,
                                float* grad_geometry, float* grad_substances, void* stream);
+
+/* 1: the adjoint's backward pass regenerates each column's thresholds instead of
+ * scanning the forward pass's queue (0, the default).  Returns GUDNI_OK. */
+int gudni_set_adjoint_regenerate(gudni_ctx* ctx, int on);
 
 /* Batch form: every scene of the uploaded batch (gudni_batch_upload) in one
  * persistent launch; target and image hold out_pixels float4 at the scenes' output

@@ -28,6 +28,8 @@ def load():
     lib.host_column_raster_job.restype = C.c_int
     lib.host_column_raster_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, vp,
                                            C.c_float, i, i, vp, C.POINTER(C.c_int)]
+    lib.host_column_set_adjoint_regenerate.restype = None
+    lib.host_column_set_adjoint_regenerate.argtypes = [i]
     lib.host_column_adjoint_job.restype = C.c_int
     lib.host_column_adjoint_job.argtypes = [vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp, i, i, i, i, i, vp, i,
                                             i, vp, vp, vp, vp, C.POINTER(C.c_int)]

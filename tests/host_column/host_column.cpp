@@ -290,12 +290,16 @@ static int stack_words(int max_shape) {
   return sections;
 }
 
+static int g_adjoint_regenerate = 0;  // host_column_set_adjoint_regenerate
+
+extern "C" void host_column_set_adjoint_regenerate(int on) { g_adjoint_regenerate = on ? 1 : 0; }
+
 template <int SECTIONS>
 static int adjoint_all(const gudni::RasterInputs& in, const gudni_tile_info* tiles, int n_tiles, int tpt, int cap,
                        float4* image, const float4* target, float* gGeo, float* gSub, int* overflow) {
   const int layerCap = in.max_shape + 1;
-  std::vector<float4> thr((size_t)cap), lineGrad((size_t)cap), bitGrad((size_t)in.max_shape + 1);
-  std::vector<uint32_t> hdr((size_t)cap), idx((size_t)in.max_shape + 1);
+  std::vector<float4> thr((size_t)cap), thrFwd((size_t)cap), lineGrad((size_t)cap), bitGrad((size_t)in.max_shape + 1);
+  std::vector<uint32_t> hdr((size_t)cap), hdrFwd((size_t)cap), idx((size_t)in.max_shape + 1);
   std::vector<int4> prov((size_t)cap);
   std::vector<gudni::LineRec> lines((size_t)cap);
   std::vector<float4> layers(2 * (size_t)layerCap);
@@ -303,6 +307,8 @@ static int adjoint_all(const gudni::RasterInputs& in, const gudni_tile_info* til
   gudni::AdjSlot s;
   s.thr = thr.data();
   s.hdr = hdr.data();
+  s.thrFwd = thrFwd.data();
+  s.hdrFwd = hdrFwd.data();
   s.prov = prov.data();
   s.lines = lines.data();
   s.lineGrad = lineGrad.data();
@@ -319,7 +325,8 @@ static int adjoint_all(const gudni::RasterInputs& in, const gudni_tile_info* til
     for (int column = 0; column < tpt; ++column) {
       int nLines = 0, nBits = 0;
       float2 delta = make_float2(0.0f, 0.0f);
-      if (gudni::adjointColumn<SECTIONS>(in, tiles[t], column, s, image, target, nLines, nBits, delta, status))
+      if (gudni::adjointColumn<SECTIONS>(in, tiles[t], column, s, image, target, g_adjoint_regenerate != 0, nLines,
+                                         nBits, delta, status))
         *overflow = 1;
       // the kernel's warp gathering, one lane at a time
       for (int i = 0; i < nLines; ++i) {

@@ -82,6 +82,28 @@ def test_adjoint_repeatable_and_accumulates_nothing_stale():
         np.testing.assert_allclose(s2.cpu().numpy(), s1, rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("name", ["random_160x120", "glyphs_256x192", "dense"])
+def test_adjoint_generated_once_equals_regenerated(name):
+    """The default adjoint (thresholds generated once per work unit, the forward
+    scanning a copy) against gudni_set_adjoint_regenerate(ctx, 1) (the forward's own
+    raster generation, the backward's second generation): the same float image bit
+    for bit, and the same gradients up to the order of the atomic adds."""
+    if name == "dense":
+        spec = L.make_spec(16, 64, 4096, 255, 4, max_strands_per_tile=1 << 24)
+        frame, target = case(lambda: G.random_shapes(seed=93, width=128, height=128, n_shapes=120), spec=spec)
+    else:
+        frame, target = case(SCENES[name])
+    with Rasterizer(frame.spec) as r:
+        fa = A.FrameAdjoint(r, frame)
+        _, i1, g1, s1 = fa.loss_and_gradient(target)
+        i1, g1, s1 = i1.cpu().numpy().copy(), g1.cpu().numpy().copy(), s1.cpu().numpy().copy()
+        r.set_adjoint_regenerate(True)
+        _, i2, g2, s2 = fa.loss_and_gradient(target)
+        np.testing.assert_array_equal(i2.cpu().numpy(), i1)
+        np.testing.assert_allclose(g2.cpu().numpy(), g1, rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(s2.cpu().numpy(), s1, rtol=1e-5, atol=1e-6)
+
+
 def test_adjoint_threads_per_tile():
     make = lambda: G.random_shapes(seed=11, width=128, height=96, n_shapes=16)  # noqa: E731
     for tpt, tile in ((16, 16), (64, 32), (128, 32)):

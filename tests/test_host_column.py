@@ -120,9 +120,10 @@ def test_non_finite_points():
     check(S.serialize_flat(flat, L.make_spec(16, 32, 4096, 127, 8)))
 
 
-def host_adjoint(frame, target, capacity=1024):
+def host_adjoint(frame, target, capacity=1024, regenerate=False):
     from host_column.build import load
     lib = load()
+    lib.host_column_set_adjoint_regenerate(1 if regenerate else 0)
     img = np.zeros((frame.canvas_h, frame.canvas_w, 4), np.float32)
     gg = np.zeros(frame.geometry.size // 4, np.float32)
     gs = np.zeros((len(frame.substances), 4), np.float32)
@@ -173,6 +174,29 @@ def test_adjoint_column_code_matches_fp64_reference(name):
     for got, want, what in ((gg, g_geo, "geometry"), (gs, g_sub, "substances")):
         norm, worst = _rel(got, want)
         assert norm <= 1e-3 and worst <= 1e-3, (what, norm, worst)
+
+
+@pytest.mark.parametrize("name", ["random", "dense", "glyphs"])
+def test_adjoint_generated_once_equals_regenerated(name):
+    """The adjoint's two modes on the host: thresholds generated once with provenance
+    (the forward scanning a copy of the sorted queue) and the raster generation for the
+    forward with a second generation for the gradients give the same float image and
+    the same gradients, bit for bit -- generateP and buildThresholds make the same
+    queue."""
+    if name == "random":
+        flat, spec = G.random_shapes(seed=21, width=150, height=110, n_shapes=30), L.make_spec(32, 32, 4096, 127, 8)
+    elif name == "dense":
+        flat = G.random_shapes(seed=92, width=96, height=80, n_shapes=120)
+        spec = L.make_spec(16, 64, 4096, 255, 4, max_strands_per_tile=1 << 24)
+    else:
+        flat = G.glyph_page(seed=4, width=256, height=192, n_glyphs=60, n_shapes=30)
+        spec = L.make_spec(32, 128, 4096, 127, 8)
+    frame = S.serialize_flat(flat, spec)
+    target = np.random.default_rng(2).random((frame.canvas_h, frame.canvas_w, 4)).astype(np.float32)
+    once = host_adjoint(frame, target, capacity=4096)
+    twice = host_adjoint(frame, target, capacity=4096, regenerate=True)
+    for a, b in zip(once, twice):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_adjoint_column_code_generated_scenes():
