@@ -82,6 +82,10 @@ def parse():
                     help="fit64: continue from a state written by --fit-checkpoint (BatchFit.load)")
     ap.add_argument("--fit-checkpoint", default=None,
                     help="fit64: write the fit's state here at the end (BatchFit.save)")
+    ap.add_argument("--fit-total-steps", type=int, default=None,
+                    help="fit64: stop the timed steps once the fit has taken this many Adam steps in all")
+    ap.add_argument("--fit-time-limit", type=float, default=None,
+                    help="fit64: stop the timed steps after this many seconds (then --fit-checkpoint)")
     ap.add_argument("--tile", type=int, default=None, help="tile size (default: the workload's)")
     ap.add_argument("--threads-per-tile", type=int, default=None, help="threads per tile (default: the workload's)")
     return ap.parse_args()
@@ -781,19 +785,28 @@ def run_fit(args, emit=True):
         fit.step()
     fit.timings = {k: 0.0 for k in fit.timings}  # the split below covers the timed steps only
     first = None
+    total = getattr(args, "fit_total_steps", None)
+    limit = getattr(args, "fit_time_limit", None)
     t0 = time.perf_counter()
     losses = []
     for k in range(args.steps):
+        if (total is not None and fit.steps >= total) or (limit is not None and time.perf_counter() - t0 > limit):
+            break
         loss = fit.step()
         losses.append(loss)
         if first is None:
             first = loss
         if k % max(1, args.steps // 10) == 0:
-            log(f"step {k}: loss {loss:.4f} per-pixel L2 {loss / (pixels * 3):.6f}")
+            log(f"step {fit.steps}: loss {loss:.4f} per-pixel L2 {loss / (pixels * 3):.6f}")
     wall = time.perf_counter() - t0
+    steps = len(losses)
+    if steps == 0:
+        raise SystemExit("fit64: no timed step (the fit had already reached --fit-total-steps)")
     final = losses[-1]
-    line = {"metric": WORKLOADS["fit64"][1], "value": args.steps / wall, "unit": "steps/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+    timings = dict(fit.timings)
+    after = fit.evaluate()  # the loss after the last update (untimed)
+    line = {"metric": WORKLOADS["fit64"][1], "value": steps / wall, "unit": "steps/s", "n_gpus": 1,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS["fit64"][0], "scenes": 64, "canvas": [256, 256], "shapes": 128,
                        **fit_spec, "lr_points_px": 0.5, "lr_colors": 0.01,
@@ -802,8 +815,11 @@ def run_fit(args, emit=True):
             "steps_total": fit.steps,
             "resumed_from_step": resumed_steps,
             "loss": {"first_timed": first, "final": final, "per_pixel_l2_first": first / (pixels * 3),
-                     "per_pixel_l2_final": final / (pixels * 3)},
-            "seconds": {k: v for k, v in fit.timings.items()}}
+                     "per_pixel_l2_final": final / (pixels * 3),
+                     "after_last_update": after, "per_pixel_l2_after_last_update": after / (pixels * 3),
+                     "note": "each step's loss is taken before its update: `final` is the loss after "
+                             "steps_total - 1 updates, `after_last_update` after steps_total"},
+            "seconds": timings}
     checkpoint = getattr(args, "fit_checkpoint", None)
     if checkpoint:
         fit.save(checkpoint)

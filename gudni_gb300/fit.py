@@ -151,8 +151,13 @@ class BatchFit:
             self._target = self.torch.from_numpy(t).to(self.dev)
         return self._target
 
-    def step(self) -> float:
-        """One Adam step over every scene; returns the summed loss before the step."""
+    def evaluate(self) -> float:
+        """The summed loss of the current scenes (no update)."""
+        return self._forward()[-1]
+
+    def _forward(self):
+        """Serialize, upload and run every scene's forward and adjoint: (frames, batch,
+        pile gradient, substance gradient, summed loss)."""
         torch = self.torch
         t0 = time.perf_counter()
         # one scene per pool thread: each serialized on its own thread (threads=1)
@@ -170,6 +175,16 @@ class BatchFit:
         d = image[:, :3] - target[:, :3]
         loss = float((d.double() * d.double()).sum())
         t3 = time.perf_counter()
+        self.timings["serialize"] += t1 - t0
+        self.timings["upload"] += t2 - t1
+        self.timings["device"] += t3 - t2
+        return frames, batch, gg, gs, loss
+
+    def step(self) -> float:
+        """One Adam step over every scene; returns the summed loss before the step."""
+        torch = self.torch
+        frames, batch, gg, gs, loss = self._forward()
+        t3 = time.perf_counter()
         dev = self.dev
         gp = pair_gradients(frames, batch.frame_geo_offsets, self.pair_start, gg)
         pairs = torch.from_numpy(np.concatenate([f.pairs for f in self.flats]).astype(np.float64)).to(dev)
@@ -184,10 +199,6 @@ class BatchFit:
         for i, f in enumerate(self.flats):
             f.pairs = pairs[self.pair_start[i]:self.pair_start[i + 1]].copy()
             f.substance_color = cols[self.sub_start[i]:self.sub_start[i + 1]].copy()
-        t4 = time.perf_counter()
-        self.timings["serialize"] += t1 - t0
-        self.timings["upload"] += t2 - t1
-        self.timings["device"] += t3 - t2
-        self.timings["update"] += t4 - t3
+        self.timings["update"] += time.perf_counter() - t3
         self.steps += 1
         return loss
