@@ -104,9 +104,12 @@ __global__ void __launch_bounds__(kAdjointBlock) adjoint_tiles_kernel(AdjointLau
   s.idx = a.idx + (size_t)slot * (size_t)a.in.max_shape;
   s.bitGrad = a.bit_grad + (size_t)slot * (size_t)a.in.max_shape;
   s.layerCap = a.in.max_shape + 1;
-  s.layer = a.layers + (size_t)slot * 2 * (size_t)s.layerCap;
-  s.front = s.layer + s.layerCap;
-  s.layerBit = a.layer_bits + (size_t)slot * (size_t)s.layerCap;
+  // layer records interleaved across the warp's lanes: lane l's k-th at [k * 32 + l]
+  s.ls = 32;
+  const size_t warpBase = (size_t)(slot & ~31u);
+  s.layer = a.layers + warpBase * 2 * (size_t)s.layerCap + lane;
+  s.front = s.layer + 32 * (size_t)s.layerCap;
+  s.layerBit = a.layer_bits + warpBase * (size_t)s.layerCap + lane;
   int status = 0;
   for (;;) {
     uint32_t k = 0;

@@ -480,8 +480,8 @@ constexpr int32_t kSolidLayer = 0x40000000;
 template <int SECTIONS>
 __device__ __forceinline__ int layersOf(const RasterInputs& in, const ShapeStack<SECTIONS>& stack,
                                         const uint32_t* shapeIdx, int px, int py, int topStart, float4* next,
-                                        float4* front, int32_t* bitOf, int cap, float4& color, bool& positional,
-                                        int& stopBit, int& status) {
+                                        float4* front, int32_t* bitOf, int cap, int ls, float4& color,
+                                        bool& positional, int& stopBit, int& status) {
   int64_t texels = 0;
   int topBit = topStart;
   float4 base = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -526,9 +526,9 @@ __device__ __forceinline__ int layersOf(const RasterInputs& in, const ShapeStack
     }
     if (shouldComposite && lastIsSet) {
       if (K >= cap) return -1;
-      next[K] = nx;
-      front[K] = base;
-      bitOf[K] = (nsolid && nbit >= 0) ? (nbit | kSolidLayer) : nbit;
+      next[K * ls] = nx;
+      front[K * ls] = base;
+      bitOf[K * ls] = (nsolid && nbit >= 0) ? (nbit | kSolidLayer) : nbit;
       positional = positional || (nbit >= 0 && !nsolid);
       ++K;
       base = composite(base, nx);
@@ -661,6 +661,7 @@ struct AdjSlot {
   int32_t* layerBit;
   int cap;
   int layerCap;
+  int ls;  // element stride of layer, front and layerBit: 32 on the device (a warp's lanes interleaved), 1 on a host
 };
 
 // The scan of K:1744-2028 with provenance.  grad == true (the kernel's second pass):
@@ -691,14 +692,37 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
   // of the next at the same mid-height, so its two contributions are summed
   // (pendCoef) and applied once.
   float gY0 = 0.0f, gY1 = 0.0f, pendCoef = 0.0f;
-  auto flushChain = [&]() {
-    if (grad && chainArea != 0.0f && K > 0) {
+  // The chain's reverse pass is linear in the gradient of its result, so a pixel's
+  // share (dL/dI times the area its sections took under this layer list, over the
+  // pixel area) is folded into dP when the pixel ends, and the chain runs once per
+  // layer list, when the list changes or the scan ends.
+  float dP0 = 0.0f, dP1 = 0.0f, dP2 = 0.0f;
+  auto foldPixel = [&]() {
+    if (grad && chainArea != 0.0f) {
       const float w = chainArea * invA;
-      float4 d = make_float4(gI[0] * w, gI[1] * w, gI[2] * w, 0.0f);
-      for (int k = K - 1; k >= 0; --k) {
+      dP0 += gI[0] * w;
+      dP1 += gI[1] * w;
+      dP2 += gI[2] * w;
+    }
+    chainArea = 0.0f;
+  };
+  auto flushChain = [&]() {
+    foldPixel();
+    if (grad && K > 0 && (dP0 != 0.0f || dP1 != 0.0f || dP2 != 0.0f)) {
+      float4 d = make_float4(dP0, dP1, dP2, 0.0f);
+      // The lanes flushing together walk their chains at the same depth k (a lane
+      // idles above its own K), so their reads of the interleaved layer records share
+      // lines.
+#ifdef __CUDA_ARCH__
+      const int kTop = __reduce_max_sync(__activemask(), K);
+#else
+      const int kTop = K;
+#endif
+      for (int k = kTop - 1; k >= 0; --k) {
+        if (k >= K) continue;
         float4 df, db;
-        compositeAdjoint(s.front[k], s.layer[k], d, df, db);
-        const int32_t lb = s.layerBit[k];
+        compositeAdjoint(s.front[k * s.ls], s.layer[k * s.ls], d, df, db);
+        const int32_t lb = s.layerBit[k * s.ls];
         if (lb >= 0 && (lb & kSolidLayer)) {
           float4& bg = s.bitGrad[lb & ~kSolidLayer];
           bg.x += db.x;
@@ -709,7 +733,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
         d = df;
       }
     }
-    chainArea = 0.0f;
+    dP0 = dP1 = dP2 = 0.0f;
   };
   // The rows and the sections of a row run as one loop (as in the forward scan,
   // renderColumnT): a step is the next section of the row or, once the row is
@@ -846,7 +870,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       srcX1 = nextXSrc;
       if (!colorOk || stack.hiFlip >= colorStop) {
         flushChain();
-        K = layersOf<SECTIONS>(in, stack, s.idx, px, py, bits, s.layer, s.front, s.layerBit, s.layerCap, col,
+        K = layersOf<SECTIONS>(in, stack, s.idx, px, py, bits, s.layer, s.front, s.layerBit, s.layerCap, s.ls, col,
                                colorPositional, colorStop, status);
         if (K < 0) {
           status |= kStatusIterLimit;
@@ -885,7 +909,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       if (current < numActive) stack.pass(q.hdr[q.start + current]);
       current += 1;
     } else {
-      flushChain();  // dL/dI changes with the pixel
+      foldPixel();  // dL/dI changes with the pixel
       if (grad) {  // the row's last band
         addY(s.lineGrad, srcY0, gY0);
         addY(s.lineGrad, srcY1, gY1);
@@ -901,6 +925,7 @@ __device__ __forceinline__ void scanP(const RasterInputs& in, const ColumnState&
       if (pixelY <= c.floatHeight) rowStart();
     }
   }
+  flushChain();  // the last layer list
 }
 
 // The forward scan (renderColumn, writing the float image) of a sorted queue.

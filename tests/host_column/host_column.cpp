@@ -319,6 +319,7 @@ static int adjoint_all(const gudni::RasterInputs& in, const gudni_tile_info* til
   s.layerBit = layerBits.data();
   s.cap = cap;
   s.layerCap = layerCap;
+  s.ls = 1;
   const float* pile = reinterpret_cast<const float*>(in.geometry);
   int status = 0;
   for (int t = 0; t < n_tiles; ++t) {
