@@ -732,7 +732,9 @@ def run_scene(args):
     return 0
 
 
-FIT_SPEC = dict(max_tile_size=32, threads_per_tile=256, max_thresholds=4096, max_shape=255,
+# 16x16 tiles of 64 threads (4-row column slices): of (32, 256), (16, 64) and (16, 128),
+# the fastest fitting step on GB300 (1.68 s against 1.76 s and 2.02 s)
+FIT_SPEC = dict(max_tile_size=16, threads_per_tile=64, max_thresholds=4096, max_shape=255,
                 max_strands_per_tile=1 << 24)
 
 
