@@ -162,3 +162,31 @@ def test_batch_fit_reduces_loss():
     finally:
         fit.close()
     assert last < 0.8 * first, (first, last)
+
+
+def test_batch_fit_resumes_from_a_checkpoint(tmp_path):
+    """BatchFit.save / load on the GPU: a fit continued in a new BatchFit from a
+    checkpoint sees the same scenes as the fit that wrote it (the same loss, bit for
+    bit: the forward image is deterministic) and takes the same step count."""
+    from gudni_gb300 import fit as Fm
+    spec = L.make_spec(16, 32, 4096, 127, 8, max_strands_per_tile=1 << 24)
+    make = lambda i: G.random_shapes(seed=80 + i, width=48, height=40, n_shapes=8)  # noqa: E731
+    targets = [O.render_float(S.serialize_flat(jitter(make(i), 2.0, 90 + i), spec)) for i in range(3)]
+    path = str(tmp_path / "fit.npz")
+    a = Fm.BatchFit([make(i) for i in range(3)], targets, spec, lr_points=0.3, lr_colors=0.01)
+    try:
+        for _ in range(3):
+            a.step()
+        a.save(path)
+        want = a.evaluate()
+    finally:
+        a.close()
+    b = Fm.BatchFit([make(i) for i in range(3)], targets, spec, lr_points=0.3, lr_colors=0.01)
+    try:
+        b.load(path)
+        assert b.steps == 3
+        assert b.evaluate() == want
+        b.step()
+        assert b.steps == 4
+    finally:
+        b.close()
