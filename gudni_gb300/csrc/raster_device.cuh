@@ -475,17 +475,22 @@ __device__ __forceinline__ void strandThresholds(G& g, const uint8_t* strand, ui
 }
 
 // buildThresholdArray K:1540-1595 with traverseTree K:1378-1408.
-// Returns the number of shape bits assigned; shape indices go to `shapeIdx`.
+// Returns the number of shape bits assigned; shape indices go to `shapeIdx`.  With
+// `nAsBit` (a tile of at most max_shape shapes, so no column runs out of bits) a
+// shape's bit is its number n in the tile instead of the running count: the bits keep
+// the shapes' order, so the colour walk meets the same shapes in the same order, and
+// a tag is read straight from the tile's shape records (DirectTags).
 template <int SECTIONS>
 __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, const ColumnState& c, Queue& q,
                                                     ShapeStack<SECTIONS>& stack, uint32_t* shapeIdx,
-                                                    int& status) {
+                                                    int& status, bool nAsBit = false) {
   GenState g{&q, &c};
   const float2 d = make_float2((float)c.deltaX, (float)c.deltaY);
   uint32_t shapeBits = 0;
   for (int n = 0; n < c.numShapes && (int)shapeBits < in.max_shape; ++n) {
     const uint32_t shapeIndex = c.shapeStart + (uint32_t)n;
     const gudni_shape shape = in.shapes[shapeIndex];
+    const uint32_t bit = nAsBit ? (uint32_t)n : shapeBits;
     bool added = false;
     bool enclosedByShape = false;
     uint32_t first = kNoStrand;
@@ -508,7 +513,7 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
         if (yr.x - d.y >= c.floatHeight + 1.0f) continue;
         const bool above = yr.y - d.y <= -1.0f;
         bool enclosedByStrand = false;
-        strandThresholds(g, in.geometry + (size_t)e.x * 8, e.y, d, shapeBits, added, enclosedByStrand, status,
+        strandThresholds(g, in.geometry + (size_t)e.x * 8, e.y, d, bit, added, enclosedByStrand, status,
                          above);
         if (q.overflow) return shapeBits;
         enclosedByShape = enclosedByShape != enclosedByStrand;
@@ -529,15 +534,15 @@ __device__ __forceinline__ uint32_t buildThresholds(const RasterInputs& in, cons
           break;
         }
         bool enclosedByStrand = false;
-        strandThresholds(g, strand, size, d, shapeBits, added, enclosedByStrand, status);
+        strandThresholds(g, strand, size, d, bit, added, enclosedByStrand, status);
         if (q.overflow) return shapeBits;
         off += (size_t)size * 8;
         enclosedByShape = enclosedByShape != enclosedByStrand;
       }
     }
-    if (enclosedByShape) stack.flip(shapeBits);
+    if (enclosedByShape) stack.flip(bit);
     if (added || enclosedByShape) {
-      shapeIdx[shapeBits] = shapeIndex;
+      if (!nAsBit) shapeIdx[shapeBits] = shapeIndex;
       shapeBits += 1;
     }
   }
@@ -1208,14 +1213,26 @@ __device__ __forceinline__ bool runColumn(const RasterInputs& in, const gudni_ti
   Queue q{thr, hdr, cap, cap, false};
   ShapeStack<SECTIONS> stack;
   stack.clear();
-  const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, idx, status);
+  // a tile of at most 64 shapes (and no more than max_shape): its shape numbers are
+  // the bits, one stack word holds them, and the colour walk reads each tag from the
+  // tile's records, which the warp's lanes share, instead of through the per-lane
+  // index
+  const bool direct = c.numShapes <= 64 && c.numShapes <= in.max_shape;
+  const uint32_t bits = buildThresholds<SECTIONS>(in, c, q, stack, idx, status, direct);
   if (q.overflow) return true;
   sortQueue(q);
   if (in.counters) {
     atomicAdd(reinterpret_cast<unsigned long long*>(&in.counters[2]), (unsigned long long)q.length());
     atomicMax(reinterpret_cast<unsigned long long*>(&in.counters[3]), (unsigned long long)bits);
   }
-  if (SECTIONS > 1 && bits <= 64) {
+  if (direct) {
+    ShapeStack<1> one;
+    one.clear();
+    one.w[0] = stack.word(0);
+    one.nz = one.w[0] ? 1u : 0u;
+    renderColumnT<1, kCounterJitter>(in, c, q, one, DirectTags{in.shapes + c.shapeStart}, status, c.numShapes,
+                                     nullptr, nullptr);
+  } else if (SECTIONS > 1 && bits <= 64) {
     // every shape bit of the column sits in the first stack word: scan with a
     // one-word stack (flips and findTop on a single register)
     ShapeStack<1> one;

@@ -87,7 +87,8 @@ def test_adjoint_generated_once_equals_regenerated(name):
     """The default adjoint (thresholds generated once per work unit, the forward
     scanning a copy) against gudni_set_adjoint_regenerate(ctx, 1) (the forward's own
     raster generation, the backward's second generation): the same float image bit
-    for bit, and the same gradients up to the order of the atomic adds."""
+    for bit, and the same gradients up to the order of the atomic adds (float sums in
+    another order: relative 1e-4 of an entry, or 1e-6 of the largest entry)."""
     if name == "dense":
         spec = L.make_spec(16, 64, 4096, 255, 4, max_strands_per_tile=1 << 24)
         frame, target = case(lambda: G.random_shapes(seed=93, width=128, height=128, n_shapes=120), spec=spec)
@@ -100,8 +101,8 @@ def test_adjoint_generated_once_equals_regenerated(name):
         r.set_adjoint_regenerate(True)
         _, i2, g2, s2 = fa.loss_and_gradient(target)
         np.testing.assert_array_equal(i2.cpu().numpy(), i1)
-        np.testing.assert_allclose(g2.cpu().numpy(), g1, rtol=1e-5, atol=1e-6)
-        np.testing.assert_allclose(s2.cpu().numpy(), s1, rtol=1e-5, atol=1e-6)
+        for got, want in ((g2.cpu().numpy(), g1), (s2.cpu().numpy(), s1)):
+            np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-6 * float(np.abs(want).max()))
 
 
 def test_adjoint_threads_per_tile():
