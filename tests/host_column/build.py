@@ -17,7 +17,9 @@ CUDA_INCLUDE = "/usr/local/cuda/include"
 def build() -> str:
     if not os.path.isfile(OUT) or max(os.path.getmtime(d) for d in DEPS) > os.path.getmtime(OUT):
         os.makedirs(os.path.dirname(OUT), exist_ok=True)
-        subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-strict-aliasing", "-fPIC", "-shared",
+        # -O1: the same IEEE results as -O2 (no contraction, no fast math) from a
+        # compile that takes a third of the time
+        subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-strict-aliasing", "-fPIC", "-shared",
                         "-w", "-pthread", "-I", CUDA_INCLUDE, "-I", os.path.join(ROOT, "include"), SRC, "-o", OUT], check=True)
     return OUT
 
