@@ -65,6 +65,22 @@ def test_dense_canvas_wide_shapes(tile, tpt):
     check(S.serialize_flat(flat, L.make_spec(tile, tpt, 4096, 255, 4, max_strands_per_tile=1 << 24)))
 
 
+@pytest.mark.parametrize("n_shapes,max_shape", [(64, 127), (65, 127), (31, 31), (32, 31), (40, 63)])
+def test_shape_numbers_as_bits_at_the_limits(n_shapes, max_shape):
+    """One 32x32 tile of canvas-wide shapes at the limits of the per-column kernel's
+    shape numbering: a tile of at most 64 shapes and no more than max_shape numbers its
+    shapes' bits by their place in the tile (64 shapes: bit 63 in use), one more shape
+    (65), or a tile above max_shape (32 shapes, max_shape 31: the reference drops the
+    shapes past max_shape bits), takes the per-column bit index; the image is the
+    oracle's either way."""
+    flat = G.random_shapes(seed=100 + n_shapes, width=32, height=32, n_shapes=n_shapes, seg_lo=4, seg_hi=8)
+    sections = 1 if max_shape < 64 else 2
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, max_shape, sections, max_strands_per_tile=1 << 24))
+    tiles = np.concatenate([j.tiles for j in frame.jobs])
+    assert tiles["shape_length"].max() == n_shapes
+    check(frame)
+
+
 def test_very_dense_small_canvas():
     """The batched mix's densest corner: a small canvas crossed by many shapes."""
     flat = G.random_shapes(seed=9, width=48, height=40, n_shapes=300, seg_lo=8, seg_hi=32)
