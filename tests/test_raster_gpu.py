@@ -117,6 +117,19 @@ def test_empty_scene_is_background():
     assert (r, g, b) == (51, 102, 153)
 
 
+@pytest.mark.parametrize("n_shapes,max_shape", [(64, 127), (65, 127), (31, 31), (32, 31)])
+def test_shape_numbers_as_bits_at_the_limits(n_shapes, max_shape):
+    """One 32x32 tile of canvas-wide shapes at the limits of the per-column kernel's
+    shape numbering (a tile of at most 64 shapes and no more than max_shape numbers its
+    shapes' bits by their place in the tile; 65 shapes, or more than max_shape, take the
+    per-column bit index): the oracle's image, bit for bit."""
+    flat = G.random_shapes(seed=100 + n_shapes, width=32, height=32, n_shapes=n_shapes, seg_lo=4, seg_hi=8)
+    sections = 1 if max_shape < 64 else 2
+    frame = S.serialize_flat(flat, L.make_spec(32, 32, 4096, max_shape, sections, max_strands_per_tile=1 << 24))
+    assert np.concatenate([j.tiles for j in frame.jobs])["shape_length"].max() == n_shapes
+    assert np.array_equal(render(frame), O.render_frame(frame))
+
+
 def test_one_pixel_canvas():
     frame = F.build("tiny_square")
     tiny = S.serialize(F.tiny_square(), 1, 1, frame.spec)
